@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the reconstruction path on one workload.
+
+Default workload (rytov_1024): 600 synthetic off-axis holograms, 1024 x 1024
+uint16 (12-bit), NXMAX 128 (256 x 256 fields), Rytov fields with Volkov
+unwrapping and aberration correction, mapped into a 512^3 spectrum and
+inverted.  One step reconstructs one volume from its 600 holograms.
+
+  value  volumes/s with the holograms already in HBM (device buffers)
+  e2e    volumes/s through the C ABI with pinned host holograms and host
+         outputs (index, absorption, OTF mask), copies inside the timed region
+
+Multi-GPU (torchrun): independent replicas, one volume per rank per step,
+no data-path collective; value is the whole-job volumes/s.
+
+--impl reference times the FP64 CPU restatement of the reference (the
+reference programs cannot be built here: FFTW3/OpenCV/libtiff are absent) on
+the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "512³ volumes/s (600 holos): plain vs batched/TV-adjoint; rel-L2≤1e-4 vs FP64"
+UNIT = "volumes/s"
+
+# Algorithmic bytes per launch unit (compulsory input + output of the kernel):
+# see DESIGN.md, section "Roofline".
+def algorithmic_bytes(name, acq, hits_per_angle):
+    H, F, D = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final
+    L = 2 * F
+    per_angle = {
+        "extract_rows": H * H * 2 + H * F * 8,
+        "extract_cols": H * F * 8 + F * F * 8,
+        "argmax": F * F * 8,
+        "field_rows": F * F * 8 * 2,
+        "field_cols": F * F * 8 + F * F * 4 * 2,
+        "volkov_rows": F * F * 4 + L * L * 4,
+        "volkov_cols": F * F * 4 + L * L * 4 + L * L * 8,
+        "volkov_integ_rows": L * L * 8 + L * F * 8,
+        "volkov_integ_cols": L * F * 8 + F * F * 4 * 2,
+        "aber_fit": 2 * F * F * 4,
+        "form": 3 * F * F * 4 + F * F * 8,
+        "cap_rows": 2 * F * F * 8,
+        "cap_cols": F * F * 8 + F * F * 10,
+    }
+    per_volume = {
+        "gather": hits_per_angle * acq.nb_holo * 10 + D ** 3 * 8 + D ** 3,
+        "ypass": 2 * D ** 3 * 8,
+        "xpass": D ** 3 * 8 + 2 * D ** 3 * 4,
+    }
+    return per_angle, per_volume
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(acq, ph, seed, sample_angles: int, threads: int):
+    """FP64 oracle on a bounded sample: `sample_angles` holograms through
+    extraction, field formation and cap mapping, plus one full volume stage;
+    extrapolated to the workload's angle count."""
+    import numpy as np
+
+    import oracle
+    from mtd_transmission_gb300 import simul
+    from tests.helpers import oracle_cfg
+    oracle.set_threads(threads)
+    cfg = oracle_cfg(acq)
+    d = simul.holograms(acq, ph, M=sample_angles, seed=seed)
+    holos = d["holos"].numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    spec = oracle.extract_stack(holos, cfg)
+    t1 = time.perf_counter()
+    fields, pos = oracle.fields(spec, cfg, d["mask"].numpy())
+    t2 = time.perf_counter()
+    r = oracle.reconstruction(fields, pos, cfg, want_counts=False, want_otf=False)
+    loop_s, vol_s = float(r["seconds"][0]), float(r["seconds"][1])
+    per_angle = (t1 - t0 + t2 - t1 + loop_s) / sample_angles
+    total = per_angle * acq.nb_holo + vol_s
+    return {"per_angle_s": per_angle, "volume_s": vol_s, "seconds_per_volume": total,
+            "sample_wall_s": time.perf_counter() - t0}
+
+
+def run_reference(args, acq, ph, seed):
+    threads = os.cpu_count() or 1
+    import oracle
+    from mtd_transmission_gb300 import simul  # noqa: F401
+    oracle.build()
+    S = args.ref_sample
+    # warm-up steps include the one-off volume stage measurement
+    vol_s = None
+    per = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(acq, ph, seed + i, S, threads)
+        if vol_s is None:
+            vol_s = r["volume_s"]
+        if i >= args.warmup:
+            per.append(r["per_angle_s"])
+    per_angle = statistics.mean(per)
+    spv = per_angle * acq.nb_holo + vol_s
+    value = 1.0 / spv
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": spv * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(acq, args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step: {S} of {acq.nb_holo} holograms through extraction, fields and cap "
+                                   f"mapping, extrapolated per angle; volume stage (normalise, shifts, "
+                                   f"{acq.dim_final}^3 FP64 3D FFT) timed once in warm-up ({vol_s:.1f} s)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config(acq, args):
+    return {"workload": f"{args.workload}: {acq.nb_holo} x {acq.ccd_roix}^2 uint16 12-bit holograms, "
+                        f"NXMAX {acq.nxmax} ({2 * acq.nxmax}^2 fields), {'Born' if acq.born else 'Rytov'}, "
+                        f"Volkov + aberration correction, {acq.dim_final}^3 volume",
+            "holograms": acq.nb_holo, "hologram_px": acq.ccd_roix, "field_px": 2 * acq.nxmax,
+            "volume": acq.dim_final, "parallelism": f"replicas x{args.gpus}",
+            "l2": "inputs larger than L2: 1.26 GB of holograms per step (no flush needed)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rytov_1024")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=12)
+    ap.add_argument("--ref-sample", type=int, default=8)
+    ap.add_argument("--profile-out", default=None)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from mtd_transmission_gb300 import simul
+    acq, ph, seed = simul.workload(args.workload)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, acq, ph, seed)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from mtd_transmission_gb300 import Context, Geometry
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # synthetic stack on the device (seeded per rank)
+    data = simul.holograms(acq, ph, seed=seed + rank, device="cuda")
+    holos = data["holos"].contiguous()
+    mask = np.ascontiguousarray(data["mask"].cpu().numpy())
+    del data
+    torch.cuda.empty_cache()
+    M, D = acq.nb_holo, acq.dim_final
+    ctx = Context(Geometry.from_acquisition(acq), M)
+    ctx.set_mask(mask)
+    re = torch.empty((D, D, D), dtype=torch.float32, device="cuda")
+    im = torch.empty_like(re)
+    otf = torch.empty((D, D, D), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    for _ in range(args.warmup):
+        ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+    ctx.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+
+    # timed region: K steps, device-resident inputs
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = ctx.launch_count
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+    ev1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = ctx.launch_count - launches0
+    clocks = sampler.stop()
+    # per-kernel device times: the same K steps again with CUDA events around every launch
+    ctx.profile(True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+    ev1.record(stream)
+    ctx.synchronize()
+    prof_ms = ev0.elapsed_time(ev1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    t_max = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    ms_max = float(t_max.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # end to end: pinned host holograms and outputs through the C ABI
+    h_holos = torch.empty(holos.shape, dtype=holos.dtype, pin_memory=True)
+    h_holos.copy_(holos)
+    h_re = torch.empty((D, D, D), dtype=torch.float32, pin_memory=True)
+    h_im = torch.empty((D, D, D), dtype=torch.float32, pin_memory=True)
+    h_otf = torch.empty((D, D, D), dtype=torch.uint8, pin_memory=True)
+    ctx.pipeline(h_holos, indice=h_re, absorption=h_im, otf=h_otf)  # warm-up of the host path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        ctx.pipeline(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
+    e2e_s = time.perf_counter() - t0
+    t_e = torch.tensor([e2e_s], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
+    e2e_value = world * args.e2e_steps / float(t_e.item())
+    h2d = int(h_holos.numel() * h_holos.element_size())
+    d2h = int(2 * D ** 3 * 4 + D ** 3)
+
+    if rank == 0:
+        # roofline of the dominant kernel
+        hits = float((np.arange(-acq.nxmax, acq.nxmax)[:, None] ** 2 +
+                      np.arange(-acq.nxmax, acq.nxmax)[None, :] ** 2 < acq.nxmax ** 2).sum())
+        per_angle, per_volume = algorithmic_bytes(None, acq, hits)
+        peak, peak_kind = measured_peaks()
+        kern = {k: (t / args.steps, n / args.steps) for k, (t, n) in prof.items()}
+        dom = max(kern, key=lambda k: kern[k][0]) if kern else None
+        roof = None
+        if dom:
+            t_step_ms, n_launch = kern[dom]
+            if dom in per_angle:
+                bytes_step = per_angle[dom] * M
+            else:
+                bytes_step = per_volume.get(dom, 0)
+            achieved = bytes_step / (t_step_ms / 1e3) / 1e9
+            roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": None,
+                    "peak_source": f"{peak_kind} hbm_gbs",
+                    "launches_per_step": n_launch, "ms_per_step": round(t_step_ms, 4),
+                    "algorithmic_bytes_per_step": int(bytes_step)}
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            r = cpu_baseline(acq, ph, seed, args.cpu_sample, threads)
+            cpu = {"value": 1.0 / r["seconds_per_volume"], "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_sample} of {acq.nb_holo} holograms through extraction, fields and cap "
+                             f"mapping ({r['per_angle_s']:.3f} s/angle), extrapolated, plus one full "
+                             f"{acq.dim_final}^3 volume stage ({r['volume_s']:.1f} s)"}
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(acq, args),
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][0])},
+            "profiled_ms_per_step": round(prof_ms / args.steps, 3),
+        }
+        if args.profile_out:
+            with open(args.profile_out, "w") as f:
+                json.dump(line, f, indent=1)
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,183 @@
+/*
+ * tdm.h — C ABI of the GB300 tomographic diffractive microscopy hot path.
+ *
+ * Drop-in for the two batch programs of madeba/MTD_transmission:
+ *   tomo_pretraitement   (Tomo_prog/pretraitement_hors_axe_CPU/main.cpp)
+ *   tomo_reconstruction  (Tomo_prog/Reconstruction/main.cpp)
+ * The reference has no library interface; these entry points are its
+ * function-level seams, each citing the reference code it replaces.  The
+ * executables tomo_pretraitement / tomo_reconstruction / tomo_pipeline built
+ * from this library keep the reference's file contracts.
+ *
+ * Conventions
+ *  - Every pointer argument may be host memory (pageable or pinned) or device
+ *    memory of the context's GPU; the library detects which.  Calls whose
+ *    buffers are all device memory are asynchronous on the context's stream
+ *    (tdm_stream); calls that touch host memory return after the results are
+ *    in host memory.
+ *  - Complex arrays are interleaved float pairs (re, im), row-major with x
+ *    fastest, as the reference's std::vector<std::complex<double>> with
+ *    cpt = x + y*dim (+ z*dim*dim).
+ *  - posspec arrays hold n x-coordinates followed by n y-coordinates (the
+ *    layout of tab_posSpec.raw, main.cpp:250-251), as int32.
+ *  - Return value: TDM_OK (0) or a negative TDM_E* status; tdm_last_error()
+ *    gives the message.  One context per host thread.
+ */
+#ifndef TDM_H
+#define TDM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDM_OK 0
+#define TDM_EINVAL -1       /* invalid argument */
+#define TDM_EUNSUPPORTED -2 /* geometry outside what the kernels support */
+#define TDM_ECUDA -3        /* CUDA runtime error */
+#define TDM_ENOMEM -4       /* device allocation failed */
+#define TDM_EDATA -5        /* data error (fit undefined, cap voxel outside the volume) */
+#define TDM_EIO -6          /* file input/output error */
+
+typedef struct tdm_ctx tdm_ctx;
+
+/* Acquisition and reconstruction parameters: the keys of recon.txt and
+ * config_manip.txt that the path reads (pretraitement_hors_axe_CPU/manip.cpp:32-104,
+ * Reconstruction/src/manip.cpp:44-94).  Real-valued keys carry the value the
+ * reference's extract_val returns, i.e. rounded to float
+ * (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:81-118). */
+typedef struct {
+    int ccd_roix;       /* CCD_ROIX: hologram side H (power of two, 256..2048) */
+    int nxmax;          /* NXMAX: N; fields are F = 2N square (F power of two, 64..512) */
+    int circle_cx;      /* CIRCLE_CX: +1 order centre in the fftshifted hologram spectrum */
+    int circle_cy;      /* CIRCLE_CY */
+    int dim_final;      /* DIM_FINAL: D, volume side (power of two, >= 4N, <= 1024) */
+    int born;           /* BORN: 1 Born, 0 Rytov */
+    int c_aber;         /* C_ABER: aberration correction (and unwrapping) on/off */
+    int deroul;         /* DEROUL: phase unwrapping on/off (only with C_ABER) */
+    int volkov;         /* VOLKOV: 1 Volkov; 0 (Herraez) is not supported */
+    double na;          /* NA */
+    double n0;          /* N0 */
+    double lambda0;     /* LAMBDA (m) */
+    double f_tube;      /* F_TUBE (m) */
+    double f_obj;       /* F_OBJ (m) */
+    double tpcam;       /* TPCAM (m) */
+    double rf;          /* RF */
+    double coef_na_obj_limit; /* COEF_NA_OBJ_LIMIT (recon.txt, default 1) */
+} tdm_geom;
+
+/* Derived quantities (pretraitement_hors_axe_CPU/manip.cpp:43-57,104;
+ * Reconstruction/src/manip.cpp:64-94). */
+typedef struct {
+    double rayon;       /* Ewald radius in spectrum pixels, round(NXMAX*n0/NA) */
+    double tp_holo;     /* tailleTheoPixelHolo (m) */
+    double tp_uborn;    /* tailleTheoPixelUborn (m) */
+    double tp_tomo;     /* tailleTheoPixelTomo (m) */
+    double delta_f;     /* Delta_fUborn (1/m) */
+} tdm_derived;
+
+/* Creates a context on the current CUDA device for stacks of up to
+ * max_angles holograms.  Replaces the FFTW plan set-up of both programs
+ * (pretraitement_hors_axe_CPU/main.cpp:91-105,180-189; Reconstruction/main.cpp:131,185,318). */
+int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out);
+int tdm_destroy(tdm_ctx* ctx);
+const char* tdm_last_error(const tdm_ctx* ctx);
+int tdm_get_derived(const tdm_ctx* ctx, tdm_derived* out);
+/* Derived quantities without a context (host arithmetic only). */
+int tdm_derive(const tdm_geom* geom, tdm_derived* out);
+
+/* Aberration mask, F*F uint8 (Image_mask.pgm); NULL selects the unit mask.
+ * Replaces init_mask_aber, countM, initCorrAber
+ * (pretraitement_hors_axe_CPU/Correction_aberration.cpp:36-149; main.cpp:192-208). */
+int tdm_set_mask(tdm_ctx* ctx, const uint8_t* mask);
+
+/* Off-axis extraction of n holograms (H*H samples each, uint8 when bits == 8,
+ * uint16 when bits == 16) into the context's spectrum stack; the F*F crops
+ * are also copied to spectra_out (n*F*F complex) when it is not NULL.
+ * Replaces holo2TF_UBorn (pretraitement_hors_axe_CPU/fonctions.cpp:279-304)
+ * called from main.cpp:130-165. */
+int tdm_extract(tdm_ctx* ctx, const void* holos, int bits, int n, float* spectra_out);
+
+/* Field formation for n spectra: specular search, recentring and inverse FFT,
+ * phase, Volkov unwrapping, aberration fits, Born/Rytov.  spectra_in NULL
+ * uses the context's stack (from tdm_extract).  fields_out (n*F*F complex,
+ * UBornFinal) and posspec_out (2n int32) may be NULL.
+ * Replaces the second loop of tomo_pretraitement (pretraitement_hors_axe_CPU/main.cpp:230-342):
+ * coordSpec (fonctions.cpp:88-101), calc_Uborn2 (:348-374),
+ * calcPhase_mpi_pi_atan2 (:39-43), deroul_volkov4_total_sym_paire
+ * (src/deroulement_volkov4.cpp:14-92), aberCorr2/ampliCorr2
+ * (Correction_aberration.cpp:166-184). */
+int tdm_fields(tdm_ctx* ctx, const float* spectra_in, int n, float* fields_out, int32_t* posspec_out);
+
+/* Same as tdm_fields, also returning per-angle intermediates (each n*F*F
+ * float, any may be NULL): wrapped phase, unwrapped phase, amplitude. */
+int tdm_fields_debug(tdm_ctx* ctx, const float* spectra_in, int n, float* fields_out, int32_t* posspec_out,
+                     float* phase_out, float* unwrapped_out, float* amp_out);
+
+/* Reconstruction of the D^3 volume from n fields: per-field window, FFT and
+ * shift, Ewald-cap mapping with hit counts, normalisation, OTF mask, 3D
+ * inverse FFT and index conversion.  fields_in / posspec_in NULL use the
+ * context's results of tdm_fields.  Outputs (D^3 each, index x + y*D + z*D*D,
+ * any may be NULL): indice (real part, indice.tif), absorption (imaginary
+ * part, absorption.tif), otf (OTF3D mask, 0/1), counts (sup_redon before its
+ * zeros are replaced).
+ * Replaces Reconstruction/main.cpp:203-352: decal2DCplxGen
+ * (src/fonctions.cpp:1268-1309), TF2Dcplx (src/FFT_fonctions.cpp:333-349),
+ * retroPropag_Born (src/fonctions.cpp:875-935), fftshift3D
+ * (src/FFT_fonctions.cpp:78-151), TF3Dcplx_INV (:394-412). */
+int tdm_reconstruct(tdm_ctx* ctx, const float* fields_in, const int32_t* posspec_in, int n, float* indice_out,
+                    float* absorption_out, uint8_t* otf_out, uint32_t* counts_out);
+
+/* Holograms to volume in one call, fields kept on the device (tomo_pipeline).
+ * Equivalent to tdm_extract + tdm_fields + tdm_reconstruct. */
+int tdm_pipeline(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                 uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out);
+
+/* Stream-ordered execution helpers. */
+int tdm_synchronize(tdm_ctx* ctx);
+void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */
+uint64_t tdm_launch_count(const tdm_ctx* ctx); /* kernels launched so far */
+/* Device-side elapsed time of the last tdm_* call's dominant kernel group
+ * (milliseconds per stage) for profiling: names are "extract", "fields",
+ * "map", "volume"; returns a negative value for an unknown name. */
+double tdm_stage_ms(const tdm_ctx* ctx, const char* stage);
+
+/* Opt-in per-kernel timing: when enabled, every kernel launch is bracketed by
+ * a pair of CUDA events on the context stream.  tdm_profile() clears the
+ * records; tdm_profile_read() waits for the stream and returns, for kernel
+ * index 0 <= index < tdm_profile_count(), its name, the summed device time
+ * and the number of launches since the last tdm_profile() call. */
+int tdm_profile(tdm_ctx* ctx, int enable);
+int tdm_profile_count(void);
+int tdm_profile_read(tdm_ctx* ctx, int index, const char** name, double* total_ms, int* launches);
+
+/* ---- Host-side file contract helpers (executables and tests) ---- */
+
+/* extract_val: value of a KEY in a whitespace "KEY value" file, last
+ * occurrence wins, '#' comment lines, float-rounded; def when absent
+ * (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:81-118,
+ * Reconstruction/src/fonctions.cpp:137-180).  Returns 1 when found, 0 when
+ * absent, TDM_EIO when the file cannot be opened. */
+int tdm_extract_val(const char* path, const char* key, double def, double* out);
+/* extract_string (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:44-79). */
+int tdm_extract_string(const char* path, const char* key, char* out, size_t cap);
+/* Fills a tdm_geom from recon.txt and config_manip.txt. */
+int tdm_read_geom(const char* recon_txt, const char* config_manip_txt, tdm_geom* out);
+/* Binary PGM (P5) reader, 8- or 16-bit (16-bit samples are big-endian in the
+ * file).  Replaces charger_image2D_OCV (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:24-40)
+ * with native sample depth: *bits is set to 8 or 16; the ROI is the top-left
+ * roi x roi corner.  buf receives roi*roi samples (uint8 or uint16). */
+int tdm_read_pgm(const char* path, int roi, void* buf, int* bits);
+int tdm_pgm_info(const char* path, int* width, int* height, int* maxval);
+/* Float32 multi-page TIFF writer (SAV3D_Tiff_Optimized,
+ * Reconstruction/src/fonctions.cpp:2286-2357): D pages of D x D, ORIENTATION_BOTLEFT,
+ * resolution 0.01/pixel_size per cm. */
+int tdm_write_tiff_f32(const char* path, const float* vol, int dim_x, int dim_y, int pages, double pixel_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDM_H */

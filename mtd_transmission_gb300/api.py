@@ -1,0 +1,280 @@
+"""Python mirror of the C ABI in include/tdm.h (ctypes over libtdm.so).
+
+The library is the product: every call goes to the sm_103a kernels.  There is
+no CPU fallback; importing works without a GPU, but creating a context needs
+the CUDA device and a built libtdm.so (``mtd_transmission_gb300.build``).
+
+Array arguments may be numpy arrays (host memory) or contiguous torch tensors
+(host or CUDA memory); the library detects device pointers itself.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtdm.so")
+
+TDM_OK = 0
+STATUS = {-1: "TDM_EINVAL", -2: "TDM_EUNSUPPORTED", -3: "TDM_ECUDA", -4: "TDM_ENOMEM", -5: "TDM_EDATA", -6: "TDM_EIO"}
+
+# Exported symbols declared in include/tdm.h.
+EXPORTS = (
+    "tdm_create", "tdm_destroy", "tdm_last_error", "tdm_get_derived", "tdm_derive", "tdm_set_mask", "tdm_extract",
+    "tdm_fields", "tdm_fields_debug", "tdm_reconstruct", "tdm_pipeline", "tdm_synchronize", "tdm_stream",
+    "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
+    "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
+)
+
+
+class TdmError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Geometry(ctypes.Structure):
+    """tdm_geom: keys of recon.txt / config_manip.txt (real keys float-rounded)."""
+    _fields_ = [
+        ("ccd_roix", ctypes.c_int), ("nxmax", ctypes.c_int), ("circle_cx", ctypes.c_int),
+        ("circle_cy", ctypes.c_int), ("dim_final", ctypes.c_int), ("born", ctypes.c_int),
+        ("c_aber", ctypes.c_int), ("deroul", ctypes.c_int), ("volkov", ctypes.c_int),
+        ("na", ctypes.c_double), ("n0", ctypes.c_double), ("lambda0", ctypes.c_double),
+        ("f_tube", ctypes.c_double), ("f_obj", ctypes.c_double), ("tpcam", ctypes.c_double),
+        ("rf", ctypes.c_double), ("coef_na_obj_limit", ctypes.c_double),
+    ]
+
+    @classmethod
+    def from_acquisition(cls, acq) -> "Geometry":
+        f = lambda v: float(np.float32(v))  # noqa: E731  extract_val returns float
+        return cls(ccd_roix=acq.ccd_roix, nxmax=acq.nxmax, circle_cx=acq.circle_cx, circle_cy=acq.circle_cy,
+                   dim_final=acq.dim_final, born=int(acq.born), c_aber=int(acq.c_aber), deroul=int(acq.deroul),
+                   volkov=int(acq.volkov), na=f(acq.na), n0=f(acq.n0), lambda0=f(acq.lambda0),
+                   f_tube=f(acq.f_tube), f_obj=f(acq.f_obj), tpcam=f(acq.tpcam), rf=f(acq.rf),
+                   coef_na_obj_limit=f(acq.coef_na_obj_limit))
+
+
+class Derived(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("rayon", "tp_holo", "tp_uborn", "tp_tomo", "delta_f")]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libtdm.so; raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m mtd_transmission_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.tdm_create.argtypes = [ctypes.POINTER(Geometry), I, ctypes.POINTER(P)]
+    L.tdm_destroy.argtypes = [P]
+    L.tdm_last_error.argtypes = [P]
+    L.tdm_last_error.restype = ctypes.c_char_p
+    L.tdm_get_derived.argtypes = [P, ctypes.POINTER(Derived)]
+    L.tdm_derive.argtypes = [ctypes.POINTER(Geometry), ctypes.POINTER(Derived)]
+    L.tdm_set_mask.argtypes = [P, P]
+    L.tdm_extract.argtypes = [P, P, I, I, P]
+    L.tdm_fields.argtypes = [P, P, I, P, P]
+    L.tdm_fields_debug.argtypes = [P, P, I, P, P, P, P, P]
+    L.tdm_reconstruct.argtypes = [P, P, P, I, P, P, P, P]
+    L.tdm_pipeline.argtypes = [P, P, I, I, P, P, P, P, P]
+    L.tdm_synchronize.argtypes = [P]
+    L.tdm_stream.argtypes = [P]
+    L.tdm_stream.restype = P
+    L.tdm_launch_count.argtypes = [P]
+    L.tdm_launch_count.restype = ctypes.c_uint64
+    L.tdm_stage_ms.argtypes = [P, ctypes.c_char_p]
+    L.tdm_stage_ms.restype = D
+    L.tdm_extract_val.argtypes = [ctypes.c_char_p, ctypes.c_char_p, D, ctypes.POINTER(D)]
+    L.tdm_extract_string.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+    L.tdm_read_geom.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(Geometry)]
+    L.tdm_read_pgm.argtypes = [ctypes.c_char_p, I, P, ctypes.POINTER(I)]
+    L.tdm_pgm_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.tdm_write_tiff_f32.argtypes = [ctypes.c_char_p, P, I, I, I, D]
+    L.tdm_profile.argtypes = [P, I]
+    L.tdm_profile_count.argtypes = []
+    L.tdm_profile_read.argtypes = [P, I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(D), ctypes.POINTER(I)]
+    _lib = L
+    return L
+
+
+def ptr(a):
+    """Address of a numpy array or contiguous torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return ctypes.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return ctypes.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def derive(geom: Geometry) -> dict:
+    d = Derived()
+    lib().tdm_derive(ctypes.byref(geom), ctypes.byref(d))
+    return {n: getattr(d, n) for n, _ in Derived._fields_}
+
+
+class Context:
+    """One reconstruction context (device buffers, tables, stream) on the current GPU."""
+
+    def __init__(self, geom: Geometry, max_angles: int):
+        self.geom = geom
+        self.max_angles = max_angles
+        h = ctypes.c_void_p()
+        rc = lib().tdm_create(ctypes.byref(geom), max_angles, ctypes.byref(h))
+        if rc != TDM_OK:
+            raise TdmError(rc, "tdm_create failed")
+        self._h = h
+        self.F = 2 * geom.nxmax
+        self.D = geom.dim_final
+
+    def _check(self, rc: int, what: str):
+        if rc != TDM_OK:
+            raise TdmError(rc, f"{what}: {lib().tdm_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tdm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        return int(lib().tdm_stream(self._h) or 0)
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib().tdm_launch_count(self._h))
+
+    def stage_ms(self, name: str) -> float:
+        return float(lib().tdm_stage_ms(self._h, name.encode()))
+
+    def profile(self, enable: bool = True):
+        """Starts (or stops) per-kernel event timing; clears previous records."""
+        self._check(lib().tdm_profile(self._h, int(enable)), "tdm_profile")
+
+    def profile_read(self) -> dict:
+        """{kernel name: (total device ms, launches)} since the last profile() call."""
+        out = {}
+        for i in range(lib().tdm_profile_count()):
+            nm, t, n = ctypes.c_char_p(), ctypes.c_double(), ctypes.c_int()
+            self._check(lib().tdm_profile_read(self._h, i, ctypes.byref(nm), ctypes.byref(t), ctypes.byref(n)),
+                        "tdm_profile_read")
+            if n.value:
+                out[nm.value.decode()] = (t.value, n.value)
+        return out
+
+    def derived(self) -> dict:
+        d = Derived()
+        self._check(lib().tdm_get_derived(self._h, ctypes.byref(d)), "tdm_get_derived")
+        return {n: getattr(d, n) for n, _ in Derived._fields_}
+
+    def synchronize(self):
+        self._check(lib().tdm_synchronize(self._h), "tdm_synchronize")
+
+    def set_mask(self, mask=None):
+        self._check(lib().tdm_set_mask(self._h, ptr(mask)), "tdm_set_mask")
+
+    @staticmethod
+    def _bits(holos) -> int:
+        dt = str(getattr(holos, "dtype", ""))
+        if "uint16" in dt:
+            return 16
+        if "uint8" in dt:
+            return 8
+        raise TypeError("holograms must be uint8 or uint16")
+
+    def extract(self, holos, n=None, spectra_out=None):
+        n = holos.shape[0] if n is None else n
+        self._check(lib().tdm_extract(self._h, ptr(holos), self._bits(holos), n, ptr(spectra_out)), "tdm_extract")
+        return spectra_out
+
+    def fields(self, spectra=None, n=None, fields_out=None, posspec_out=None):
+        n = spectra.shape[0] if n is None else n
+        self._check(lib().tdm_fields(self._h, ptr(spectra), n, ptr(fields_out), ptr(posspec_out)), "tdm_fields")
+        return fields_out, posspec_out
+
+    def fields_debug(self, spectra=None, n=None, fields_out=None, posspec_out=None, phase=None, unwrapped=None,
+                     amp=None):
+        n = spectra.shape[0] if n is None else n
+        self._check(lib().tdm_fields_debug(self._h, ptr(spectra), n, ptr(fields_out), ptr(posspec_out), ptr(phase),
+                                           ptr(unwrapped), ptr(amp)), "tdm_fields_debug")
+
+    def reconstruct(self, fields=None, posspec=None, n=None, indice=None, absorption=None, otf=None, counts=None):
+        n = fields.shape[0] if n is None else n
+        self._check(lib().tdm_reconstruct(self._h, ptr(fields), ptr(posspec), n, ptr(indice), ptr(absorption),
+                                          ptr(otf), ptr(counts)), "tdm_reconstruct")
+
+    def pipeline(self, holos, indice=None, absorption=None, otf=None, counts=None, posspec=None, n=None):
+        n = holos.shape[0] if n is None else n
+        self._check(lib().tdm_pipeline(self._h, ptr(holos), self._bits(holos), n, ptr(indice), ptr(absorption),
+                                       ptr(otf), ptr(counts), ptr(posspec)), "tdm_pipeline")
+
+
+# ---- host-side file helpers -------------------------------------------------
+
+def extract_val(path: str, key: str, default: float = 0.0):
+    out = ctypes.c_double()
+    rc = lib().tdm_extract_val(path.encode(), key.encode(), default, ctypes.byref(out))
+    if rc < 0:
+        raise TdmError(rc, f"cannot read {path}")
+    return out.value, bool(rc)
+
+
+def extract_string(path: str, key: str) -> str | None:
+    buf = ctypes.create_string_buffer(4096)
+    rc = lib().tdm_extract_string(path.encode(), key.encode(), buf, len(buf))
+    if rc < 0:
+        raise TdmError(rc, f"cannot read {path}")
+    return buf.value.decode() if rc else None
+
+
+def read_geom(recon_txt: str, config_manip_txt: str) -> Geometry:
+    g = Geometry()
+    rc = lib().tdm_read_geom(recon_txt.encode(), config_manip_txt.encode(), ctypes.byref(g))
+    if rc != TDM_OK:
+        raise TdmError(rc, "tdm_read_geom")
+    return g
+
+
+def read_pgm(path: str, roi: int) -> np.ndarray:
+    w, h, mx = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rc = lib().tdm_pgm_info(path.encode(), ctypes.byref(w), ctypes.byref(h), ctypes.byref(mx))
+    if rc != TDM_OK:
+        raise TdmError(rc, f"cannot read {path}")
+    out = np.empty((roi, roi), np.uint8 if mx.value < 256 else np.uint16)
+    bits = ctypes.c_int()
+    rc = lib().tdm_read_pgm(path.encode(), roi, ptr(out), ctypes.byref(bits))
+    if rc != TDM_OK:
+        raise TdmError(rc, f"cannot read {path}")
+    return out
+
+
+def write_tiff(path: str, vol: np.ndarray, pixel_size: float):
+    v = np.ascontiguousarray(vol, np.float32)
+    pages, hgt, wdt = v.shape
+    rc = lib().tdm_write_tiff_f32(path.encode(), ptr(v), wdt, hgt, pages, pixel_size)
+    if rc != TDM_OK:
+        raise TdmError(rc, f"cannot write {path}")

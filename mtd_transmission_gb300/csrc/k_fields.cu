@@ -1,0 +1,512 @@
+// Field formation: second loop of tomo_pretraitement
+// (pretraitement_hors_axe_CPU/main.cpp:230-342) on chunks of angles.
+//
+//  argmax     coordSpec (fonctions.cpp:88-101), |z|^2 at index 0, |z| elsewhere,
+//             first maximum wins.
+//  field      calc_Uborn2 (fonctions.cpp:348-374): shift by -posSpec, unnormalised
+//             inverse FFT, shift by (N, N) -- index remaps on load and store.
+//  volkov     deroul_volkov4_total_sym_paire (src/deroulement_volkov4.cpp:14-92) on
+//             the 2F x 2F even mirror.  A 2D spectral derivative along x is the
+//             1D spectral derivative of each row (kappa depends on kx only), so
+//             gradient_fft4 becomes a row pass and a column pass; the two real
+//             fields of integ_grad4 share one complex 2D FFT (x + i y) and are
+//             separated by Hermitian symmetry.  Literal kappa (Nyquist -1/2),
+//             literal Re() projections, zero-frequency term 0.
+//  fit/form   aberCorr2 / ampliCorr2 (Correction_aberration.cpp:166-217) and the
+//             Born/Rytov formation (main.cpp:289-316).  The least-squares
+//             projection onto degree-4 polynomials is computed in a basis that is
+//             orthonormal over the sample points (same projection as the
+//             reference's normal equations, better conditioned).
+#include "tdm_internal.cuh"
+
+namespace tdm {
+namespace {
+
+constexpr float kTwoPi = 6.283185307179586f;
+constexpr float kInvTwoPi = 0.15915494309189535f;
+
+template <class K>
+cudaError_t allow_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+__device__ __forceinline__ float kappa(int k, int L) {  // init_kvect_shift, FFT_fonctions.cpp:7-17
+    return (float)(k < L / 2 ? k : k - L) / (float)L;
+}
+__device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F - 1 - X; }
+
+// ---------------------------------------------------------------- argmax
+__global__ void __launch_bounds__(1024) k_argmax(const float2* __restrict__ spectra, int F, int2* __restrict__ posspec,
+                                                 float2* __restrict__ specval) {
+    const int a = blockIdx.x;
+    const float2* s = spectra + (size_t)a * F * F;
+    float best = -1.0f;
+    int bi = 0x7fffffff;
+    for (int i = threadIdx.x; i < F * F; i += blockDim.x) {
+        const float2 z = s[i];
+        const float sq = z.x * z.x + z.y * z.y;
+        const float m = (i == 0) ? sq : sqrtf(sq);
+        if (m > best) { best = m; bi = i; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    __shared__ float sb[32];
+    __shared__ int si[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { sb[w] = best; si[w] = bi; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        best = l < nw ? sb[l] : -1.0f;
+        bi = l < nw ? si[l] : 0x7fffffff;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ob = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (l == 0) {
+            if (bi == 0x7fffffff) bi = 0;  // all NaN: the reference keeps index 0
+            posspec[a] = make_int2(bi % F, bi / F);
+            specval[a] = s[bi];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
+template <int F>
+struct FieldCfg {
+    static constexpr int T = F / 8;
+    static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;
+};
+
+template <int F>
+__global__ void __launch_bounds__(FieldCfg<F>::B * (F / 8))
+k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspec, const float2* __restrict__ specval,
+             int normalize, const float2* __restrict__ tw, float2* __restrict__ I1) {
+    using C = FieldCfg<F>;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
+    const int2 p = posspec[a];
+    float2 nrm = make_float2(1.0f, 0.0f);
+    if (normalize) {  // TF_UBorn * conj(spec) / |spec| (main.cpp:332-335)
+        const float2 s0 = specval[a];
+        const float mod = sqrtf(s0.y * s0.y + s0.x * s0.x);
+        nrm = make_float2(s0.x / mod, -s0.y / mod);
+    }
+    float2* s = sm + tr * padded_len(F);
+    const float2* src = spectra + ((size_t)a * F + ((r + p.y) & (F - 1))) * F;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int kx = j + t * C::T;
+        float2 v = src[(kx + p.x) & (F - 1)];
+        if (normalize) v = c_mul(v, nrm);
+        s[pad_idx(kx)] = v;
+    }
+    __syncthreads();
+    fft_smem<F, +1>(s, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int x = j + t * C::T;
+        I1[((size_t)a * F + r) * F + x] = s[pad_idx(x)];
+    }
+}
+
+// mode 1: phase/amplitude (C_ABER); mode 0: the field itself is the result.
+template <int F>
+__global__ void __launch_bounds__(FieldCfg<F>::B * (F / 8))
+k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ tw, float* __restrict__ phase,
+             float* __restrict__ amp, float2* __restrict__ fields) {
+    using C = FieldCfg<F>;
+    constexpr int B = C::B;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y, x0 = blockIdx.x * B;
+    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
+        const int t = i % B, r = i / B;
+        sm[t * padded_len(F) + pad_idx(r)] = I1[((size_t)a * F + r) * F + x0 + t];
+    }
+    __syncthreads();
+    fft_smem<F, +1>(sm + tr * padded_len(F), j, tw);
+    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
+        const int t = i % B, y = i / B;
+        const float2 u = sm[t * padded_len(F) + pad_idx(y)];
+        const int yo = (y + F / 2) & (F - 1), xo = (x0 + t + F / 2) & (F - 1);
+        const size_t o = ((size_t)a * F + yo) * F + xo;
+        if (mode) {
+            phase[o] = atan2f(u.y, u.x);
+            amp[o] = hypotf(u.x, u.y);
+        } else {
+            fields[o] = u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Volkov unwrap
+template <int L>
+struct VolkovCfg {
+    static constexpr int T = L / 8;
+    static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;  // rows/columns per CTA
+};
+
+// Pass 1: rows of the mirror.  gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi.
+template <int L>
+__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, float* __restrict__ gx) {
+    using C = VolkovCfg<L>;
+    constexpr int F = L / 2;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y, Y = blockIdx.x * C::B + tr;
+    float2* sz = sm + tr * padded_len(L);
+    float2* sp = sm + (C::B + tr) * padded_len(L);
+    const float* ph = phase + ((size_t)a * F + mirror(Y, F)) * F;
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int X = j + t * C::T;
+        v[t] = ph[mirror(X, F)];
+        float sn, cs;
+        sincosf(v[t], &sn, &cs);
+        sz[pad_idx(X)] = make_float2(cs, sn);
+        sp[pad_idx(X)] = make_float2(v[t], 0.0f);
+    }
+    __syncthreads();
+    fft_smem<L, -1>(sz, j, tw);
+    fft_smem<L, -1>(sp, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int k = j + t * C::T;
+        const float c = kTwoPi * kappa(k, L) / (float)L;
+        const float2 z = sz[pad_idx(k)], q = sp[pad_idx(k)];
+        sz[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
+        sp[pad_idx(k)] = make_float2(-c * q.y, c * q.x);
+    }
+    __syncthreads();
+    fft_smem<L, +1>(sz, j, tw);
+    fft_smem<L, +1>(sp, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int X = j + t * C::T;
+        float sn, cs;
+        sincosf(v[t], &sn, &cs);
+        const float2 g = sz[pad_idx(X)];
+        const float ax = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);  // Re(-i g / Z)
+        gx[((size_t)a * L + Y) * L + X] = (ax - sp[pad_idx(X)].x) * kInvTwoPi;
+    }
+}
+
+// Pass 2: columns of the mirror: gy like gx, then Q = gx + i gy, FFT along y.
+template <int L>
+__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gx, const float2* __restrict__ tw,
+              float2* __restrict__ qc) {
+    using C = VolkovCfg<L>;
+    constexpr int F = L / 2, B = C::B;
+    extern __shared__ float2 sm[];
+    float* sph = reinterpret_cast<float*>(sm + 2 * B * padded_len(L));  // B x L phase
+    float* sgx = sph + B * L;                                           // B x L gx
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y, X0 = blockIdx.x * B;
+    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
+        const int t = i % B, Y = i / B;
+        const float v = phase[((size_t)a * F + mirror(Y, F)) * F + mirror(X0 + t, F)];
+        float sn, cs;
+        sincosf(v, &sn, &cs);
+        sm[t * padded_len(L) + pad_idx(Y)] = make_float2(cs, sn);
+        sm[(B + t) * padded_len(L) + pad_idx(Y)] = make_float2(v, 0.0f);
+        sph[t * L + Y] = v;
+        sgx[t * L + Y] = gx[((size_t)a * L + Y) * L + X0 + t];
+    }
+    __syncthreads();
+    float2* sz = sm + tr * padded_len(L);
+    float2* sp = sm + (B + tr) * padded_len(L);
+    fft_smem<L, -1>(sz, j, tw);
+    fft_smem<L, -1>(sp, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int k = j + t * C::T;
+        const float c = kTwoPi * kappa(k, L) / (float)L;
+        const float2 z = sz[pad_idx(k)], q = sp[pad_idx(k)];
+        sz[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
+        sp[pad_idx(k)] = make_float2(-c * q.y, c * q.x);
+    }
+    __syncthreads();
+    fft_smem<L, +1>(sz, j, tw);
+    fft_smem<L, +1>(sp, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int Y = j + t * C::T;
+        const float v = sph[tr * L + Y];
+        float sn, cs;
+        sincosf(v, &sn, &cs);
+        const float2 g = sz[pad_idx(Y)];
+        const float ay = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);
+        const float gy = (ay - sp[pad_idx(Y)].x) * kInvTwoPi;
+        sz[pad_idx(Y)] = make_float2(sgx[tr * L + Y], gy);
+    }
+    __syncthreads();
+    fft_smem<L, -1>(sz, j, tw);
+    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
+        const int t = i % B, Y = i / B;
+        qc[((size_t)a * L + Y) * L + X0 + t] = sm[t * padded_len(L) + pad_idx(Y)];
+    }
+}
+
+// Pass 3: rows of FFT2(Q), paired with their mirror rows; integ_grad4's
+// tampon; inverse FFT along x; only the quadrant-4 columns are kept.
+template <int L>
+__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw, float2* __restrict__ tq) {
+    using C = VolkovCfg<L>;
+    constexpr int F = L / 2;
+    static_assert(C::B % 2 == 0, "rows are processed in pairs");
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y;
+    const int q = blockIdx.x * (C::B / 2) + (tr >> 1), which = tr & 1;
+    int r, ptr;
+    if (q == 0) {          // rows 0 and L/2 are their own mirrors
+        r = which ? L / 2 : 0;
+        ptr = tr;
+    } else {
+        r = which ? L - q : q;
+        ptr = tr ^ 1;
+    }
+    float2* s = sm + tr * padded_len(L);
+    const float2* sp = sm + ptr * padded_len(L);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int X = j + t * C::T;
+        s[pad_idx(X)] = qc[((size_t)a * L + r) * L + X];
+    }
+    __syncthreads();
+    fft_smem<L, -1>(s, j, tw);
+    const float nrm = 1.0f / ((float)L * (float)L);
+    const float ky = kappa(r, L);
+    float2 tam[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int kx = j + t * C::T, kxm = (L - kx) & (L - 1);
+        const float2 Q = s[pad_idx(kx)], Qm = sp[pad_idx(kxm)];
+        const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y - Qm.y) * nrm);
+        const float2 Gy = make_float2(0.5f * (Q.y + Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
+        const float kxv = kappa(kx, L);
+        const float k2 = kxv * kxv + ky * ky;
+        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
+        const float den = kTwoPi * k2;
+        tam[t] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 8; ++t) s[pad_idx(j + t * C::T)] = tam[t];
+    __syncthreads();
+    fft_smem<L, +1>(s, j, tw);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int X = j + t * C::T;
+        if (X >= F) tq[((size_t)a * L + r) * F + (X - F)] = s[pad_idx(X)];
+    }
+}
+
+// Pass 4: columns of quadrant 4: inverse FFT along y, real part, phi + 2 pi IntM.
+template <int L>
+__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ phase, const float2* __restrict__ tw,
+                    float* __restrict__ unwrapped) {
+    using C = VolkovCfg<L>;
+    constexpr int F = L / 2, B = C::B;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int a = blockIdx.y, c0 = blockIdx.x * B;
+    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
+        const int t = i % B, ky = i / B;
+        sm[t * padded_len(L) + pad_idx(ky)] = tq[((size_t)a * L + ky) * F + c0 + t];
+    }
+    __syncthreads();
+    fft_smem<L, +1>(sm + tr * padded_len(L), j, tw);
+    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
+        const int t = i % B, y = i / B;
+        const size_t o = ((size_t)a * F + y) * F + c0 + t;
+        unwrapped[o] = phase[o] + kTwoPi * sm[t * padded_len(L) + pad_idx(F + y)].x;
+    }
+}
+
+// ---------------------------------------------------------------- aberration fit
+// beta[a][img][:] = Rinv * (Q^T b): monomial coefficients (scaled coordinates)
+// of the least-squares fit of image img (0: unwrapped phase, 1: amplitude).
+__global__ void __launch_bounds__(256) k_aber_fit(const float* __restrict__ unwrapped, const float* __restrict__ amp,
+                                                  const int* __restrict__ samp_idx, const float* __restrict__ samp_q,
+                                                  int nsamp, const double* __restrict__ rinv, int F,
+                                                  double* __restrict__ beta) {
+    const int a = blockIdx.x, im = blockIdx.y;
+    const float* img = (im == 0 ? unwrapped : amp) + (size_t)a * F * F;
+    double acc[kNC];
+#pragma unroll
+    for (int k = 0; k < kNC; ++k) acc[k] = 0.0;
+    for (int s = threadIdx.x; s < nsamp; s += blockDim.x) {
+        const double v = (double)img[samp_idx[s]];
+        const float* q = samp_q + (size_t)s * kNC;
+#pragma unroll
+        for (int k = 0; k < kNC; ++k) acc[k] = fma((double)q[k], v, acc[k]);
+    }
+    __shared__ double red[8][kNC];
+    __shared__ double cf[kNC];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < kNC; ++k) {
+        double x = acc[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if (l == 0) red[w][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNC) {
+        double x = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) x += red[i][threadIdx.x];
+        cf[threadIdx.x] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNC) {
+        double x = 0.0;
+#pragma unroll
+        for (int i = 0; i < kNC; ++i) x = fma(rinv[threadIdx.x * kNC + i], cf[i], x);
+        beta[((size_t)a * 2 + im) * kNC + threadIdx.x] = x;
+    }
+}
+
+// Evaluates the fits, corrects phase and amplitude and forms the Born or Rytov field.
+__global__ void __launch_bounds__(256) k_form(const float* __restrict__ unwrapped, const float* __restrict__ amp,
+                                              const double* __restrict__ beta, int F, int born,
+                                              float2* __restrict__ fields) {
+    const int a = blockIdx.y;
+    __shared__ float bf[2 * kNC];
+    if (threadIdx.x < 2 * kNC) bf[threadIdx.x] = (float)beta[(size_t)a * 2 * kNC + threadIdx.x];
+    __syncthreads();
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= F * F) return;
+    const int x = idx % F, y = idx / F;
+    const float h = 0.5f * (float)(F - 1);
+    const float u = ((float)x - h) / h, v = ((float)y - h) / h;
+    float sp = 0.0f, sa = 0.0f, up = 1.0f;
+    int k = 0;
+#pragma unroll
+    for (int px = 0; px <= 4; ++px) {
+        float pp = 0.0f, pa = 0.0f, vp = 1.0f;
+#pragma unroll
+        for (int py = 0; px + py <= 4; ++py) {
+            pp = fmaf(bf[k], vp, pp);
+            pa = fmaf(bf[kNC + k], vp, pa);
+            vp *= v;
+            ++k;
+        }
+        sp = fmaf(pp, up, sp);
+        sa = fmaf(pa, up, sa);
+        up *= u;
+    }
+    const size_t o = (size_t)a * F * F + idx;
+    const float pf = unwrapped[o] - sp;
+    float af = amp[o] / (sa + 0.00000001f);
+    if (af > 10.0f) af = 1.0f;
+    if (af < -10.0f) af = 1.0f;
+    float sn, cs;
+    sincosf(pf, &sn, &cs);
+    const float m = fabsf(af);  // sqrt(A^2)
+    fields[o] = born ? make_float2(m * cs - 1.0f, m * sn) : make_float2(logf(m), pf);
+}
+
+template <int F>
+int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp) {
+    constexpr int L = 2 * F;
+    using FC = FieldCfg<F>;
+    using VC = VolkovCfg<L>;
+    const Params& p = c->p;
+    Buffers& b = c->b;
+    const size_t FF = (size_t)F * F;
+    const size_t sm_field = (size_t)FC::B * padded_len(F) * sizeof(float2);
+    const size_t sm_vrows = (size_t)2 * VC::B * padded_len(L) * sizeof(float2);
+    const size_t sm_vcols = sm_vrows + (size_t)2 * VC::B * L * sizeof(float);
+    const size_t sm_vir = (size_t)VC::B * padded_len(L) * sizeof(float2);
+    if (allow_smem(k_field_rows<F>, sm_field) || allow_smem(k_field_cols<F>, sm_field) ||
+        allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
+        allow_smem(k_volkov_integ_rows<L>, sm_vir) || allow_smem(k_volkov_integ_cols<L>, sm_vir))
+        return TDM_ECUDA;
+    for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
+        const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
+        const float2* spec = b.spectra + (size_t)g0 * FF;
+        {
+            Launch l(c, K_ARGMAX);
+            k_argmax<<<m, 1024, 0, c->stream>>>(spec, F, b.posspec + g0, b.specval + g0);
+        }
+        {
+            Launch l(c, K_FIELD_ROWS);
+            k_field_rows<F><<<dim3(F / FC::B, m), FC::B * FC::T, sm_field, c->stream>>>(
+                spec, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
+        }
+        {
+            Launch l(c, K_FIELD_COLS);
+            k_field_cols<F><<<dim3(F / FC::B, m), FC::B * FC::T, sm_field, c->stream>>>(
+                b.I1, p.c_aber, b.tw, b.phase, b.amp, b.fields + (size_t)g0 * FF);
+        }
+        if (!p.c_aber) continue;
+        const float* unw = b.phase;
+        if (p.deroul) {
+            {
+                Launch l(c, K_VOLKOV_ROWS);
+                k_volkov_rows<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vrows, c->stream>>>(b.phase, b.tw, b.gx);
+            }
+            {
+                Launch l(c, K_VOLKOV_COLS);
+                k_volkov_cols<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vcols, c->stream>>>(b.phase, b.gx, b.tw,
+                                                                                             b.qc);
+            }
+            {
+                Launch l(c, K_VOLKOV_INTEG_ROWS);
+                k_volkov_integ_rows<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(b.qc, b.tw, b.tq);
+            }
+            {
+                Launch l(c, K_VOLKOV_INTEG_COLS);
+                k_volkov_integ_cols<L><<<dim3(F / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(b.tq, b.phase, b.tw,
+                                                                                                  b.unwrapped);
+            }
+            unw = b.unwrapped;
+        }
+        {
+            Launch l(c, K_ABER_FIT);
+            k_aber_fit<<<dim3(m, 2), 256, 0, c->stream>>>(unw, b.amp, b.samp_idx, b.samp_q, c->nsamp, b.rinv, F,
+                                                          b.beta);
+        }
+        {
+            Launch l(c, K_FORM);
+            k_form<<<dim3((unsigned)((FF + 255) / 256), m), 256, 0, c->stream>>>(unw, b.amp, b.beta, F, p.born,
+                                                                                b.fields + (size_t)g0 * FF);
+        }
+        if (dbg_phase)
+            cudaMemcpyAsync(dbg_phase + (g0 - a0) * FF, b.phase, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+        if (dbg_unwrapped)
+            cudaMemcpyAsync(dbg_unwrapped + (g0 - a0) * FF, unw, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+        if (dbg_amp)
+            cudaMemcpyAsync(dbg_amp + (g0 - a0) * FF, b.amp, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+}  // namespace
+
+int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp) {
+    switch (c->p.F) {
+        case 64: return fields_impl<64>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
+        case 128: return fields_impl<128>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
+        case 256: return fields_impl<256>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
+        case 512: return fields_impl<512>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
+        default: return TDM_EUNSUPPORTED;
+    }
+}
+
+}  // namespace tdm

@@ -1,0 +1,658 @@
+// C ABI of the reconstruction path: context, tables, buffers and entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "tdm_internal.cuh"
+
+using namespace tdm;
+
+namespace tdm {
+const char* const kKernelNames[K_COUNT] = {
+    "extract_rows", "extract_cols", "argmax", "field_rows", "field_cols", "volkov_rows", "volkov_cols",
+    "volkov_integ_rows", "volkov_integ_cols", "aber_fit", "form", "fzm0", "cap_rows", "cap_cols", "gather",
+    "ypass", "xpass", "posspec"};
+
+cudaEvent_t prof_event(tdm_ctx* c) {
+    if (!c->ev_pool.empty()) {
+        cudaEvent_t e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace tdm
+
+namespace {
+
+void prof_release(tdm_ctx* c) {
+    for (const ProfRec& r : c->prof_recs) {
+        c->ev_pool.push_back(r.a);
+        c->ev_pool.push_back(r.b);
+    }
+    c->prof_recs.clear();
+}
+
+int fail(tdm_ctx* c, int code, const std::string& msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int cuda_fail(tdm_ctx* c, cudaError_t e, const char* what) {
+    if (c) c->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? TDM_ENOMEM : TDM_ECUDA;
+}
+
+#define TDM_CU(call)                                                   \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);         \
+    } while (0)
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Tukey window factor, same float arithmetic as tukey2D
+// (pretraitement_hors_axe_CPU/FFT_fonctions.cpp:61-87): the 2D window is the
+// product of this factor along x and along y.
+std::vector<double> tukey_factor(int n, float alpha) {
+    std::vector<double> t(n, 0.0);
+    const int b1 = (int)std::round(alpha * (n - 1) / 2);
+    const int b2 = (int)std::round((n - 1) * (1 - alpha / 2));
+    for (int i = 0; i < b1 + 1 && i < n; ++i) {
+        const float arg = 2 * i / (alpha * (n - 1)) - 1;
+        t[i] = 0.5 * (1 + std::cos(3.1415 * arg));
+    }
+    for (int i = b1 + 1; i < b2 + 1 && i < n; ++i) t[i] = 1;
+    for (int i = b2 + 1; i < n; ++i) {
+        const float arg = 2 * i / (alpha * (n - 1)) - 2 / alpha + 1;
+        t[i] = 0.5 * (1 + std::cos(3.1415 * arg));
+    }
+    return t;
+}
+
+template <class T>
+int dev_alloc(tdm_ctx* c, T** p, size_t count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    return TDM_OK;
+}
+
+void free_all(tdm_ctx* c) {
+    Buffers& b = c->b;
+    void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
+                    b.specval, b.fzm0, b.I1, b.phase, b.amp, b.gx, b.qc, b.tq, b.unwrapped, b.beta, b.fields,
+                    b.r1, b.rec_val, b.rec_z, b.acc, b.vol, b.out_re, b.out_im, b.out_otf, b.out_cnt,
+                    b.samp_idx, b.samp_q, b.rinv, b.err};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    b = Buffers{};
+}
+
+__global__ void k_pack_posspec(const int32_t* __restrict__ xy, int n, int2* __restrict__ out) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = make_int2(xy[a], xy[n + a]);
+}
+__global__ void k_unpack_posspec(const int2* __restrict__ in, int n, int32_t* __restrict__ xy) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) {
+        xy[a] = in[a].x;
+        xy[n + a] = in[a].y;
+    }
+}
+
+// Aberration sample points and an orthonormal basis of the degree-4
+// polynomials over them (modified Gram-Schmidt in long double, twice).
+int build_aberration(tdm_ctx* c, const uint8_t* mask_host) {
+    const int F = c->p.F;
+    std::vector<int> idx;
+    std::vector<long double> A;  // nsamp x kNC
+    const long double h = 0.5L * (F - 1);
+    // countM (Correction_aberration.cpp:86-106) marks every 5th row/column
+    // pixel with value > 45; the samples are those pixels in row-major order.
+    for (int y = 0; y < F; ++y)
+        for (int x = 0; x < F; ++x) {
+            const uint8_t v = mask_host ? mask_host[(size_t)y * F + x] : 255;
+            if (x % 5 == 0 && y % 5 == 0 && v > 45) {
+                idx.push_back(y * F + x);
+                const long double u = (x - h) / h, w = (y - h) / h;
+                for (int px = 0; px <= 4; ++px)
+                    for (int py = 0; px + py <= 4; ++py) A.push_back(std::pow(u, (long double)px) * std::pow(w, (long double)py));
+            }
+        }
+    const int ns = (int)idx.size();
+    if (ns < kNC) return fail(c, TDM_EDATA, "aberration mask leaves fewer than 15 background samples");
+    std::vector<long double> Q(A), R(kNC * kNC, 0.0L);
+    for (int k = 0; k < kNC; ++k) {
+        for (int pass = 0; pass < 2; ++pass)
+            for (int i = 0; i < k; ++i) {
+                long double d = 0;
+                for (int s = 0; s < ns; ++s) d += Q[(size_t)s * kNC + i] * Q[(size_t)s * kNC + k];
+                R[i * kNC + k] += d;
+                for (int s = 0; s < ns; ++s) Q[(size_t)s * kNC + k] -= d * Q[(size_t)s * kNC + i];
+            }
+        long double nrm = 0;
+        for (int s = 0; s < ns; ++s) nrm += Q[(size_t)s * kNC + k] * Q[(size_t)s * kNC + k];
+        nrm = std::sqrt(nrm);
+        if (!(nrm > 1e-12L)) return fail(c, TDM_EDATA, "aberration samples do not determine a degree-4 fit");
+        R[k * kNC + k] = nrm;
+        for (int s = 0; s < ns; ++s) Q[(size_t)s * kNC + k] /= nrm;
+    }
+    // Rinv = R^-1 (upper triangular)
+    std::vector<long double> Ri(kNC * kNC, 0.0L);
+    for (int col = 0; col < kNC; ++col) {
+        for (int row = col; row >= 0; --row) {
+            long double s = (row == col) ? 1.0L : 0.0L;
+            for (int k = row + 1; k <= col; ++k) s -= R[row * kNC + k] * Ri[k * kNC + col];
+            Ri[row * kNC + col] = s / R[row * kNC + row];
+        }
+    }
+    std::vector<float> qf((size_t)ns * kNC);
+    for (size_t i = 0; i < qf.size(); ++i) qf[i] = (float)Q[i];
+    std::vector<double> rd(kNC * kNC);
+    for (int i = 0; i < kNC * kNC; ++i) rd[i] = (double)Ri[i];
+    Buffers& b = c->b;
+    if (b.samp_idx) cudaFree(b.samp_idx);
+    if (b.samp_q) cudaFree(b.samp_q);
+    b.samp_idx = nullptr;
+    b.samp_q = nullptr;
+    if (int rc = dev_alloc(c, &b.samp_idx, ns)) return rc;
+    if (int rc = dev_alloc(c, &b.samp_q, qf.size())) return rc;
+    TDM_CU(cudaMemcpy(b.samp_idx, idx.data(), ns * sizeof(int), cudaMemcpyHostToDevice));
+    TDM_CU(cudaMemcpy(b.samp_q, qf.data(), qf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    TDM_CU(cudaMemcpy(b.rinv, rd.data(), rd.size() * sizeof(double), cudaMemcpyHostToDevice));
+    c->nsamp = ns;
+    return TDM_OK;
+}
+
+int check_geom(const tdm_geom* g, std::string& why) {
+    if (!is_pow2(g->ccd_roix) || g->ccd_roix < 256 || g->ccd_roix > 2048) {
+        why = "CCD_ROIX must be a power of two in [256, 2048]";
+        return TDM_EUNSUPPORTED;
+    }
+    const int F = 2 * g->nxmax;
+    if (!is_pow2(F) || F < 64 || F > 512) {
+        why = "2*NXMAX must be a power of two in [64, 512]";
+        return TDM_EUNSUPPORTED;
+    }
+    if (!is_pow2(g->dim_final) || g->dim_final < 4 * g->nxmax || g->dim_final > 1024 || g->dim_final < 128) {
+        why = "DIM_FINAL must be a power of two in [max(128, 4*NXMAX), 1024]";
+        return TDM_EUNSUPPORTED;
+    }
+    const int x0 = g->circle_cx - g->nxmax, y0 = g->circle_cy - g->nxmax;
+    if (x0 < 0 || y0 < 0 || x0 + F > g->ccd_roix || y0 + F > g->ccd_roix) {
+        why = "crop window (CIRCLE_CX/CY +- NXMAX) outside the hologram spectrum";
+        return TDM_EINVAL;
+    }
+    if (g->c_aber && g->deroul && !g->volkov) {
+        why = "VOLKOV 0 (Herraez unwrapping) is not supported";
+        return TDM_EUNSUPPORTED;
+    }
+    if (!(g->na > 0) || !(g->n0 > 0) || !(g->lambda0 > 0) || !(g->f_obj > 0) || !(g->rf > 0) || !(g->f_tube > 0) ||
+        !(g->tpcam > 0)) {
+        why = "optical parameters must be positive";
+        return TDM_EINVAL;
+    }
+    return TDM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tdm_derive(const tdm_geom* g, tdm_derived* d) {
+    if (!g || !d) return TDM_EINVAL;
+    // manip (pretraitement_hors_axe_CPU/manip.cpp:35-57,104; Reconstruction/src/manip.cpp:56-94)
+    const double G = g->f_tube / g->f_obj;
+    const double Gt = G / g->rf;
+    d->tp_holo = g->tpcam / Gt;
+    const size_t twoN = 2 * (size_t)g->nxmax;
+    d->tp_uborn = d->tp_holo * g->ccd_roix / (double)twoN;
+    d->delta_f = 1 / (d->tp_uborn * 2 * (double)g->nxmax);
+    d->tp_tomo = d->tp_uborn * (double)twoN / (double)g->dim_final;
+    d->rayon = std::round((double)(size_t)g->nxmax * g->n0 / g->na);
+    return TDM_OK;
+}
+
+int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
+    if (!geom || !out || max_angles <= 0) return TDM_EINVAL;
+    *out = nullptr;
+    std::string why;
+    if (int rc = check_geom(geom, why)) {
+        fprintf(stderr, "tdm_create: %s\n", why.c_str());
+        return rc;
+    }
+    tdm_ctx* c = new tdm_ctx();
+    c->g = *geom;
+    c->max_angles = max_angles;
+    tdm_derive(geom, &c->dv);
+    Params& p = c->p;
+    p.H = geom->ccd_roix;
+    p.N = geom->nxmax;
+    p.F = 2 * p.N;
+    p.L = 2 * p.F;
+    p.D = geom->dim_final;
+    p.x0 = geom->circle_cx - p.N;
+    p.y0 = geom->circle_cy - p.N;
+    p.born = geom->born ? 1 : 0;
+    p.c_aber = geom->c_aber ? 1 : 0;
+    p.deroul = geom->deroul ? 1 : 0;
+    p.rayon = c->dv.rayon;
+    p.inv_rayon = 1.0 / c->dv.rayon;
+    const int N = p.N, F = p.F, D = p.D;
+    // disc test fd^2 < COEF_NA_OBJ_LIMIT * N^2 on integers (fonctions.cpp:915)
+    const double lim = geom->coef_na_obj_limit * (double)(N * N);
+    p.disc_thr = (int)std::min<double>(std::ceil(lim), 2.0 * N * N + 1);
+    // cap heights sqrt(rayon^2 - fd^2) exactly as fonctions.cpp:920, and the z band
+    const double r2 = p.rayon * p.rayon;
+    std::vector<double> stab((size_t)F * F, std::numeric_limits<double>::quiet_NaN());
+    double smin = std::numeric_limits<double>::infinity();
+    for (int fdy = -N; fdy < N; ++fdy)
+        for (int fdx = -N; fdx < N; ++fdx) {
+            const double fdz2 = r2 - fdx * fdx - fdy * fdy;
+            stab[(size_t)(fdy + N) * F + fdx + N] = std::sqrt(fdz2);
+            if (fdx * fdx + fdy * fdy < p.disc_thr) {
+                if (!(fdz2 >= 0)) {
+                    delete c;
+                    fprintf(stderr, "tdm_create: NA disc reaches beyond the Ewald sphere\n");
+                    return TDM_EUNSUPPORTED;
+                }
+                smin = std::min(smin, std::sqrt(fdz2));
+            }
+        }
+    double fzmin = std::numeric_limits<double>::infinity(), fzmax = 0;
+    for (int fy = -N; fy < N; ++fy)
+        for (int fx = -N; fx < N; ++fx) {
+            const double cz = r2 - fx * fx - fy * fy;
+            if (std::round(cz) >= 0) {
+                fzmin = std::min(fzmin, std::sqrt(cz));
+                fzmax = std::max(fzmax, std::sqrt(cz));
+            }
+        }
+    const int kmin = (int)std::round(smin - fzmax), kmax = (int)std::round(p.rayon - fzmin);
+    p.zmin = D / 2 + kmin;
+    p.band = kmax - kmin + 1;
+    if (p.zmin < 0 || p.zmin + p.band > D) {
+        delete c;
+        fprintf(stderr, "tdm_create: Ewald caps exceed the DIM_FINAL volume along z\n");
+        return TDM_EUNSUPPORTED;
+    }
+    // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:885-902): k0 is a float
+    const float n0f = (float)geom->n0;
+    const float kv = (float)(2 * M_PI / geom->lambda0);
+    const float k0 = kv * n0f;
+    p.cap_scale = (float)(((double)k0 / M_PI) * (-2 * M_PI));
+    p.dx2 = (float)std::pow(c->dv.tp_uborn, 2);
+    const double k_v = 2 * M_PI / geom->lambda0;  // main.cpp:346-347
+    p.out_scale = (float)(std::pow(c->dv.delta_f, 3) * (-1 / (2 * geom->n0 * k_v * k_v)));
+
+    int rc = TDM_OK;
+#define TRY(x)                         \
+    do {                               \
+        if ((rc = (x)) != TDM_OK) {    \
+            free_all(c);               \
+            tdm_ctx* dead = c;         \
+            std::string m = dead->last_error; \
+            delete dead;               \
+            fprintf(stderr, "tdm_create: %s\n", m.c_str()); \
+            return rc;                 \
+        }                              \
+    } while (0)
+    cudaGetDevice(&c->device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return TDM_ECUDA;
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaEventCreateWithFlags(&c->ev_copy[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&c->ev_free[i], cudaEventDisableTiming);
+    }
+    for (auto& e : c->ev_stage) cudaEventCreate(&e);
+    Buffers& b = c->b;
+    const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk, L = p.L;
+    c->holo_chunk = 16;
+    TRY(dev_alloc(c, &b.tw, kTwN));
+    TRY(dev_alloc(c, &b.tuk_h, p.H));
+    TRY(dev_alloc(c, &b.tuk_f, F));
+    TRY(dev_alloc(c, &b.s_tab, FF));
+    TRY(dev_alloc(c, &b.s_tabf, FF));
+    TRY(dev_alloc(c, &b.holo_stage, 2 * (size_t)c->holo_chunk * p.H * p.H * 2));
+    TRY(dev_alloc(c, &b.inter, (size_t)c->holo_chunk * p.H * F));
+    TRY(dev_alloc(c, &b.spectra, M * FF));
+    TRY(dev_alloc(c, &b.posspec, M));
+    TRY(dev_alloc(c, &b.specval, M));
+    TRY(dev_alloc(c, &b.fzm0, M));
+    TRY(dev_alloc(c, &b.I1, CH * FF));
+    TRY(dev_alloc(c, &b.phase, CH * FF));
+    TRY(dev_alloc(c, &b.amp, CH * FF));
+    TRY(dev_alloc(c, &b.gx, CH * L * L));
+    TRY(dev_alloc(c, &b.qc, CH * L * L));
+    TRY(dev_alloc(c, &b.tq, CH * L * F));
+    TRY(dev_alloc(c, &b.unwrapped, CH * FF));
+    TRY(dev_alloc(c, &b.beta, CH * 2 * kNC));
+    TRY(dev_alloc(c, &b.fields, M * FF));
+    TRY(dev_alloc(c, &b.r1, CH * FF));
+    TRY(dev_alloc(c, &b.rec_val, M * FF));
+    TRY(dev_alloc(c, &b.rec_z, M * FF));
+    TRY(dev_alloc(c, &b.acc, (size_t)D * D * p.band));
+    TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
+    TRY(dev_alloc(c, &b.rinv, kNC * kNC));
+    TRY(dev_alloc(c, &b.err, 4));
+    // tables
+    std::vector<float2> tw(kTwN);
+    for (int k = 0; k < kTwN; ++k) {
+        const long double a = -2.0L * 3.14159265358979323846264338327950288L * k / kTwN;
+        tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    std::vector<double> th = tukey_factor(p.H, 0.05f), tf = tukey_factor(F, 0.1f);
+    std::vector<float> thf(th.begin(), th.end()), tff(tf.begin(), tf.end());
+    std::vector<float> stabf(stab.begin(), stab.end());
+    if (cudaMemcpy(b.tw, tw.data(), kTwN * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.tuk_h, thf.data(), p.H * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.tuk_f, tff.data(), F * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.s_tab, stab.data(), FF * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.s_tabf, stabf.data(), FF * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(b.err, 0, 4 * sizeof(int)) != cudaSuccess)
+        TRY(cuda_fail(c, cudaGetLastError(), "table upload"));
+    if (p.c_aber) TRY(build_aberration(c, nullptr));
+#undef TRY
+    *out = c;
+    return TDM_OK;
+}
+
+int tdm_destroy(tdm_ctx* c) {
+    if (!c) return TDM_EINVAL;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    free_all(c);
+    for (int i = 0; i < 2; ++i) {
+        if (c->ev_copy[i]) cudaEventDestroy(c->ev_copy[i]);
+        if (c->ev_free[i]) cudaEventDestroy(c->ev_free[i]);
+    }
+    for (auto& e : c->ev_stage)
+        if (e) cudaEventDestroy(e);
+    prof_release(c);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    delete c;
+    return TDM_OK;
+}
+
+const char* tdm_last_error(const tdm_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int tdm_get_derived(const tdm_ctx* c, tdm_derived* out) {
+    if (!c || !out) return TDM_EINVAL;
+    *out = c->dv;
+    return TDM_OK;
+}
+
+int tdm_set_mask(tdm_ctx* c, const uint8_t* mask) {
+    if (!c) return TDM_EINVAL;
+    cudaSetDevice(c->device);
+    if (!c->p.c_aber) return TDM_OK;
+    std::vector<uint8_t> hm;
+    if (mask && is_device_ptr(mask)) {
+        hm.resize((size_t)c->p.F * c->p.F);
+        TDM_CU(cudaMemcpy(hm.data(), mask, hm.size(), cudaMemcpyDeviceToHost));
+        mask = hm.data();
+    }
+    TDM_CU(cudaStreamSynchronize(c->stream));
+    return build_aberration(c, mask);
+}
+
+int tdm_synchronize(tdm_ctx* c) {
+    if (!c) return TDM_EINVAL;
+    TDM_CU(cudaStreamSynchronize(c->copy_stream));
+    TDM_CU(cudaStreamSynchronize(c->stream));
+    int err = 0;
+    TDM_CU(cudaMemcpy(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(c->b.err, 0, sizeof(int));
+        return fail(c, TDM_EDATA, "an Ewald-cap voxel fell outside the DIM_FINAL volume");
+    }
+    return TDM_OK;
+}
+
+void* tdm_stream(tdm_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int tdm_profile_count(void) { return K_COUNT; }
+
+int tdm_profile(tdm_ctx* c, int enable) {
+    if (!c) return TDM_EINVAL;
+    TDM_CU(cudaStreamSynchronize(c->stream));
+    prof_release(c);
+    c->prof = enable != 0;
+    return TDM_OK;
+}
+
+int tdm_profile_read(tdm_ctx* c, int index, const char** name, double* total_ms, int* launches) {
+    if (!c || index < 0 || index >= K_COUNT) return TDM_EINVAL;
+    TDM_CU(cudaStreamSynchronize(c->stream));
+    double t = 0;
+    int n = 0;
+    for (const ProfRec& r : c->prof_recs) {
+        if (r.id != index) continue;
+        float ms = 0;
+        TDM_CU(cudaEventElapsedTime(&ms, r.a, r.b));
+        t += ms;
+        ++n;
+    }
+    if (name) *name = kKernelNames[index];
+    if (total_ms) *total_ms = t;
+    if (launches) *launches = n;
+    return TDM_OK;
+}
+uint64_t tdm_launch_count(const tdm_ctx* c) { return c ? c->launches : 0; }
+
+double tdm_stage_ms(const tdm_ctx* c, const char* stage) {
+    if (!c || !stage) return -1;
+    int a, b;
+    if (!strcmp(stage, "extract")) a = 0, b = 1;
+    else if (!strcmp(stage, "fields")) a = 1, b = 2;
+    else if (!strcmp(stage, "map")) a = 2, b = 3;
+    else if (!strcmp(stage, "gather")) a = 4, b = 5;
+    else if (!strcmp(stage, "volume")) a = 4, b = 6;
+    else if (!strcmp(stage, "total")) a = 0, b = 6;
+    else return -1;
+    float ms = -1;
+    if (cudaEventElapsedTime(&ms, c->ev_stage[a], c->ev_stage[b]) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return ms;
+}
+
+// ---------------------------------------------------------------- stages
+static int stage_extract(tdm_ctx* c, const void* holos, int bits, int n) {
+    const Params& p = c->p;
+    const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
+    if (is_device_ptr(holos)) return launch_extract(c, holos, bits, n, 0);
+    // host holograms: chunked copies on the copy stream, double buffered
+    const size_t stage_bytes = (size_t)c->holo_chunk * p.H * p.H * 2;
+    for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
+        const int m = std::min(c->holo_chunk, n - h0);
+        const int buf = k & 1;
+        uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
+        if (k >= 2) TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));
+        TDM_CU(cudaMemcpyAsync(dst, static_cast<const char*>(holos) + h0 * per, m * per, cudaMemcpyHostToDevice,
+                               c->copy_stream));
+        TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
+        TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf], 0));
+        if (int rc = launch_extract(c, dst, bits, m, h0)) return rc;
+        TDM_CU(cudaEventRecord(c->ev_free[buf], c->stream));
+    }
+    return TDM_OK;
+}
+
+int tdm_extract(tdm_ctx* c, const void* holos, int bits, int n, float* spectra_out) {
+    if (!c || !holos || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
+        return fail(c, TDM_EINVAL, "tdm_extract: invalid argument");
+    cudaSetDevice(c->device);
+    TDM_CU(cudaEventRecord(c->ev_stage[0], c->stream));
+    if (int rc = stage_extract(c, holos, bits, n)) return rc;
+    TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));
+    c->n_spectra = n;
+    const size_t FF = (size_t)c->p.F * c->p.F;
+    if (spectra_out)
+        TDM_CU(cudaMemcpyAsync(spectra_out, c->b.spectra, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
+    if (!is_device_ptr(holos) || (spectra_out && !is_device_ptr(spectra_out))) return tdm_synchronize(c);
+    return TDM_OK;
+}
+
+static int run_fields(tdm_ctx* c, const float* spectra_in, int n, float* fields_out, int32_t* posspec_out,
+                      float* dph, float* dun, float* dam) {
+    if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, "tdm_fields: invalid argument");
+    cudaSetDevice(c->device);
+    const size_t FF = (size_t)c->p.F * c->p.F;
+    if (spectra_in && spectra_in != reinterpret_cast<float*>(c->b.spectra)) {
+        TDM_CU(cudaMemcpyAsync(c->b.spectra, spectra_in, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
+    } else if (!spectra_in && n > c->n_spectra) {
+        return fail(c, TDM_EINVAL, "tdm_fields: fewer spectra in the context than requested");
+    }
+    TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));
+    if (int rc = launch_fields(c, 0, n, dph, dun, dam)) return fail(c, rc, "tdm_fields: kernel launch failed");
+    TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
+    c->n_fields = n;
+    bool host = (spectra_in && !is_device_ptr(spectra_in));
+    if (fields_out) {
+        TDM_CU(cudaMemcpyAsync(fields_out, c->b.fields, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
+        host |= !is_device_ptr(fields_out);
+    }
+    if (posspec_out) {
+        if (is_device_ptr(posspec_out)) {
+            Launch l(c, K_POSSPEC);
+            k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
+        } else {
+            std::vector<int2> tmp(n);
+            TDM_CU(cudaMemcpyAsync(tmp.data(), c->b.posspec, n * sizeof(int2), cudaMemcpyDeviceToHost, c->stream));
+            TDM_CU(cudaStreamSynchronize(c->stream));
+            for (int a = 0; a < n; ++a) {
+                posspec_out[a] = tmp[a].x;
+                posspec_out[n + a] = tmp[a].y;
+            }
+        }
+    }
+    if (host || dph || dun || dam) return tdm_synchronize(c);
+    return TDM_OK;
+}
+
+int tdm_fields(tdm_ctx* c, const float* spectra_in, int n, float* fields_out, int32_t* posspec_out) {
+    return run_fields(c, spectra_in, n, fields_out, posspec_out, nullptr, nullptr, nullptr);
+}
+
+int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_out, int32_t* posspec_out,
+                     float* phase_out, float* unwrapped_out, float* amp_out) {
+    return run_fields(c, spectra_in, n, fields_out, posspec_out, phase_out, unwrapped_out, amp_out);
+}
+
+// Cap mapping and volume; outputs may be host or device memory.
+static int run_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
+    const Params& p = c->p;
+    const size_t NT = (size_t)p.D * p.D * p.D;
+    if (int rc = launch_cap(c, n)) return fail(c, rc, "cap mapping launch failed");
+    TDM_CU(cudaEventRecord(c->ev_stage[3], c->stream));
+    Buffers& b = c->b;
+    auto dev_or_stage = [&](auto* user, auto*& stage) -> decltype(user) {
+        if (!user) return nullptr;
+        if (is_device_ptr(user)) return user;
+        if (!stage) {
+            if (cudaMalloc(reinterpret_cast<void**>(&stage), NT * sizeof(*user)) != cudaSuccess) return nullptr;
+        }
+        return stage;
+    };
+    float* dre = dev_or_stage(re, b.out_re);
+    float* dim = dev_or_stage(im, b.out_im);
+    uint8_t* dotf = dev_or_stage(otf, b.out_otf);
+    uint32_t* dcnt = dev_or_stage(cnt, b.out_cnt);
+    if ((re && !dre) || (im && !dim) || (otf && !dotf) || (cnt && !dcnt))
+        return fail(c, TDM_ENOMEM, "output staging allocation failed");
+    if (int rc = launch_volume(c, n, dre, dim, dotf, dcnt)) return fail(c, rc, "volume launch failed");
+    bool host = false;
+    if (re && dre != re) { TDM_CU(cudaMemcpyAsync(re, dre, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream)); host = true; }
+    if (im && dim != im) { TDM_CU(cudaMemcpyAsync(im, dim, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream)); host = true; }
+    if (otf && dotf != otf) { TDM_CU(cudaMemcpyAsync(otf, dotf, NT, cudaMemcpyDeviceToHost, c->stream)); host = true; }
+    if (cnt && dcnt != cnt) { TDM_CU(cudaMemcpyAsync(cnt, dcnt, NT * 4, cudaMemcpyDeviceToHost, c->stream)); host = true; }
+    return host ? tdm_synchronize(c) : TDM_OK;
+}
+
+int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_in, int n, float* indice_out,
+                    float* absorption_out, uint8_t* otf_out, uint32_t* counts_out) {
+    if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, "tdm_reconstruct: invalid argument");
+    cudaSetDevice(c->device);
+    const size_t FF = (size_t)c->p.F * c->p.F;
+    if ((!fields_in || !posspec_in) && n > c->n_fields)
+        return fail(c, TDM_EINVAL, "tdm_reconstruct: fewer fields in the context than requested");
+    if (fields_in && fields_in != reinterpret_cast<const float*>(c->b.fields))
+        TDM_CU(cudaMemcpyAsync(c->b.fields, fields_in, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
+    if (posspec_in) {
+        if (is_device_ptr(posspec_in)) {
+            Launch l(c, K_POSSPEC);
+            k_pack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(posspec_in, n, c->b.posspec);
+        } else {
+            std::vector<int2> tmp(n);
+            for (int a = 0; a < n; ++a) {
+                if (posspec_in[a] < 0 || posspec_in[a] >= c->p.F || posspec_in[n + a] < 0 || posspec_in[n + a] >= c->p.F)
+                    return fail(c, TDM_EINVAL, "tdm_reconstruct: specular position outside the field");
+                tmp[a] = make_int2(posspec_in[a], posspec_in[n + a]);
+            }
+            TDM_CU(cudaMemcpyAsync(c->b.posspec, tmp.data(), n * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+            TDM_CU(cudaStreamSynchronize(c->stream));
+        }
+    }
+    TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
+    int rc = run_volume(c, n, indice_out, absorption_out, otf_out, counts_out);
+    if (rc) return rc;
+    if (fields_in && !is_device_ptr(fields_in)) return tdm_synchronize(c);
+    return TDM_OK;
+}
+
+int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                 uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out) {
+    if (!c || !holos || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
+        return fail(c, TDM_EINVAL, "tdm_pipeline: invalid argument");
+    cudaSetDevice(c->device);
+    TDM_CU(cudaEventRecord(c->ev_stage[0], c->stream));
+    if (int rc = stage_extract(c, holos, bits, n)) return rc;
+    TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));
+    c->n_spectra = n;
+    if (int rc = launch_fields(c, 0, n, nullptr, nullptr, nullptr)) return fail(c, rc, "fields launch failed");
+    TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
+    c->n_fields = n;
+    if (posspec_out && is_device_ptr(posspec_out)) {
+        Launch l(c, K_POSSPEC);
+        k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
+    }
+    int rc = run_volume(c, n, indice_out, absorption_out, otf_out, counts_out);
+    if (rc) return rc;
+    if (posspec_out && !is_device_ptr(posspec_out)) {
+        std::vector<int2> tmp(n);
+        TDM_CU(cudaMemcpyAsync(tmp.data(), c->b.posspec, n * sizeof(int2), cudaMemcpyDeviceToHost, c->stream));
+        TDM_CU(cudaStreamSynchronize(c->stream));
+        for (int a = 0; a < n; ++a) {
+            posspec_out[a] = tmp[a].x;
+            posspec_out[n + a] = tmp[a].y;
+        }
+    }
+    if (!is_device_ptr(holos)) return tdm_synchronize(c);
+    return TDM_OK;
+}
+
+}  // extern "C"

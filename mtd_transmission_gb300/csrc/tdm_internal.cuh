@@ -1,0 +1,137 @@
+// Internal declarations shared by the kernel and API translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tdm.h"
+#include "fft_core.cuh"
+
+namespace tdm {
+
+constexpr int kNC = 15;  // degree-4 2D polynomial: 15 monomials
+
+// Device-side parameters of one volume, fixed at context creation.
+struct Params {
+    int H, N, F, L, D;
+    int x0, y0;              // crop corner in the fftshifted hologram spectrum
+    int born, c_aber, deroul;
+    int disc_thr;            // fd^2 < disc_thr  <=>  fd^2 < COEF_NA_OBJ_LIMIT * N^2
+    int zmin, band;          // cap planes z in [zmin, zmin + band)
+    double rayon, inv_rayon;
+    float cap_scale;         // (k0/pi)*(-2pi) of retroPropag_Born, k0 in float
+    float dx2;               // tailleTheoPixelUborn^2
+    float out_scale;         // Delta_f^3 * (-1/(2 n0 kv^2))
+};
+
+// Device buffers (all owned by the context).
+struct Buffers {
+    float2* tw = nullptr;          // kTwN twiddles
+    float* tuk_h = nullptr;        // H, hologram Tukey alpha 0.05 (1D factor)
+    float* tuk_f = nullptr;        // F, field Tukey alpha 0.1 (1D factor)
+    double* s_tab = nullptr;       // F*F, sqrt(rayon^2 - fd^2) at [fdy+N][fdx+N]
+    float* s_tabf = nullptr;       // float copy
+    uint8_t* holo_stage = nullptr; // host staging: 2 x chunk x H*H*2 bytes
+    float2* inter = nullptr;       // chunk x H x F (extraction row pass)
+    float2* spectra = nullptr;     // max_angles x F*F
+    int2* posspec = nullptr;       // max_angles
+    float2* specval = nullptr;     // max_angles
+    double* fzm0 = nullptr;        // max_angles (negative: angle skipped)
+    float2* I1 = nullptr;          // chunk x F*F
+    float* phase = nullptr;        // chunk x F*F
+    float* amp = nullptr;          // chunk x F*F
+    float* gx = nullptr;           // chunk x L*L
+    float2* qc = nullptr;          // chunk x L*L
+    float2* tq = nullptr;          // chunk x L*F
+    float* unwrapped = nullptr;    // chunk x F*F
+    double* beta = nullptr;        // chunk x 2 x kNC
+    float2* fields = nullptr;      // max_angles x F*F
+    float2* r1 = nullptr;          // chunk x F*F
+    float2* rec_val = nullptr;     // max_angles x F*F
+    int16_t* rec_z = nullptr;      // max_angles x F*F
+    double2* acc = nullptr;        // (D*D/128) x band x 128 gather accumulators (scratch)
+    float2* vol = nullptr;         // D^3 complex, [y][x][z] layout
+    float* out_re = nullptr;       // D^3 staging when the caller's output is in host memory
+    float* out_im = nullptr;
+    uint8_t* out_otf = nullptr;
+    uint32_t* out_cnt = nullptr;
+    int* samp_idx = nullptr;       // nsamp aberration sample pixels
+    float* samp_q = nullptr;       // nsamp x kNC orthonormal basis values
+    double* rinv = nullptr;        // kNC x kNC: monomial coefficients from basis coefficients
+    int* err = nullptr;            // device error flags
+};
+
+// Kernel names for the opt-in per-launch profiler (tdm_profile).
+enum KernelId {
+    K_EXTRACT_ROWS, K_EXTRACT_COLS, K_ARGMAX, K_FIELD_ROWS, K_FIELD_COLS, K_VOLKOV_ROWS, K_VOLKOV_COLS,
+    K_VOLKOV_INTEG_ROWS, K_VOLKOV_INTEG_COLS, K_ABER_FIT, K_FORM, K_FZM0, K_CAP_ROWS, K_CAP_COLS, K_GATHER,
+    K_YPASS, K_XPASS, K_POSSPEC, K_COUNT
+};
+extern const char* const kKernelNames[K_COUNT];
+
+struct ProfRec {
+    int id;
+    cudaEvent_t a, b;
+};
+
+}  // namespace tdm
+
+struct tdm_ctx {
+    tdm_geom g{};
+    tdm_derived dv{};
+    tdm::Params p{};
+    tdm::Buffers b{};
+    int max_angles = 0;
+    int chunk = 16;              // angles per chunk of the per-angle stages
+    int holo_chunk = 16;         // holograms per extraction chunk
+    int nsamp = 0;
+    int device = 0;
+    int n_fields = 0;            // angles held in b.fields / b.posspec
+    int n_spectra = 0;           // angles held in b.spectra
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy[2] = {nullptr, nullptr};
+    cudaEvent_t ev_free[2] = {nullptr, nullptr};
+    cudaEvent_t ev_stage[8] = {};
+    uint64_t launches = 0;
+    bool prof = false;
+    std::vector<tdm::ProfRec> prof_recs;
+    std::vector<cudaEvent_t> ev_pool;
+    std::string last_error;
+};
+
+// Kernel launchers (defined in the kernel translation units).
+namespace tdm {
+// Scope around one kernel launch on c->stream: counts the launch and, when
+// profiling is on, brackets it with a pair of CUDA events.
+cudaEvent_t prof_event(tdm_ctx* c);
+struct Launch {
+    tdm_ctx* c;
+    int id;
+    cudaEvent_t b = nullptr;
+    Launch(tdm_ctx* ctx, int kid) : c(ctx), id(kid) {
+        if (c->prof) {
+            cudaEvent_t a = prof_event(c);
+            b = prof_event(c);
+            cudaEventRecord(a, c->stream);
+            c->prof_recs.push_back(ProfRec{id, a, b});
+        }
+    }
+    ~Launch() {
+        if (b) cudaEventRecord(b, c->stream);
+        c->launches++;
+    }
+};
+// extraction of holograms [0, n) from device memory into spectra[a0, a0 + n)
+int launch_extract(tdm_ctx* c, const void* holos_dev, int bits, int n, int a0);
+// per-angle field formation for spectra [a0, a0 + n)
+int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp);
+// per-field spectra and cap contributions for fields [0, n)
+int launch_cap(tdm_ctx* c, int n);
+// gather, normalisation and 3D inverse FFT into the output buffers
+int launch_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt);
+// one-off kernels
+int launch_fzm0(tdm_ctx* c, int n);
+}  // namespace tdm

@@ -1,0 +1,215 @@
+"""ctypes wrapper of the FP64 CPU oracle (``tdm_oracle.cpp``).
+
+Test infrastructure only: imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` as the checker.  Parity is unpinned:
+the reference cannot be built here and ships no golden vectors for this path,
+so the oracle restates the reference functions (cited file:line in the C++).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "liboracle_tdm.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle_tdm.so with the Makefile beside this file."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "tdm_oracle.cpp"))
+    ):
+        subprocess.run(["make", "-C", _HERE, "-s", "-B" if force else "all"], check=True)
+    return _LIB_PATH
+
+
+class OrcCfg(ctypes.Structure):
+    _fields_ = [
+        ("n0", ctypes.c_double), ("na", ctypes.c_double), ("lambda0", ctypes.c_double),
+        ("f_tube", ctypes.c_double), ("f_obj", ctypes.c_double), ("tpcam", ctypes.c_double),
+        ("rf", ctypes.c_double), ("coef_na_obj_limit", ctypes.c_double),
+        ("ccd_roix", ctypes.c_int), ("nxmax", ctypes.c_int), ("circle_cx", ctypes.c_int),
+        ("circle_cy", ctypes.c_int), ("dim_final", ctypes.c_int),
+        ("born", ctypes.c_int), ("c_aber", ctypes.c_int), ("deroul", ctypes.c_int), ("volkov", ctypes.c_int),
+    ]
+
+
+class OrcDerived(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("rayon", "tp_holo", "tp_uborn", "tp_tomo", "delta_f")]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        L.orc_derive.argtypes = [ctypes.POINTER(OrcCfg), ctypes.POINTER(OrcDerived)]
+        L.orc_tukey2d.argtypes = [ctypes.c_int, ctypes.c_float, P]
+        L.orc_fft2d.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_fft3d.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_extract.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
+        L.orc_coord_spec.argtypes = [P, ctypes.c_int]
+        L.orc_calc_uborn2.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+        L.orc_volkov.argtypes = [P, ctypes.c_int, P]
+        L.orc_aber_surface.argtypes = [P, ctypes.c_int, P, P]
+        L.orc_fields.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OrcCfg), P, P, P, P, P, P, P, P]
+        L.orc_reconstruction.argtypes = [P, P, ctypes.c_int, ctypes.POINTER(OrcCfg), P, P, P, P, P]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f32(v) -> float:
+    """extract_val returns float: keys are rounded to single precision."""
+    return float(np.float32(v))
+
+
+@dataclass
+class Config:
+    """Keys of config_manip.txt / recon.txt used on the path."""
+    ccd_roix: int = 512
+    nxmax: int = 64
+    circle_cx: int = 128
+    circle_cy: int = 128
+    dim_final: int = 256
+    na: float = 1.40
+    n0: float = 1.515
+    lambda0: float = 633e-9
+    f_tube: float = 0.15
+    f_obj: float = 0.002
+    tpcam: float = 5.5e-6
+    rf: float = 0.75
+    born: int = 1
+    c_aber: int = 1
+    deroul: int = 1
+    volkov: int = 1
+    coef_na_obj_limit: float = 1.0
+
+    def cstruct(self) -> OrcCfg:
+        return OrcCfg(
+            n0=_f32(self.n0), na=_f32(self.na), lambda0=_f32(self.lambda0), f_tube=_f32(self.f_tube),
+            f_obj=_f32(self.f_obj), tpcam=_f32(self.tpcam), rf=_f32(self.rf),
+            coef_na_obj_limit=_f32(self.coef_na_obj_limit), ccd_roix=self.ccd_roix, nxmax=self.nxmax,
+            circle_cx=self.circle_cx, circle_cy=self.circle_cy, dim_final=self.dim_final,
+            born=int(self.born), c_aber=int(self.c_aber), deroul=int(self.deroul), volkov=int(self.volkov))
+
+
+def derive(cfg: Config) -> dict:
+    d = OrcDerived()
+    c = cfg.cstruct()
+    lib().orc_derive(ctypes.byref(c), ctypes.byref(d))
+    return {n: getattr(d, n) for n, _ in OrcDerived._fields_}
+
+
+def tukey2d(n: int, alpha: float) -> np.ndarray:
+    out = np.empty((n, n), np.float64)
+    lib().orc_tukey2d(n, alpha, _p(out))
+    return out
+
+
+def fft2d(a: np.ndarray, sign: int = -1) -> np.ndarray:
+    x = np.ascontiguousarray(a, np.complex128).copy()
+    assert lib().orc_fft2d(_p(x), x.shape[0], sign) == 0
+    return x
+
+
+def fft3d(a: np.ndarray, sign: int = -1) -> np.ndarray:
+    x = np.ascontiguousarray(a, np.complex128).copy()
+    assert lib().orc_fft3d(_p(x), x.shape[0], sign) == 0
+    return x
+
+
+def extract(holo: np.ndarray, cfg: Config) -> np.ndarray:
+    """holo2TF_UBorn for one hologram (H x H samples) -> F x F complex crop."""
+    H = holo.shape[0]
+    tk = tukey2d(H, 0.05)
+    h = np.ascontiguousarray(holo, np.float64)
+    F = 2 * cfg.nxmax
+    out = np.empty((F, F), np.complex128)
+    rc = lib().orc_extract(_p(h), H, cfg.nxmax, cfg.circle_cx, cfg.circle_cy, _p(tk), _p(out))
+    if rc != 0:
+        raise ValueError(f"orc_extract failed rc={rc}")
+    return out
+
+
+def extract_stack(holos: np.ndarray, cfg: Config) -> np.ndarray:
+    return np.stack([extract(h, cfg) for h in holos])
+
+
+def coord_spec(spec: np.ndarray) -> int:
+    s = np.ascontiguousarray(spec, np.complex128)
+    return int(lib().orc_coord_spec(_p(s), s.shape[0]))
+
+
+def calc_uborn2(spec: np.ndarray, px: int, py: int) -> np.ndarray:
+    s = np.ascontiguousarray(spec, np.complex128)
+    out = np.empty_like(s)
+    lib().orc_calc_uborn2(_p(s), s.shape[0], px, py, _p(out))
+    return out
+
+
+def volkov(phase: np.ndarray) -> np.ndarray:
+    p = np.ascontiguousarray(phase, np.float64)
+    out = np.empty_like(p)
+    lib().orc_volkov(_p(p), p.shape[0], _p(out))
+    return out
+
+
+def aber_surface(img: np.ndarray, mask: np.ndarray | None = None):
+    im = np.ascontiguousarray(img, np.float64)
+    F = im.shape[0]
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    out = np.empty_like(im)
+    n = lib().orc_aber_surface(_p(m), F, _p(im), _p(out))
+    if n < 0:
+        raise ValueError("aberration fit undefined (<= 9 background samples)")
+    return out
+
+
+def fields(spectra: np.ndarray, cfg: Config, mask: np.ndarray | None = None, debug: bool = False):
+    """Second loop of tomo_pretraitement: returns (fields, tabPosSpec[, dbg])."""
+    s = np.ascontiguousarray(spectra, np.complex128)
+    M, F, _ = s.shape
+    out = np.empty_like(s)
+    pos = np.empty(2 * M, np.float64)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    dbg = {k: np.empty((M, F, F), np.float64) for k in ("phase", "unwrap", "amp", "phase_corr", "amp_corr")} if debug else {}
+    c = cfg.cstruct()
+    rc = lib().orc_fields(_p(s), M, cfg.nxmax, ctypes.byref(c), _p(m), _p(out), _p(pos),
+                          _p(dbg.get("phase")), _p(dbg.get("unwrap")), _p(dbg.get("amp")),
+                          _p(dbg.get("phase_corr")), _p(dbg.get("amp_corr")))
+    if rc != 0:
+        raise ValueError(f"orc_fields failed rc={rc}")
+    return (out, pos, dbg) if debug else (out, pos)
+
+
+def reconstruction(fields_: np.ndarray, posspec: np.ndarray, cfg: Config, want_counts=True, want_otf=True,
+                   want_spectrum=False, want_indice=True):
+    f = np.ascontiguousarray(fields_, np.complex128)
+    p = np.ascontiguousarray(posspec, np.float64)
+    M = f.shape[0]
+    D = cfg.dim_final
+    ind = np.empty((D, D, D), np.complex128)
+    secs = np.zeros(2, np.float64)
+    cnt = np.empty((D, D, D), np.float64) if want_counts else None
+    otf = np.empty((D, D, D), np.float64) if want_otf else None
+    spc = np.empty((D, D, D), np.complex128) if want_spectrum else None
+    c = cfg.cstruct()
+    rc = lib().orc_reconstruction(_p(f), _p(p), M, ctypes.byref(c), _p(ind), _p(cnt), _p(otf), _p(spc), _p(secs))
+    if rc != 0:
+        raise ValueError(f"orc_reconstruction failed rc={rc}")
+    return {"indice": ind, "counts": cnt, "otf": otf, "spectrum": spc, "seconds": secs}
+
+
+def set_threads(n: int) -> int:
+    return int(lib().orc_set_threads(n))

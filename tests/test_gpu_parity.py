@@ -1,0 +1,203 @@
+"""GPU parity against the FP64 oracle, stage by stage and end to end.
+
+Bars: bit-exact specular positions, hit counts and OTF masks; rel-L2 <= 1e-4
+on spectra, fields and volumes (FP32 FFTs vs the FP64 oracle).
+"""
+from __future__ import annotations
+
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+import oracle
+from mtd_transmission_gb300 import Context, Geometry, TdmError
+from tests.helpers import c64, oracle_cfg, rel_l2, small_case
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def _wrap(d):
+    return np.angle(np.exp(1j * d))
+
+
+@pytest.fixture(scope="module")
+def born():
+    acq, ph, d = small_case("plain_512_born", M=8)
+    cfg = oracle_cfg(acq)
+    spec = oracle.extract_stack(d["holos"].astype(np.float64), cfg)
+    fields, pos, dbg = oracle.fields(spec, cfg, d["mask"], debug=True)
+    return acq, cfg, d, spec, fields, pos, dbg
+
+
+@pytest.fixture(scope="module")
+def rytov():
+    acq, ph, d = small_case("rytov_1024", M=8, ccd_roix=512, nxmax=64, circle_cx=128, circle_cy=128,
+                            dim_final=256)
+    cfg = oracle_cfg(acq)
+    spec = oracle.extract_stack(d["holos"].astype(np.float64), cfg)
+    fields, pos, dbg = oracle.fields(spec, cfg, d["mask"], debug=True)
+    return acq, cfg, d, spec, fields, pos, dbg
+
+
+def test_extract_parity(born):
+    acq, cfg, d, spec, *_ = born
+    F = 2 * acq.nxmax
+    with Context(Geometry.from_acquisition(acq), 8) as ctx:
+        out = np.zeros((8, F, F), np.complex64)
+        ctx.extract(np.ascontiguousarray(d["holos"]), spectra_out=out)
+    for a in range(8):
+        assert rel_l2(out[a], spec[a]) <= TOL, a
+
+
+def test_extract_8bit():
+    acq, ph, d = small_case("plain_512_born", M=3)
+    h8 = np.ascontiguousarray((d["holos"] >> 4).astype(np.uint8))
+    cfg = oracle_cfg(acq)
+    ref = oracle.extract_stack(h8.astype(np.float64), cfg)
+    F = 2 * acq.nxmax
+    with Context(Geometry.from_acquisition(acq), 3) as ctx:
+        out = np.zeros((3, F, F), np.complex64)
+        ctx.extract(h8, spectra_out=out)
+    for a in range(3):
+        assert rel_l2(out[a], ref[a]) <= TOL
+
+
+@pytest.mark.parametrize("case", ["born", "rytov"])
+def test_fields_parity(case, request):
+    acq, cfg, d, spec, fields, pos, dbg = request.getfixturevalue(case)
+    F, M = 2 * acq.nxmax, spec.shape[0]
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        fo = np.zeros((M, F, F), np.complex64)
+        po = np.zeros(2 * M, np.int32)
+        ph = np.zeros((M, F, F), np.float32)
+        un = np.zeros((M, F, F), np.float32)
+        am = np.zeros((M, F, F), np.float32)
+        ctx.fields_debug(c64(spec), fields_out=fo, posspec_out=po, phase=ph, unwrapped=un, amp=am)
+    np.testing.assert_array_equal(po, pos.astype(np.int32))
+    for a in range(M):
+        assert rel_l2(am[a], dbg["amp"][a]) <= TOL, ("amp", a)
+        big = dbg["amp"][a] > 1e-3 * dbg["amp"][a].max()
+        assert np.abs(_wrap(ph[a] - dbg["phase"][a]))[big].max() < 1e-3, ("phase", a)
+        assert rel_l2(un[a], dbg["unwrap"][a]) <= TOL, ("unwrap", a)
+        assert rel_l2(fo[a], fields[a]) <= TOL, ("field", a)
+
+
+@pytest.mark.parametrize("over", [dict(c_aber=0), dict(deroul=0)])
+def test_fields_options(over):
+    acq, ph, d = small_case("plain_512_born", M=4, **over)
+    cfg = oracle_cfg(acq)
+    spec = oracle.extract_stack(d["holos"].astype(np.float64), cfg)
+    fields, pos = oracle.fields(spec, cfg, d["mask"])
+    F = 2 * acq.nxmax
+    with Context(Geometry.from_acquisition(acq), 4) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        fo = np.zeros((4, F, F), np.complex64)
+        po = np.zeros(8, np.int32)
+        ctx.fields(c64(spec), fields_out=fo, posspec_out=po)
+    np.testing.assert_array_equal(po, pos.astype(np.int32))
+    for a in range(4):
+        assert rel_l2(fo[a], fields[a]) <= TOL, a
+
+
+@pytest.mark.parametrize("case", ["born", "rytov"])
+def test_reconstruct_parity(case, request):
+    acq, cfg, d, spec, fields, pos, dbg = request.getfixturevalue(case)
+    D, M = acq.dim_final, spec.shape[0]
+    ref = oracle.reconstruction(fields, pos, cfg)
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        re = np.zeros((D, D, D), np.float32)
+        im = np.zeros((D, D, D), np.float32)
+        otf = np.zeros((D, D, D), np.uint8)
+        cnt = np.zeros((D, D, D), np.uint32)
+        ctx.reconstruct(c64(fields), pos.astype(np.int32), indice=re, absorption=im, otf=otf, counts=cnt)
+    np.testing.assert_array_equal(cnt, ref["counts"].astype(np.uint32))
+    np.testing.assert_array_equal(otf, ref["otf"].astype(np.uint8))
+    assert rel_l2(re, ref["indice"].real) <= TOL
+    assert rel_l2(im, ref["indice"].imag) <= TOL
+
+
+def test_pipeline_end_to_end(born):
+    acq, cfg, d, spec, fields, pos, dbg = born
+    D, M = acq.dim_final, spec.shape[0]
+    ref = oracle.reconstruction(fields, pos, cfg)
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        re = np.zeros((D, D, D), np.float32)
+        im = np.zeros((D, D, D), np.float32)
+        cnt = np.zeros((D, D, D), np.uint32)
+        po = np.zeros(2 * M, np.int32)
+        ctx.pipeline(np.ascontiguousarray(d["holos"]), indice=re, absorption=im, counts=cnt, posspec=po)
+        assert ctx.launch_count > 0
+    np.testing.assert_array_equal(po, pos.astype(np.int32))
+    np.testing.assert_array_equal(cnt, ref["counts"].astype(np.uint32))
+    assert rel_l2(re, ref["indice"].real) <= TOL
+    assert rel_l2(im, ref["indice"].imag) <= TOL
+
+
+def test_reconstruct_edge_positions():
+    """Specular positions at the crop edges and corners (corner angles fall
+    outside the Ewald sphere and are skipped by the reference)."""
+    acq, ph, d = small_case("plain_512_born", M=1)
+    N, F, D = acq.nxmax, 2 * acq.nxmax, acq.dim_final
+    rng = np.random.default_rng(5)
+    pos_xy = [(0, 0), (F - 1, F - 1), (0, N), (N, F - 1), (N, N), (F - 1, 0), (N + 10, N - 33)]
+    M = len(pos_xy)
+    f = (rng.standard_normal((M, F, F)) + 1j * rng.standard_normal((M, F, F))) * 0.1
+    pos = np.array([p[0] for p in pos_xy] + [p[1] for p in pos_xy], np.float64)
+    cfg = oracle_cfg(acq)
+    ref = oracle.reconstruction(f, pos, cfg)
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        re = np.zeros((D, D, D), np.float32)
+        im = np.zeros((D, D, D), np.float32)
+        cnt = np.zeros((D, D, D), np.uint32)
+        ctx.reconstruct(c64(f), pos.astype(np.int32), indice=re, absorption=im, counts=cnt)
+    np.testing.assert_array_equal(cnt, ref["counts"].astype(np.uint32))
+    assert rel_l2(re, ref["indice"].real) <= TOL
+    assert rel_l2(im, ref["indice"].imag) <= TOL
+
+
+def test_single_angle_counts():
+    """One angle: every in-disc cap pixel is hit exactly once."""
+    acq, ph, d = small_case("plain_512_born", M=1)
+    N, F, D = acq.nxmax, 2 * acq.nxmax, acq.dim_final
+    f = np.ones((1, F, F), np.complex64)
+    with Context(Geometry.from_acquisition(acq), 1) as ctx:
+        cnt = np.zeros((D, D, D), np.uint32)
+        ctx.reconstruct(f, np.array([N + 3, N - 5], np.int32), counts=cnt)
+    fd = np.arange(-N, N)
+    disc = (fd[:, None] ** 2 + fd[None, :] ** 2) < N * N
+    assert cnt.sum() == disc.sum() and cnt.max() == 1
+
+
+def test_device_buffers_match_host():
+    """Device (torch CUDA) inputs and outputs give the same volume as host buffers."""
+    import torch
+    acq, ph, d = small_case("plain_512_born", M=4)
+    D = acq.dim_final
+    with Context(Geometry.from_acquisition(acq), 4) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        re_h = np.zeros((D, D, D), np.float32)
+        ctx.pipeline(np.ascontiguousarray(d["holos"]), indice=re_h)
+        h_dev = torch.from_numpy(np.ascontiguousarray(d["holos"])).cuda()
+        re_d = torch.zeros((D, D, D), dtype=torch.float32, device="cuda")
+        ctx.pipeline(h_dev, indice=re_d)
+        ctx.synchronize()
+    np.testing.assert_array_equal(re_d.cpu().numpy(), re_h)
+
+
+def test_invalid_geometry():
+    acq, ph, d = small_case("plain_512_born", M=1)
+    for over in (dict(dim_final=128), dict(nxmax=60), dict(circle_cx=10), dict(ccd_roix=500)):
+        with pytest.raises(TdmError):
+            Context(Geometry.from_acquisition(replace(acq, **over)), 1)
+
+
+def test_mask_without_background():
+    acq, ph, d = small_case("plain_512_born", M=1)
+    F = 2 * acq.nxmax
+    with Context(Geometry.from_acquisition(acq), 1) as ctx:
+        with pytest.raises(TdmError):
+            ctx.set_mask(np.zeros((F, F), np.uint8))
