@@ -172,9 +172,12 @@ int tdm_read_geom(const char* recon_txt, const char* config_manip_txt, tdm_geom*
 int tdm_read_pgm(const char* path, int roi, void* buf, int* bits);
 int tdm_pgm_info(const char* path, int* width, int* height, int* maxval);
 /* Float32 multi-page TIFF writer (SAV3D_Tiff_Optimized,
- * Reconstruction/src/fonctions.cpp:2286-2357): D pages of D x D, ORIENTATION_BOTLEFT,
- * resolution 0.01/pixel_size per cm. */
-int tdm_write_tiff_f32(const char* path, const float* vol, int dim_x, int dim_y, int pages, double pixel_size);
+ * Reconstruction/src/fonctions.cpp:2286-2357, pages of dim_x x dim_y, resolution
+ * 0.01/pixel_size per cm; BigTIFF beyond 4 GB).  orientation is the TIFF
+ * Orientation tag: 4 (BOTLEFT) for the volumes, 1 (TOPLEFT) for the 2D images
+ * of SAV_Tiff2D (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:364-400). */
+int tdm_write_tiff_f32(const char* path, const float* vol, int dim_x, int dim_y, int pages, double pixel_size,
+                       int orientation);
 
 #ifdef __cplusplus
 }

@@ -96,7 +96,7 @@ def lib():
     L.tdm_read_geom.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(Geometry)]
     L.tdm_read_pgm.argtypes = [ctypes.c_char_p, I, P, ctypes.POINTER(I)]
     L.tdm_pgm_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
-    L.tdm_write_tiff_f32.argtypes = [ctypes.c_char_p, P, I, I, I, D]
+    L.tdm_write_tiff_f32.argtypes = [ctypes.c_char_p, P, I, I, I, D, I]
     L.tdm_profile.argtypes = [P, I]
     L.tdm_profile_count.argtypes = []
     L.tdm_profile_read.argtypes = [P, I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(D), ctypes.POINTER(I)]
@@ -272,9 +272,11 @@ def read_pgm(path: str, roi: int) -> np.ndarray:
     return out
 
 
-def write_tiff(path: str, vol: np.ndarray, pixel_size: float):
+def write_tiff(path: str, vol: np.ndarray, pixel_size: float, orientation: int = 4):
     v = np.ascontiguousarray(vol, np.float32)
+    if v.ndim == 2:
+        v = v[None]
     pages, hgt, wdt = v.shape
-    rc = lib().tdm_write_tiff_f32(path.encode(), ptr(v), wdt, hgt, pages, pixel_size)
+    rc = lib().tdm_write_tiff_f32(path.encode(), ptr(v), wdt, hgt, pages, pixel_size, orientation)
     if rc != TDM_OK:
         raise TdmError(rc, f"cannot write {path}")

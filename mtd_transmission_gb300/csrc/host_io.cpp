@@ -221,7 +221,8 @@ int tdm_read_pgm(const char* path, int roi, void* buf, int* bits) {
     return TDM_OK;
 }
 
-int tdm_write_tiff_f32(const char* path, const float* vol, int wdt, int hgt, int pages, double pixel_size) {
+int tdm_write_tiff_f32(const char* path, const float* vol, int wdt, int hgt, int pages, double pixel_size,
+                       int orientation) {
     if (!path || !vol || wdt <= 0 || hgt <= 0 || pages <= 0) return TDM_EINVAL;
     FILE* f = std::fopen(path, "wb");
     if (!f) return TDM_EIO;
@@ -278,7 +279,7 @@ int tdm_write_tiff_f32(const char* path, const float* vol, int wdt, int hgt, int
         tag(259, SHORT, 1, 1);                                      // Compression: none
         tag(262, SHORT, 1, 1);                                      // Photometric: min-is-black
         tag(273, big ? LONG8 : LONG, 1, data_off);                  // StripOffsets
-        tag(274, SHORT, 1, 4);                                      // Orientation: BOTLEFT
+        tag(274, SHORT, 1, (uint16_t)orientation);                  // Orientation
         tag(277, SHORT, 1, 1);                                      // SamplesPerPixel
         tag(278, LONG, 1, (uint32_t)hgt);                           // RowsPerStrip
         tag(279, big ? LONG8 : LONG, 1, page_bytes);                // StripByteCounts

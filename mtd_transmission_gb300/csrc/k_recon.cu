@@ -136,7 +136,7 @@ k_gather(const float2* __restrict__ rec_val, const int16_t* __restrict__ rec_z, 
     const int tid = threadIdx.x, tx = tid % kGX, ty = tid / kGX;
     const int X0 = blockIdx.x * kGX, Y0 = blockIdx.y * kGY;
     const int X = X0 + tx, Y = Y0 + ty;
-    const int F = p.F, N = p.N, band = p.band, zmin = p.zmin;
+    const int F = p.F, band = p.band, zmin = p.zmin;
     double2* acc = acc_all + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * band * kGC;
     for (int i = tid; i < M; i += kGC) sp[i] = posspec[i];
     for (int zb = 0; zb < band; ++zb) {

@@ -1,0 +1,155 @@
+"""Host-side file contracts and the C ABI surface (no GPU needed).
+
+Covers: every function declared in include/tdm.h is exported by libtdm.so;
+extract_val semantics of the reference's KEY value files; the derived
+geometry against the oracle; PGM reading (8/16-bit, comments, ROI); the
+float32 multi-page TIFF writer.
+"""
+from __future__ import annotations
+
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+import oracle
+from mtd_transmission_gb300 import api, simul
+from mtd_transmission_gb300.api import Geometry
+from tests.helpers import oracle_cfg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    txt = open(os.path.join(ROOT, "include", "tdm.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(tdm_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_function():
+    lib = api.lib()
+    declared = _header_functions()
+    assert len(declared) >= 20
+    missing = [f for f in declared if not hasattr(lib, f)]
+    assert not missing, missing
+    assert sorted(api.EXPORTS) == declared
+
+
+def test_extract_val_semantics(tmp_path):
+    f = tmp_path / "recon.txt"
+    f.write_text("# comment\nNXMAX 64\n\n#NXMAX 99\nNA 1.40\nNA 1.2\nLAMBDA 0.000000633\nFLAG\nWIN 5\r\n")
+    p = str(f)
+    assert api.extract_val(p, "NXMAX") == (64.0, True)
+    assert api.extract_val(p, "NA")[0] == float(np.float32(1.2))        # last occurrence wins, float-rounded
+    assert api.extract_val(p, "LAMBDA")[0] == float(np.float32(6.33e-7))
+    assert api.extract_val(p, "MISSING", 7.5) == (7.5, False)
+    assert api.extract_val(p, "WIN")[0] == 5.0                           # trailing CR ignored by atof
+    assert api.extract_val(p, "FLAG")[0] == 0.0                          # key without value reads 0
+    assert api.extract_string(p, "NXMAX") == "64"
+    with pytest.raises(api.TdmError):
+        api.extract_val(str(tmp_path / "absent.txt"), "NXMAX")
+
+
+@pytest.mark.parametrize("name", ["plain_512_born", "rytov_1024", "large_2048"])
+def test_read_geom_and_derive(tmp_path, name):
+    acq, _, _ = simul.workload(name)
+    (tmp_path / "recon.txt").write_text(acq.recon_txt())
+    (tmp_path / "config_manip.txt").write_text(acq.config_manip_txt())
+    g = api.read_geom(str(tmp_path / "recon.txt"), str(tmp_path / "config_manip.txt"))
+    ref = Geometry.from_acquisition(acq)
+    for fname, _ in Geometry._fields_:
+        assert getattr(g, fname) == getattr(ref, fname), fname
+    d = api.derive(g)
+    o = oracle.derive(oracle_cfg(acq))
+    for k in ("rayon", "tp_holo", "tp_uborn", "tp_tomo", "delta_f"):
+        assert d[k] == o[k], k
+
+
+def _write_pgm(path, img, maxval, comment=True):
+    h, w = img.shape
+    hdr = b"P5\n" + (b"# written by the test\n" if comment else b"") + f"{w} {h}\n{maxval}\n".encode()
+    data = img.astype(">u2").tobytes() if maxval > 255 else img.astype(np.uint8).tobytes()
+    path.write_bytes(hdr + data)
+
+
+def test_pgm_16bit_big_endian_roi(tmp_path):
+    rng = np.random.default_rng(0)
+    img = rng.integers(0, 4096, (40, 48), dtype=np.uint16)
+    p = tmp_path / "i000.pgm"
+    _write_pgm(p, img, 4095)
+    out = api.read_pgm(str(p), 32)
+    assert out.dtype == np.uint16
+    np.testing.assert_array_equal(out, img[:32, :32])
+
+
+def test_pgm_8bit(tmp_path):
+    img = (np.arange(64 * 64) % 251).astype(np.uint8).reshape(64, 64)
+    p = tmp_path / "mask.pgm"
+    _write_pgm(p, img, 255, comment=False)
+    out = api.read_pgm(str(p), 64)
+    assert out.dtype == np.uint8
+    np.testing.assert_array_equal(out, img)
+
+
+def test_pgm_errors(tmp_path):
+    img = np.zeros((16, 16), np.uint16)
+    p = tmp_path / "t.pgm"
+    _write_pgm(p, img, 4095)
+    p.write_bytes(p.read_bytes()[:-10])          # truncated data
+    with pytest.raises(api.TdmError):
+        api.read_pgm(str(p), 16)
+    with pytest.raises(api.TdmError):             # ROI larger than the image
+        _write_pgm(p, img, 4095)
+        api.read_pgm(str(p), 32)
+    (tmp_path / "bad.pgm").write_bytes(b"P6\n2 2\n255\n" + bytes(12))
+    with pytest.raises(api.TdmError):
+        api.read_pgm(str(tmp_path / "bad.pgm"), 2)
+
+
+def _read_tiff(path):
+    """Minimal classic-TIFF reader: returns a list of (tags, float32 page)."""
+    b = open(path, "rb").read()
+    assert b[:4] == b"II*\x00"
+    off = struct.unpack_from("<I", b, 4)[0]
+    pages = []
+    while off:
+        n = struct.unpack_from("<H", b, off)[0]
+        tags = {}
+        for i in range(n):
+            tag, typ, cnt, val = struct.unpack_from("<HHII", b, off + 2 + 12 * i)
+            if typ == 3 and cnt == 1:
+                val &= 0xFFFF
+            if typ == 5:
+                num, den = struct.unpack_from("<II", b, val)
+                val = num / den
+            tags[tag] = (val if not (typ == 3 and cnt == 2) else (val & 0xFFFF, val >> 16))
+        w, h = tags[256], tags[257]
+        data = np.frombuffer(b, "<f4", w * h, tags[273]).reshape(h, w)
+        pages.append((tags, data))
+        off = struct.unpack_from("<I", b, off + 2 + 12 * n)[0]
+    return pages
+
+
+def test_tiff_volume_roundtrip(tmp_path):
+    rng = np.random.default_rng(2)
+    vol = rng.standard_normal((5, 12, 16)).astype(np.float32)
+    p = str(tmp_path / "indice.tif")
+    api.write_tiff(p, vol, 1.1e-7)
+    pages = _read_tiff(p)
+    assert len(pages) == 5
+    for z, (tags, data) in enumerate(pages):
+        np.testing.assert_array_equal(data, vol[z])
+        assert tags[258] == 32 and tags[339] == 3 and tags[274] == 4 and tags[296] == 3
+        assert tags[285] == (z, 5)
+        assert abs(tags[282] - 0.01 / np.float32(1.1e-7)) / tags[282] < 1e-6
+
+
+def test_tiff_2d_topleft(tmp_path):
+    img = np.arange(64, dtype=np.float32).reshape(8, 8)
+    p = str(tmp_path / "centres.tif")
+    api.write_tiff(p, img, 0.02, orientation=1)
+    (tags, data), = _read_tiff(p)
+    np.testing.assert_array_equal(data, img)
+    assert tags[274] == 1
