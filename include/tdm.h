@@ -135,6 +135,21 @@ int tdm_reconstruct(tdm_ctx* ctx, const float* fields_in, const int32_t* posspec
 int tdm_pipeline(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
                  uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out);
 
+/* Off-axis extraction that allocates nothing.  No counterpart in the
+ * reference: it is for callers that cannot allocate GPU memory, such as a
+ * camera acquisition loop that must not stall on cudaMalloc between bursts of
+ * frames, or a host application whose memory pool already owns the device.
+ * Same result as tdm_extract, without a context: holos (n*H*H uint8/uint16)
+ * and spectra_out (n*F*F complex) must be device memory; the work runs on
+ * `stream` (a cudaStream_t, 0 for the default stream) and the call returns
+ * without waiting.  Scratch lives in a fixed 4 MiB array inside the library
+ * (held by every GPU that loads it until exit): CCD_ROIX * 2*NXMAX may not
+ * exceed 524288 (TDM_EUNSUPPORTED otherwise).  The first call on a device
+ * looks up that array and uploads the twiddle and window tables; make it
+ * before any stream capture.  All calls share the scratch, so calls that
+ * overlap on the GPU (other streams or threads) race. */
+int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n, float* spectra_out, void* stream);
+
 /* Stream-ordered execution helpers. */
 int tdm_synchronize(tdm_ctx* ctx);
 void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */

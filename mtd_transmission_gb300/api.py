@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libtdm.so")
 
 TDM_OK = 0
 STATUS = {-1: "TDM_EINVAL", -2: "TDM_EUNSUPPORTED", -3: "TDM_ECUDA", -4: "TDM_ENOMEM", -5: "TDM_EDATA", -6: "TDM_EIO"}
+STATUS_CODES = {v: k for k, v in STATUS.items()}
 
 # Exported symbols declared in include/tdm.h.
 EXPORTS = (
@@ -26,6 +27,7 @@ EXPORTS = (
     "tdm_fields", "tdm_fields_debug", "tdm_reconstruct", "tdm_pipeline", "tdm_synchronize", "tdm_stream",
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
+    "tdm_extract_noalloc",
 )
 
 
@@ -97,6 +99,7 @@ def lib():
     L.tdm_read_pgm.argtypes = [ctypes.c_char_p, I, P, ctypes.POINTER(I)]
     L.tdm_pgm_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
     L.tdm_write_tiff_f32.argtypes = [ctypes.c_char_p, P, I, I, I, D, I]
+    L.tdm_extract_noalloc.argtypes = [ctypes.POINTER(Geometry), P, I, I, P, P]
     L.tdm_profile.argtypes = [P, I]
     L.tdm_profile_count.argtypes = []
     L.tdm_profile_read.argtypes = [P, I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(D), ctypes.POINTER(I)]
@@ -231,6 +234,17 @@ class Context:
         n = holos.shape[0] if n is None else n
         self._check(lib().tdm_pipeline(self._h, ptr(holos), self._bits(holos), n, ptr(indice), ptr(absorption),
                                        ptr(otf), ptr(counts), ptr(posspec)), "tdm_pipeline")
+
+
+def extract_noalloc(geom: Geometry, holos, spectra_out, stream: int = 0, n=None) -> int:
+    """tdm_extract_noalloc: extraction without any GPU allocation (device buffers only).
+
+    For callers that cannot allocate GPU memory (an acquisition loop that must
+    not stall on cudaMalloc, or an application whose memory pool owns the
+    device).  Returns the TDM status; the work is queued on `stream`."""
+    n = holos.shape[0] if n is None else n
+    return int(lib().tdm_extract_noalloc(ctypes.byref(geom), ptr(holos), Context._bits(holos), n, ptr(spectra_out),
+                                         ctypes.c_void_p(stream)))
 
 
 # ---- host-side file helpers -------------------------------------------------

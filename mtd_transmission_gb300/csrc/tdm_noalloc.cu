@@ -1,0 +1,152 @@
+// Allocation-free off-axis extraction.
+//
+// Some callers cannot allocate GPU memory: a camera acquisition loop that
+// extracts each burst of holograms as it arrives cannot afford cudaMalloc
+// (it may synchronise the device and stall the frame loop), and a host
+// application whose memory pool already owns the GPU's memory has none to
+// give.  tdm_extract_noalloc serves them: it runs the same extraction kernels
+// as tdm_extract, on the caller's device buffers and stream, and keeps its
+// scratch (the row-pass intermediate) in a fixed array compiled into this
+// library.  Every GPU that loads the library holds that array until the
+// process exits.
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
+#include "extract_kernels.cuh"
+#include "host_tables.h"
+
+namespace {
+
+using namespace tdm;
+using namespace tdm::extract;
+
+constexpr size_t kScratchBytes = size_t(4) << 20;  // 4 MiB: one 2048 x 256 band, or two 1024 x 256
+constexpr int kMaxH = 2048;
+constexpr int kTukeyLen = 256 + 512 + 1024 + 2048;  // one table per supported CCD_ROIX
+
+static __device__ __align__(256) float2 g_scratch[kScratchBytes / sizeof(float2)];
+static __device__ __align__(256) float2 g_twiddle[kTwN];
+static __device__ __align__(256) float g_tukey[kTukeyLen];
+
+int tukey_offset(int H) { return H - 256; }  // 256 -> 0, 512 -> 256, 1024 -> 768, 2048 -> 1792
+
+// Device addresses of the arrays above.  In host code the array names are
+// host-side stand-ins, not device addresses, so they are looked up once per
+// device with cudaGetSymbolAddress while that device is current.
+struct Symbols {
+    bool ready = false;
+    float2* scratch = nullptr;
+    float2* twiddle = nullptr;
+    float* tukey = nullptr;
+};
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+Symbols g_sym[kMaxDevices];
+
+int device_symbols(int dev, Symbols& out) {
+    if (dev < 0 || dev >= kMaxDevices) return TDM_EUNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_mu);
+    Symbols& s = g_sym[dev];
+    if (!s.ready) {
+        if (cudaGetSymbolAddress(reinterpret_cast<void**>(&s.scratch), g_scratch) != cudaSuccess ||
+            cudaGetSymbolAddress(reinterpret_cast<void**>(&s.twiddle), g_twiddle) != cudaSuccess ||
+            cudaGetSymbolAddress(reinterpret_cast<void**>(&s.tukey), g_tukey) != cudaSuccess) {
+            cudaGetLastError();
+            return TDM_ECUDA;
+        }
+        std::vector<float2> tw(kTwN);
+        for (int k = 0; k < kTwN; ++k) {
+            const long double a = -2.0L * 3.14159265358979323846264338327950288L * k / kTwN;
+            tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        std::vector<float> tk(kTukeyLen);
+        for (int H = 256; H <= kMaxH; H *= 2) {
+            const std::vector<double> t = tukey_factor(H, 0.05f);  // hologram window, main.cpp:105
+            for (int i = 0; i < H; ++i) tk[tukey_offset(H) + i] = (float)t[i];
+        }
+        if (cudaMemcpy(s.twiddle, tw.data(), kTwN * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s.tukey, tk.data(), kTukeyLen * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            return TDM_ECUDA;
+        }
+        s.ready = true;
+    }
+    out = s;
+    return TDM_OK;
+}
+
+bool on_device(const void* p) {
+    cudaPointerAttributes at;
+    if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+template <int H>
+int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F, int x0, int y0,
+        cudaStream_t st) {
+    using C = ExtractCfg<H>;
+    const size_t sm_rows = (size_t)C::PAIRS * padded_len(H) * sizeof(float2);
+    const size_t sm_cols = (size_t)C::COLS * padded_len(H) * sizeof(float2);
+    if (sm_rows > 48 * 1024 &&
+        cudaFuncSetAttribute(k_extract_rows<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
+        return TDM_ECUDA;
+    if (sm_cols > 48 * 1024 &&
+        cudaFuncSetAttribute(k_extract_cols<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_cols))
+        return TDM_ECUDA;
+    const size_t per_holo = (size_t)H * F * sizeof(float2);
+    const int chunk = (int)(kScratchBytes / per_holo);
+    const size_t in_bytes = (size_t)H * H * (bits == 16 ? 2 : 1);
+    for (int h0 = 0; h0 < n; h0 += chunk) {
+        const int m = n - h0 < chunk ? n - h0 : chunk;
+        k_extract_rows<H><<<dim3(H / 2 / C::PAIRS, m), C::PAIRS * C::T, sm_rows, st>>>(
+            static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), s.twiddle, s.scratch, F,
+            x0);
+        k_extract_cols<H><<<dim3(F / C::COLS, m), C::COLS * C::T, sm_cols, st>>>(
+            s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+}  // namespace
+
+extern "C" int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n, float* spectra_out,
+                                   void* stream) {
+    if (!geom || !holos || !spectra_out || n <= 0 || (bits != 8 && bits != 16)) return TDM_EINVAL;
+    const int H = geom->ccd_roix, N = geom->nxmax, F = 2 * N;
+    const int x0 = geom->circle_cx - N, y0 = geom->circle_cy - N;
+    if ((H & (H - 1)) || H < 256 || H > kMaxH || (F & (F - 1)) || F < 64 || F > 512) {
+        std::fprintf(stderr, "tdm_extract_noalloc: CCD_ROIX must be a power of two in [256, 2048] and 2*NXMAX in [64, 512]\n");
+        return TDM_EUNSUPPORTED;
+    }
+    if (x0 < 0 || y0 < 0 || x0 + F > H || y0 + F > H) {
+        std::fprintf(stderr, "tdm_extract_noalloc: crop window outside the hologram spectrum\n");
+        return TDM_EINVAL;
+    }
+    if ((size_t)H * F * sizeof(float2) > kScratchBytes) {
+        std::fprintf(stderr,
+                     "tdm_extract_noalloc: one %dx%d hologram needs %zu bytes of scratch; the fixed scratch holds %zu "
+                     "(CCD_ROIX * 2*NXMAX must not exceed 524288)\n",
+                     H, H, (size_t)H * F * sizeof(float2), kScratchBytes);
+        return TDM_EUNSUPPORTED;
+    }
+    if (!on_device(holos) || !on_device(spectra_out)) {
+        std::fprintf(stderr, "tdm_extract_noalloc: holograms and spectra must be in device memory\n");
+        return TDM_EINVAL;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TDM_ECUDA;
+    Symbols s;
+    if (int rc = device_symbols(dev, s)) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float2* out = reinterpret_cast<float2*>(spectra_out);
+    switch (H) {
+        case 256: return run<256>(s, holos, bits, n, out, F, x0, y0, st);
+        case 512: return run<512>(s, holos, bits, n, out, F, x0, y0, st);
+        case 1024: return run<1024>(s, holos, bits, n, out, F, x0, y0, st);
+        default: return run<2048>(s, holos, bits, n, out, F, x0, y0, st);
+    }
+}
