@@ -212,11 +212,16 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=8)
     ap.add_argument("--profile-out", default=None)
     ap.add_argument("--no-profile-pass", action="store_true", help="skip the per-kernel event pass")
+    ap.add_argument("--holograms", type=int, default=None, help="override the workload's hologram count")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    from dataclasses import replace
+
     from mtd_transmission_gb300 import simul
     acq, ph, seed = simul.workload(args.workload)
+    if args.holograms:
+        acq = replace(acq, nb_holo=args.holograms)
     world, rank, local = dist_setup()
 
     if args.impl == "reference":

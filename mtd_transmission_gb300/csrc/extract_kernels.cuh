@@ -24,7 +24,7 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
     const int pr = threadIdx.x / C::T, j = threadIdx.x % C::T;
     const int a = blockIdx.y;
     const int ya = 2 * (blockIdx.x * C::PAIRS + pr), yb = ya + 1;
-    float2* s = sm + pr * padded_len(H);
+    float2* s = sm + pr * tstride(H);
     const size_t base = (size_t)a * H * H;
     const float wa = tuk[ya], wb = tuk[yb];
 #pragma unroll
@@ -64,20 +64,22 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     extern __shared__ float2 sm[];
     constexpr int B = C::COLS;
     const int a = blockIdx.y;
+    constexpr int NT = B * C::T;
     const int c0 = blockIdx.x * B;
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    for (int i = threadIdx.x; i < B * H; i += blockDim.x) {
-        const int t = i % B, y = i / B;
-        sm[t * padded_len(H) + pad_idx(y)] = inter[((size_t)a * H + y) * F + c0 + t];
+#pragma unroll
+    for (int r = 0; r < B * H / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, y = i / B;
+        sm[t * tstride(H) + pad_idx(y)] = inter[((size_t)a * H + y) * F + c0 + t];
     }
     __syncthreads();
-    fft_smem<H, -1>(sm + tr * padded_len(H), j, tw);
+    fft_smem<H, -1>(sm + tr * tstride(H), j, tw);
     const float inv = 1.0f / ((float)H * (float)H);
     for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
         const int t = i % B, r = i / B;
         const int ky = y0 + r, kx = x0 + c0 + t;
         const float sg = ((kx + ky) & 1) ? -inv : inv;
-        spectra[((size_t)a * F + r) * F + c0 + t] = c_scale(sm[t * padded_len(H) + pad_idx(ky)], sg);
+        spectra[((size_t)a * F + r) * F + c0 + t] = c_scale(sm[t * tstride(H) + pad_idx(ky)], sg);
     }
 }
 

@@ -10,7 +10,7 @@
 //
 // Layout: logical point i of a transform lives at pad_idx(i) = i + i/16, one
 // spare complex every 16, which spreads the stride-R stores of the early
-// stages over all banks.
+// stages over all banks; transforms are tstride(N) (odd) complexes apart.
 //
 // Sign conventions follow FFTW: DIR = -1 is exp(-2 pi i jk/N) (forward),
 // DIR = +1 is exp(+2 pi i jk/N) (backward); neither is normalised.
@@ -25,6 +25,9 @@ constexpr int kTwN = 4096;  // twiddle table size: exp(-2 pi i k / 4096)
 
 __host__ __device__ constexpr int pad_idx(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4); }
+// Distance between consecutive transforms of a CTA in shared memory: odd, so
+// that B transforms read at the same logical index fall in distinct banks.
+__host__ __device__ constexpr int tstride(int n) { return padded_len(n) + 1; }
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -80,37 +83,42 @@ __device__ __forceinline__ void dft8(float2* x) {
 }
 
 // One Stockham stage on a transform held in shared memory (in place).
-// Every thread of the CTA must call it (it contains __syncthreads()).
+// Every thread of the CTA must call it (it contains __syncthreads()); threads
+// with active == false only take part in the barriers.
 template <int N, int R, int NS, int DIR>
-__device__ __forceinline__ void fft_stage(float2* s, int j, const float2* __restrict__ tw) {
+__device__ __forceinline__ void fft_stage(float2* s, int j, const float2* __restrict__ tw, bool active) {
     constexpr int T = N / 8;
     constexpr int NB = 8 / R;
     float2 x[8];
+    if (active) {
 #pragma unroll
-    for (int t = 0; t < NB; ++t) {
-        const int b = j + t * T;
+        for (int t = 0; t < NB; ++t) {
+            const int b = j + t * T;
 #pragma unroll
-        for (int k = 0; k < R; ++k) x[t * R + k] = s[pad_idx(b + k * (N / R))];
+            for (int k = 0; k < R; ++k) x[t * R + k] = s[pad_idx(b + k * (N / R))];
+        }
     }
     __syncthreads();
+    if (active) {
 #pragma unroll
-    for (int t = 0; t < NB; ++t) {
-        const int b = j + t * T;
-        const int p = b % NS;
-        if constexpr (NS > 1) {
+        for (int t = 0; t < NB; ++t) {
+            const int b = j + t * T;
+            const int p = b % NS;
+            if constexpr (NS > 1) {
 #pragma unroll
-            for (int k = 1; k < R; ++k) {
-                float2 w = __ldg(&tw[p * k * (kTwN / (NS * R))]);
-                if constexpr (DIR > 0) w.y = -w.y;
-                x[t * R + k] = c_mul(x[t * R + k], w);
+                for (int k = 1; k < R; ++k) {
+                    float2 w = __ldg(&tw[p * k * (kTwN / (NS * R))]);
+                    if constexpr (DIR > 0) w.y = -w.y;
+                    x[t * R + k] = c_mul(x[t * R + k], w);
+                }
             }
-        }
-        if constexpr (R == 8) dft8<DIR>(&x[t * R]);
-        else if constexpr (R == 4) dft4<DIR>(x[t * R], x[t * R + 1], x[t * R + 2], x[t * R + 3]);
-        else dft2<DIR>(x[t * R], x[t * R + 1]);
-        const int base = (b / NS) * NS * R + p;
+            if constexpr (R == 8) dft8<DIR>(&x[t * R]);
+            else if constexpr (R == 4) dft4<DIR>(x[t * R], x[t * R + 1], x[t * R + 2], x[t * R + 3]);
+            else dft2<DIR>(x[t * R], x[t * R + 1]);
+            const int base = (b / NS) * NS * R + p;
 #pragma unroll
-        for (int m = 0; m < R; ++m) s[pad_idx(base + m * NS)] = x[t * R + m];
+            for (int m = 0; m < R; ++m) s[pad_idx(base + m * NS)] = x[t * R + m];
+        }
     }
     __syncthreads();
 }
@@ -118,18 +126,18 @@ __device__ __forceinline__ void fft_stage(float2* s, int j, const float2* __rest
 // Full N-point transform of the padded shared-memory array s, worked by
 // thread j in [0, N/8) of the transform.  Input and output in natural order.
 template <int N, int DIR>
-__device__ __forceinline__ void fft_smem(float2* s, int j, const float2* __restrict__ tw) {
+__device__ __forceinline__ void fft_smem(float2* s, int j, const float2* __restrict__ tw, bool active = true) {
     static_assert(N >= 64 && N <= kTwN && (N & (N - 1)) == 0, "power-of-two size in [64, 4096]");
     constexpr int L2 = ilog2c(N);
     constexpr int n8 = L2 / 3;
     constexpr int rem = L2 % 3;
-    fft_stage<N, 8, 1, DIR>(s, j, tw);
-    fft_stage<N, 8, 8, DIR>(s, j, tw);
-    if constexpr (n8 >= 3) fft_stage<N, 8, 64, DIR>(s, j, tw);
-    if constexpr (n8 >= 4) fft_stage<N, 8, 512, DIR>(s, j, tw);
+    fft_stage<N, 8, 1, DIR>(s, j, tw, active);
+    fft_stage<N, 8, 8, DIR>(s, j, tw, active);
+    if constexpr (n8 >= 3) fft_stage<N, 8, 64, DIR>(s, j, tw, active);
+    if constexpr (n8 >= 4) fft_stage<N, 8, 512, DIR>(s, j, tw, active);
     constexpr int NSf = 1 << (3 * n8);
-    if constexpr (rem == 1) fft_stage<N, 2, NSf, DIR>(s, j, tw);
-    if constexpr (rem == 2) fft_stage<N, 4, NSf, DIR>(s, j, tw);
+    if constexpr (rem == 1) fft_stage<N, 2, NSf, DIR>(s, j, tw, active);
+    if constexpr (rem == 2) fft_stage<N, 4, NSf, DIR>(s, j, tw, active);
 }
 
 }  // namespace tdm

@@ -25,8 +25,8 @@ template <int H>
 int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
     using C = ExtractCfg<H>;
     const Params& p = c->p;
-    const size_t sm_rows = (size_t)C::PAIRS * padded_len(H) * sizeof(float2);
-    const size_t sm_cols = (size_t)C::COLS * padded_len(H) * sizeof(float2);
+    const size_t sm_rows = (size_t)C::PAIRS * tstride(H) * sizeof(float2);
+    const size_t sm_cols = (size_t)C::COLS * tstride(H) * sizeof(float2);
     if (allow_smem(k_extract_rows<H>, sm_rows) != cudaSuccess) return TDM_ECUDA;
     if (allow_smem(k_extract_cols<H>, sm_cols) != cudaSuccess) return TDM_ECUDA;
     const size_t bytes_per = (size_t)H * H * (bits == 16 ? 2 : 1);

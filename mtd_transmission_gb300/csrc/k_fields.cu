@@ -100,7 +100,7 @@ k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspe
         const float mod = sqrtf(s0.y * s0.y + s0.x * s0.x);
         nrm = make_float2(s0.x / mod, -s0.y / mod);
     }
-    float2* s = sm + tr * padded_len(F);
+    float2* s = sm + tr * tstride(F);
     const float2* src = spectra + ((size_t)a * F + ((r + p.y) & (F - 1))) * F;
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
@@ -127,16 +127,19 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
     constexpr int B = C::B;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    constexpr int NT = B * C::T;
     const int a = blockIdx.y, x0 = blockIdx.x * B;
-    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
-        const int t = i % B, r = i / B;
-        sm[t * padded_len(F) + pad_idx(r)] = I1[((size_t)a * F + r) * F + x0 + t];
+#pragma unroll
+    for (int r0 = 0; r0 < B * F / NT; ++r0) {
+        const int i = threadIdx.x + r0 * NT, t = i % B, r = i / B;
+        sm[t * tstride(F) + pad_idx(r)] = I1[((size_t)a * F + r) * F + x0 + t];
     }
     __syncthreads();
-    fft_smem<F, +1>(sm + tr * padded_len(F), j, tw);
-    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
-        const int t = i % B, y = i / B;
-        const float2 u = sm[t * padded_len(F) + pad_idx(y)];
+    fft_smem<F, +1>(sm + tr * tstride(F), j, tw);
+#pragma unroll
+    for (int r0 = 0; r0 < B * F / NT; ++r0) {
+        const int i = threadIdx.x + r0 * NT, t = i % B, y = i / B;
+        const float2 u = sm[t * tstride(F) + pad_idx(y)];
         const int yo = (y + F / 2) & (F - 1), xo = (x0 + t + F / 2) & (F - 1);
         const size_t o = ((size_t)a * F + yo) * F + xo;
         if (mode) {
@@ -155,107 +158,140 @@ struct VolkovCfg {
     static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;  // rows/columns per CTA
 };
 
-// Pass 1: rows of the mirror.  gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi.
+// Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
+// row, and the spectral x derivative of a mirror row is odd about the row's
+// centre (its Nyquist bin is zero), so only image rows y are transformed and
+// only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi is kept:
+// gx[Y][X] = sign(X) gxh[m(Y)][m(X)].  Per pair of image rows: the Z row of
+// each, and both phase rows packed into one complex row (their derivatives
+// are real).
 template <int L>
-__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
-k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, float* __restrict__ gx) {
-    using C = VolkovCfg<L>;
-    constexpr int F = L / 2;
+struct V1Cfg {
+    static constexpr int T = L / 8;
+    static constexpr int P = (384 / (3 * T)) >= 1 ? 384 / (3 * T) : 1;  // row pairs per CTA
+};
+
+template <int L>
+__global__ void __launch_bounds__(3 * V1Cfg<L>::P * (L / 8))
+k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, float* __restrict__ gxh) {
+    using C = V1Cfg<L>;
+    constexpr int F = L / 2, T = C::T;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    const int a = blockIdx.y, Y = blockIdx.x * C::B + tr;
-    float2* sz = sm + tr * padded_len(L);
-    float2* sp = sm + (C::B + tr) * padded_len(L);
-    const float* ph = phase + ((size_t)a * F + mirror(Y, F)) * F;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    const int pair = tr / 3, kind = tr % 3;  // kind 0: Z of row a, 1: Z of row b, 2: phases packed
+    const int a = blockIdx.y;
+    const int ya = blockIdx.x * 2 * C::P + 2 * pair, yb = ya + 1;
+    float2* s = sm + tr * tstride(L);
+    const float* pa = phase + ((size_t)a * F + ya) * F;
+    const float* pb = phase + ((size_t)a * F + yb) * F;
     float v[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
-        const int X = j + t * C::T;
-        v[t] = ph[mirror(X, F)];
-        float sn, cs;
-        sincosf(v[t], &sn, &cs);
-        sz[pad_idx(X)] = make_float2(cs, sn);
-        sp[pad_idx(X)] = make_float2(v[t], 0.0f);
+        const int X = j + t * T, mx = mirror(X, F);
+        const float fa = pa[mx], fb = pb[mx];
+        if (kind == 2) {
+            s[pad_idx(X)] = make_float2(fa, fb);
+        } else {
+            v[t] = kind == 0 ? fa : fb;
+            float sn, cs;
+            sincosf(v[t], &sn, &cs);
+            s[pad_idx(X)] = make_float2(cs, sn);
+        }
     }
     __syncthreads();
-    fft_smem<L, -1>(sz, j, tw);
-    fft_smem<L, -1>(sp, j, tw);
+    fft_smem<L, -1>(s, j, tw);
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
-        const int k = j + t * C::T;
+        const int k = j + t * T;
         const float c = kTwoPi * kappa(k, L) / (float)L;
-        const float2 z = sz[pad_idx(k)], q = sp[pad_idx(k)];
-        sz[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
-        sp[pad_idx(k)] = make_float2(-c * q.y, c * q.x);
+        const float2 z = s[pad_idx(k)];
+        s[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
     }
     __syncthreads();
-    fft_smem<L, +1>(sz, j, tw);
-    fft_smem<L, +1>(sp, j, tw);
+    fft_smem<L, +1>(s, j, tw);
+    if (kind < 2) {
+        const float2* sp = sm + (3 * pair + 2) * tstride(L);
+        float* out = gxh + ((size_t)a * F + (kind == 0 ? ya : yb)) * F;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int X = j + t * C::T;
-        float sn, cs;
-        sincosf(v[t], &sn, &cs);
-        const float2 g = sz[pad_idx(X)];
-        const float ax = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);  // Re(-i g / Z)
-        gx[((size_t)a * L + Y) * L + X] = (ax - sp[pad_idx(X)].x) * kInvTwoPi;
+        for (int t = 4; t < 8; ++t) {  // X = j + t T >= F
+            const int X = j + t * T;
+            float sn, cs;
+            sincosf(v[t], &sn, &cs);
+            const float2 g = s[pad_idx(X)];
+            const float ax = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);  // Re(-i g / Z)
+            const float2 q = sp[pad_idx(X)];
+            out[X - F] = (ax - (kind == 0 ? q.x : q.y)) * kInvTwoPi;
+        }
     }
 }
 
-// Pass 2: columns of the mirror: gy like gx, then Q = gx + i gy, FFT along y.
+// Pass 2: columns X = F + x of the mirror (columns X and L-1-X are the same
+// image column): gy like gx, then Q = gx + i gy and its FFT along y.  The
+// columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
+// pass 3.
 template <int L>
-__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
-k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gx, const float2* __restrict__ tw,
+struct V2Cfg {
+    static constexpr int T = L / 8;
+    static constexpr int P = (768 / (3 * T)) >= 1 ? 768 / (3 * T) : 1;  // column pairs per CTA
+};
+
+template <int L>
+__global__ void __launch_bounds__(3 * V2Cfg<L>::P * (L / 8))
+k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, const float2* __restrict__ tw,
               float2* __restrict__ qc) {
-    using C = VolkovCfg<L>;
-    constexpr int F = L / 2, B = C::B;
+    using C = V2Cfg<L>;
+    constexpr int F = L / 2, T = C::T, P = C::P, NC = 2 * P, NT = 3 * P * T, LS = L + 1;
     extern __shared__ float2 sm[];
-    float* sph = reinterpret_cast<float*>(sm + 2 * B * padded_len(L));  // B x L phase
-    float* sgx = sph + B * L;                                           // B x L gx
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    const int a = blockIdx.y, X0 = blockIdx.x * B;
-    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
-        const int t = i % B, Y = i / B;
-        const float v = phase[((size_t)a * F + mirror(Y, F)) * F + mirror(X0 + t, F)];
+    float* sph = reinterpret_cast<float*>(sm + 3 * P * tstride(L));  // NC x LS phase along the mirror column
+    float* sgx = sph + NC * LS;                                      // NC x LS gx along the mirror column
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    const int pair = tr / 3, kind = tr % 3;
+    const int a = blockIdx.y, x0 = blockIdx.x * NC;
+#pragma unroll 6
+    for (int i = threadIdx.x; i < NC * L; i += NT) {
+        const int c = i % NC, Y = i / NC;
+        const size_t src = ((size_t)a * F + mirror(Y, F)) * F + x0 + c;
+        const float v = phase[src];
+        sph[c * LS + Y] = v;
+        sgx[c * LS + Y] = gxh[src];
         float sn, cs;
         sincosf(v, &sn, &cs);
-        sm[t * padded_len(L) + pad_idx(Y)] = make_float2(cs, sn);
-        sm[(B + t) * padded_len(L) + pad_idx(Y)] = make_float2(v, 0.0f);
-        sph[t * L + Y] = v;
-        sgx[t * L + Y] = gx[((size_t)a * L + Y) * L + X0 + t];
+        const int pp = c >> 1, ab = c & 1;
+        sm[(3 * pp + ab) * tstride(L) + pad_idx(Y)] = make_float2(cs, sn);
+        reinterpret_cast<float*>(&sm[(3 * pp + 2) * tstride(L) + pad_idx(Y)])[ab] = v;
     }
     __syncthreads();
-    float2* sz = sm + tr * padded_len(L);
-    float2* sp = sm + (B + tr) * padded_len(L);
-    fft_smem<L, -1>(sz, j, tw);
-    fft_smem<L, -1>(sp, j, tw);
+    float2* s = sm + tr * tstride(L);
+    fft_smem<L, -1>(s, j, tw);
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
-        const int k = j + t * C::T;
+        const int k = j + t * T;
         const float c = kTwoPi * kappa(k, L) / (float)L;
-        const float2 z = sz[pad_idx(k)], q = sp[pad_idx(k)];
-        sz[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
-        sp[pad_idx(k)] = make_float2(-c * q.y, c * q.x);
+        const float2 z = s[pad_idx(k)];
+        s[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
     }
     __syncthreads();
-    fft_smem<L, +1>(sz, j, tw);
-    fft_smem<L, +1>(sp, j, tw);
+    fft_smem<L, +1>(s, j, tw);
+    if (kind < 2) {
+        const int c = 2 * pair + kind;
+        const float2* sp = sm + (3 * pair + 2) * tstride(L);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int Y = j + t * C::T;
-        const float v = sph[tr * L + Y];
-        float sn, cs;
-        sincosf(v, &sn, &cs);
-        const float2 g = sz[pad_idx(Y)];
-        const float ay = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);
-        const float gy = (ay - sp[pad_idx(Y)].x) * kInvTwoPi;
-        sz[pad_idx(Y)] = make_float2(sgx[tr * L + Y], gy);
+        for (int t = 0; t < 8; ++t) {
+            const int Y = j + t * T;
+            float sn, cs;
+            sincosf(sph[c * LS + Y], &sn, &cs);
+            const float2 g = s[pad_idx(Y)];
+            const float ay = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);
+            const float2 q = sp[pad_idx(Y)];
+            s[pad_idx(Y)] = make_float2(sgx[c * LS + Y], (ay - (kind == 0 ? q.x : q.y)) * kInvTwoPi);
+        }
     }
     __syncthreads();
-    fft_smem<L, -1>(sz, j, tw);
-    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
-        const int t = i % B, Y = i / B;
-        qc[((size_t)a * L + Y) * L + X0 + t] = sm[t * padded_len(L) + pad_idx(Y)];
+    fft_smem<L, -1>(s, j, tw, kind < 2);
+#pragma unroll 6
+    for (int i = threadIdx.x; i < NC * L; i += NT) {
+        const int c = i % NC, ky = i / NC;
+        qc[((size_t)a * L + ky) * F + x0 + c] = sm[(3 * (c >> 1) + (c & 1)) * tstride(L) + pad_idx(ky)];
     }
 }
 
@@ -279,12 +315,19 @@ k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw
         r = which ? L - q : q;
         ptr = tr ^ 1;
     }
-    float2* s = sm + tr * padded_len(L);
-    const float2* sp = sm + ptr * padded_len(L);
+    float2* s = sm + tr * tstride(L);
+    const float2* sp = sm + ptr * tstride(L);
+    // Qc holds columns X >= F; Qc[ky][X] = -conj(Qc[-ky][L-1-X]) for X < F
+    const int rp = (L - r) & (L - 1);
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
         const int X = j + t * C::T;
-        s[pad_idx(X)] = qc[((size_t)a * L + r) * L + X];
+        if (X >= F) {
+            s[pad_idx(X)] = qc[((size_t)a * L + r) * F + (X - F)];
+        } else {
+            const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
+            s[pad_idx(X)] = make_float2(-u.x, u.y);
+        }
     }
     __syncthreads();
     fft_smem<L, -1>(s, j, tw);
@@ -324,40 +367,44 @@ k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ pha
     constexpr int F = L / 2, B = C::B;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    constexpr int NT = B * C::T;
     const int a = blockIdx.y, c0 = blockIdx.x * B;
-    for (int i = threadIdx.x; i < B * L; i += blockDim.x) {
-        const int t = i % B, ky = i / B;
-        sm[t * padded_len(L) + pad_idx(ky)] = tq[((size_t)a * L + ky) * F + c0 + t];
+#pragma unroll
+    for (int r = 0; r < B * L / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
+        sm[t * tstride(L) + pad_idx(ky)] = tq[((size_t)a * L + ky) * F + c0 + t];
     }
     __syncthreads();
-    fft_smem<L, +1>(sm + tr * padded_len(L), j, tw);
-    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
-        const int t = i % B, y = i / B;
+    fft_smem<L, +1>(sm + tr * tstride(L), j, tw);
+#pragma unroll
+    for (int r = 0; r < B * F / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, y = i / B;
         const size_t o = ((size_t)a * F + y) * F + c0 + t;
-        unwrapped[o] = phase[o] + kTwoPi * sm[t * padded_len(L) + pad_idx(F + y)].x;
+        unwrapped[o] = phase[o] + kTwoPi * sm[t * tstride(L) + pad_idx(F + y)].x;
     }
 }
 
 // ---------------------------------------------------------------- aberration fit
-// beta[a][img][:] = Rinv * (Q^T b): monomial coefficients (scaled coordinates)
-// of the least-squares fit of image img (0: unwrapped phase, 1: amplitude).
-__global__ void __launch_bounds__(256) k_aber_fit(const float* __restrict__ unwrapped, const float* __restrict__ amp,
-                                                  const int* __restrict__ samp_idx, const float* __restrict__ samp_q,
-                                                  int nsamp, const double* __restrict__ rinv, int F,
-                                                  double* __restrict__ beta) {
-    const int a = blockIdx.x, im = blockIdx.y;
+// Partial sums c_k = sum_s q_k(s) b(s) of the least-squares projection of
+// image img (0: unwrapped phase, 1: amplitude) over slice blockIdx.z of the
+// background samples, in FP64.
+__global__ void __launch_bounds__(256) k_aber_partial(const float* __restrict__ unwrapped, const float* __restrict__ amp,
+                                                      const int* __restrict__ samp_idx, const float* __restrict__ samp_q,
+                                                      int nsamp, int F, double* __restrict__ part) {
+    const int a = blockIdx.x, im = blockIdx.y, sl = blockIdx.z;
     const float* img = (im == 0 ? unwrapped : amp) + (size_t)a * F * F;
+    const int per = (nsamp + kFitSlices - 1) / kFitSlices;
+    const int s0 = sl * per, s1 = min(nsamp, s0 + per);
     double acc[kNC];
 #pragma unroll
     for (int k = 0; k < kNC; ++k) acc[k] = 0.0;
-    for (int s = threadIdx.x; s < nsamp; s += blockDim.x) {
+    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         const double v = (double)img[samp_idx[s]];
         const float* q = samp_q + (size_t)s * kNC;
 #pragma unroll
         for (int k = 0; k < kNC; ++k) acc[k] = fma((double)q[k], v, acc[k]);
     }
     __shared__ double red[8][kNC];
-    __shared__ double cf[kNC];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < kNC; ++k) {
@@ -370,14 +417,30 @@ __global__ void __launch_bounds__(256) k_aber_fit(const float* __restrict__ unwr
     if (threadIdx.x < kNC) {
         double x = 0.0;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) x += red[i][threadIdx.x];
-        cf[threadIdx.x] = x;
+        part[(((size_t)a * 2 + im) * kFitSlices + sl) * kNC + threadIdx.x] = x;
+    }
+}
+
+// beta[a][img][:] = Rinv * c: monomial coefficients (scaled coordinates) of
+// the fit, summing the slices in a fixed order.
+__global__ void k_aber_reduce(const double* __restrict__ part, const double* __restrict__ rinv,
+                              double* __restrict__ beta) {
+    const int a = blockIdx.x;
+    __shared__ double cf[2][kNC];
+    const int t = threadIdx.x;
+    if (t < 2 * kNC) {
+        const int im = t / kNC, k = t % kNC;
+        double x = 0.0;
+        for (int sl = 0; sl < kFitSlices; ++sl) x += part[(((size_t)a * 2 + im) * kFitSlices + sl) * kNC + k];
+        cf[im][k] = x;
     }
     __syncthreads();
-    if (threadIdx.x < kNC) {
+    if (t < 2 * kNC) {
+        const int im = t / kNC, k = t % kNC;
         double x = 0.0;
 #pragma unroll
-        for (int i = 0; i < kNC; ++i) x = fma(rinv[threadIdx.x * kNC + i], cf[i], x);
-        beta[((size_t)a * 2 + im) * kNC + threadIdx.x] = x;
+        for (int i = 0; i < kNC; ++i) x = fma(rinv[k * kNC + i], cf[im][i], x);
+        beta[((size_t)a * 2 + im) * kNC + k] = x;
     }
 }
 
@@ -429,21 +492,23 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
-    const size_t sm_field = (size_t)FC::B * padded_len(F) * sizeof(float2);
-    const size_t sm_vrows = (size_t)2 * VC::B * padded_len(L) * sizeof(float2);
-    const size_t sm_vcols = sm_vrows + (size_t)2 * VC::B * L * sizeof(float);
-    const size_t sm_vir = (size_t)VC::B * padded_len(L) * sizeof(float2);
+    const size_t sm_field = (size_t)FC::B * tstride(F) * sizeof(float2);
+    using V1 = V1Cfg<L>;
+    using V2 = V2Cfg<L>;
+    const size_t sm_vrows = (size_t)3 * V1::P * tstride(L) * sizeof(float2);
+    const size_t sm_vcols = (size_t)3 * V2::P * tstride(L) * sizeof(float2) + (size_t)2 * 2 * V2::P * (L + 1) * sizeof(float);
+    const size_t sm_vir = (size_t)VC::B * tstride(L) * sizeof(float2);
     if (allow_smem(k_field_rows<F>, sm_field) || allow_smem(k_field_cols<F>, sm_field) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
         allow_smem(k_volkov_integ_rows<L>, sm_vir) || allow_smem(k_volkov_integ_cols<L>, sm_vir))
         return TDM_ECUDA;
+    {
+        Launch l(c, K_ARGMAX);
+        k_argmax<<<n, 1024, 0, c->stream>>>(b.spectra + (size_t)a0 * FF, F, b.posspec + a0, b.specval + a0);
+    }
     for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
         const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
         const float2* spec = b.spectra + (size_t)g0 * FF;
-        {
-            Launch l(c, K_ARGMAX);
-            k_argmax<<<m, 1024, 0, c->stream>>>(spec, F, b.posspec + g0, b.specval + g0);
-        }
         {
             Launch l(c, K_FIELD_ROWS);
             k_field_rows<F><<<dim3(F / FC::B, m), FC::B * FC::T, sm_field, c->stream>>>(
@@ -459,12 +524,13 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                k_volkov_rows<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vrows, c->stream>>>(b.phase, b.tw, b.gx);
+                k_volkov_rows<L><<<dim3(F / (2 * V1::P), m), 3 * V1::P * V1::T, sm_vrows, c->stream>>>(b.phase, b.tw,
+                                                                                                     b.gx);
             }
             {
                 Launch l(c, K_VOLKOV_COLS);
-                k_volkov_cols<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vcols, c->stream>>>(b.phase, b.gx, b.tw,
-                                                                                             b.qc);
+                k_volkov_cols<L><<<dim3(F / (2 * V2::P), m), 3 * V2::P * V2::T, sm_vcols, c->stream>>>(b.phase, b.gx,
+                                                                                                     b.tw, b.qc);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_ROWS);
@@ -479,8 +545,12 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         }
         {
             Launch l(c, K_ABER_FIT);
-            k_aber_fit<<<dim3(m, 2), 256, 0, c->stream>>>(unw, b.amp, b.samp_idx, b.samp_q, c->nsamp, b.rinv, F,
-                                                          b.beta);
+            k_aber_partial<<<dim3(m, 2, kFitSlices), 256, 0, c->stream>>>(unw, b.amp, b.samp_idx, b.samp_q, c->nsamp,
+                                                                          F, b.fit_part);
+        }
+        {
+            Launch l(c, K_ABER_REDUCE);
+            k_aber_reduce<<<m, 32, 0, c->stream>>>(b.fit_part, b.rinv, b.beta);
         }
         {
             Launch l(c, K_FORM);

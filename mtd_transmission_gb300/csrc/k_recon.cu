@@ -6,7 +6,7 @@
 //     (-1)^(kx+ky) dx^2 FFT2(field * tukey)[k],
 // so the per-field kernels work on natural FFT bins and store, per bin, the
 // cap contribution -2i k0 sdz value (cteUb2Pot*cteNorm*sdz, fonctions.cpp:902,927)
-// and its volume plane z (-1 outside the NA disc).
+// and its volume plane z (-1 outside the NA disc), packed as one 16-byte record.
 //
 // Mapping (retroPropag_Born, src/fonctions.cpp:875-935) as a gather: voxel
 // column (X, Y) reads bin kx = (X - D/2) mod F for every angle whose cap window
@@ -54,7 +54,7 @@ k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, con
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
     const int a = blockIdx.y, y = blockIdx.x * C::B + tr;
-    float2* s = sm + tr * padded_len(F);
+    float2* s = sm + tr * tstride(F);
     const float wy = tuk[y];
     const float2* src = fields + ((size_t)a * F + y) * F;
 #pragma unroll
@@ -75,28 +75,31 @@ template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::B * (F / 8))
 k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ fzm0,
            const double* __restrict__ s_tab, const float* __restrict__ s_tabf, Params p,
-           const float2* __restrict__ tw, float2* __restrict__ rec_val, int16_t* __restrict__ rec_z,
-           int* __restrict__ err) {
+           const float2* __restrict__ tw, float4* __restrict__ rec, int* __restrict__ err) {
     using C = CapCfg<F>;
     constexpr int B = C::B;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    constexpr int NT = B * C::T;
     const int a = blockIdx.y, kx0 = blockIdx.x * B;
-    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
-        const int t = i % B, ky = i / B;
-        sm[t * padded_len(F) + pad_idx(ky)] = r1[((size_t)a * F + ky) * F + kx0 + t];
+#pragma unroll
+    for (int r = 0; r < B * F / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
+        sm[t * tstride(F) + pad_idx(ky)] = r1[((size_t)a * F + ky) * F + kx0 + t];
     }
     __syncthreads();
-    fft_smem<F, -1>(sm + tr * padded_len(F), j, tw);
+    fft_smem<F, -1>(sm + tr * tstride(F), j, tw);
     const int2 ps = posspec[a];
     const double fz = fzm0[a];
     const float fzf = (float)fz;
     const int N = p.N;
-    for (int i = threadIdx.x; i < B * F; i += blockDim.x) {
-        const int t = i % B, ky = i / B, kx = kx0 + t;
+#pragma unroll 2
+    for (int r = 0; r < B * F / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, ky = i / B, kx = kx0 + t;
         const size_t o = ((size_t)a * F + ky) * F + kx;
         const int fdx = ((kx + ps.x) & (F - 1)) - N, fdy = ((ky + ps.y) & (F - 1)) - N;
         int z = -1;
+        float2 val = make_float2(0.f, 0.f);
         if (fz >= 0.0 && fdx * fdx + fdy * fdy < p.disc_thr) {
             const int ti = (fdy + N) * F + fdx + N;
             const float sf = s_tabf[ti];
@@ -110,98 +113,98 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
                 atomicOr(err, 1);
                 z = -1;
             } else {
-                float2 v = sm[t * padded_len(F) + pad_idx(ky)];
+                float2 v = sm[t * tstride(F) + pad_idx(ky)];
                 const float sg = ((kx + ky) & 1) ? -p.dx2 : p.dx2;
                 const float Bc = p.cap_scale * (sf * (float)p.inv_rayon) * sg;  // (k0/pi)(-2pi) sdz dx^2 (+-1)
-                rec_val[o] = make_float2(-Bc * v.y, Bc * v.x);
+                val = make_float2(-Bc * v.y, Bc * v.x);
             }
         }
-        rec_z[o] = (int16_t)z;
+        rec[o] = make_float4(val.x, val.y, __int_as_float(z), 0.f);
     }
 }
 
-// ---------------------------------------------------------------- gather + z inverse FFT
-constexpr int kGX = 16, kGY = 8, kGC = kGX * kGY;  // columns per CTA
+// ---------------------------------------------------------------- cap accumulation
+// One warp per voxel column (X, Y); the lanes take 32 consecutive angles at a
+// time.  An angle hits a column at most once, at one plane; lanes whose hits
+// share a plane are grouped and the group's lowest lane adds the members'
+// contributions in ascending angle order to the column's FP64 accumulator in
+// shared memory.  The sums are therefore deterministic, and hit counts exact.
+constexpr int kGW = 8;  // warps per CTA; a CTA covers 32 consecutive x at one y
 
 template <int D>
-__global__ void __launch_bounds__(kGC)
-k_gather(const float2* __restrict__ rec_val, const int16_t* __restrict__ rec_z, const int2* __restrict__ posspec,
-         int M, Params p, double2* __restrict__ acc_all, const float2* __restrict__ tw, float2* __restrict__ vol,
-         uint8_t* __restrict__ otf, uint32_t* __restrict__ cnt_out) {
-    constexpr int T = D / 8, G = kGC / T;
+__global__ void __launch_bounds__(kGW * 32)
+k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, int M, Params p,
+             float2* __restrict__ vol, uint32_t* __restrict__ cnt_out) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    float2* fbuf = reinterpret_cast<float2*>(smraw);                       // G x padded(D)
-    int2* sp = reinterpret_cast<int2*>(fbuf + G * padded_len(D));          // M
-    uint16_t* cnt = reinterpret_cast<uint16_t*>(sp + M);                   // band x kGC
-    const int tid = threadIdx.x, tx = tid % kGX, ty = tid / kGX;
-    const int X0 = blockIdx.x * kGX, Y0 = blockIdx.y * kGY;
-    const int X = X0 + tx, Y = Y0 + ty;
-    const int F = p.F, band = p.band, zmin = p.zmin;
-    double2* acc = acc_all + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * band * kGC;
-    for (int i = tid; i < M; i += kGC) sp[i] = posspec[i];
-    for (int zb = 0; zb < band; ++zb) {
-        acc[zb * kGC + tid] = make_double2(0.0, 0.0);
-        cnt[zb * kGC + tid] = 0;
-    }
+    const int band = p.band;
+    double2* acc_all = reinterpret_cast<double2*>(smraw);                // kGW x band
+    float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);   // kGW x 32
+    uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32); // kGW x band
+    int2* sp = reinterpret_cast<int2*>(cnt_all + ((kGW * band + 3) & ~3));  // M
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double2* acc = acc_all + w * band;
+    uint16_t* cnt = cnt_all + w * band;
+    float2* stg = stg_all + w * 32;
+    for (int i = threadIdx.x; i < M; i += kGW * 32) sp[i] = posspec[i];
     __syncthreads();
-    const int h = D / 2;
-    const int kx = (X - h) & (F - 1), ky = (Y - h) & (F - 1);
-    const size_t koff = (size_t)ky * F + kx;
-    const int bx = X - h, by = Y - h;  // fd + N = X - D/2 + posSpec
+    const int F = p.F, h = D / 2, zmin = p.zmin;
     const size_t FF = (size_t)F * F;
-    for (int a = 0; a < M; ++a) {
-        const int2 q = sp[a];
-        const int ux = bx + q.x, uy = by + q.y;  // fd + N
-        if ((unsigned)ux < (unsigned)F && (unsigned)uy < (unsigned)F) {
-            const size_t idx = (size_t)a * FF + koff;
-            const int z = rec_z[idx];
-            if (z >= 0) {
-                const float2 v = rec_val[idx];
-                const int e = (z - zmin) * kGC + tid;
+    const int Y = blockIdx.y;
+    const int by = Y - h;
+    for (int cx = 0; cx < 32; cx += kGW) {
+        const int X = blockIdx.x * 32 + cx + w;
+        const int bx = X - h;  // fd + N = X - D/2 + posSpec
+        const size_t koff = (size_t)(by & (F - 1)) * F + (bx & (F - 1));
+        for (int e = lane; e < band; e += 32) {
+            acc[e] = make_double2(0.0, 0.0);
+            cnt[e] = 0;
+        }
+        __syncwarp();
+        for (int a0 = 0; a0 < M; a0 += 32) {
+            const int a = a0 + lane;
+            int e = -1;
+            float2 v = make_float2(0.f, 0.f);
+            if (a < M) {
+                const int2 q = sp[a];
+                if ((unsigned)(bx + q.x) < (unsigned)F && (unsigned)(by + q.y) < (unsigned)F) {
+                    const float4 r = __ldg(&rec[(size_t)a * FF + koff]);
+                    const int z = __float_as_int(r.z);
+                    if (z >= 0) {
+                        e = z - zmin;
+                        v = make_float2(r.x, r.y);
+                    }
+                }
+            }
+            const unsigned grp = __match_any_sync(0xffffffffu, e >= 0 ? e : -1 - lane);
+            stg[lane] = v;
+            __syncwarp();
+            if (e >= 0 && (grp & ((1u << lane) - 1)) == 0) {  // lowest lane of its plane group
+                double sx = 0.0, sy = 0.0;
+                for (unsigned g = grp; g; g &= g - 1) {
+                    const float2 u = stg[__ffs(g) - 1];
+                    sx += (double)u.x;
+                    sy += (double)u.y;
+                }
                 double2 t = acc[e];
-                t.x += (double)v.x;
-                t.y += (double)v.y;
+                t.x += sx;
+                t.y += sy;
                 acc[e] = t;
-                cnt[e] += 1;
+                cnt[e] += (uint16_t)__popc(grp);
             }
+            __syncwarp();
         }
-    }
-    __syncthreads();
-    // OTF mask (Re != 0 after normalisation, main.cpp:262-267) and hit counts
-    if (otf || cnt_out) {
-        for (int Z = 0; Z < D; ++Z) {
-            const int zb = Z - zmin;
-            const bool in = zb >= 0 && zb < band;
-            const size_t o = ((size_t)Z * D + Y) * D + X;
-            if (otf) otf[o] = (in && acc[zb * kGC + tid].x != 0.0) ? 1 : 0;
-            if (cnt_out) cnt_out[o] = in ? cnt[zb * kGC + tid] : 0u;
+        // normalise (main.cpp:243-249); (-1)^(X+Y+Z) stands for the first fftshift3D
+        float2* col = vol + ((size_t)Y * D + X) * D + zmin;
+        for (int e = lane; e < band; e += 32) {
+            const double2 t = acc[e];
+            const unsigned n = cnt[e];
+            const float dn = n ? (float)n : 1.0f;
+            float2 val = make_float2((float)t.x / dn, (float)t.y / dn);
+            if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
+            col[e] = val;
+            if (cnt_out) cnt_out[((size_t)(zmin + e) * D + Y) * D + X] = n;
         }
-    }
-    // normalise, modulate, inverse FFT along z, G columns at a time
-    const int tr = tid / T, j = tid % T;
-    for (int c0 = 0; c0 < kGC; c0 += G) {
-        for (int i = tid; i < G * D; i += kGC) {
-            const int g = i % G, Z = i / G, col = c0 + g;
-            const int Xc = X0 + col % kGX, Yc = Y0 + col / kGX;
-            float2 v = make_float2(0.0f, 0.0f);
-            const int zb = Z - zmin;
-            if (zb >= 0 && zb < band) {
-                const double2 t = acc[zb * kGC + col];
-                const unsigned n = cnt[zb * kGC + col];
-                const double dn = n ? (double)n : 1.0;
-                v = make_float2((float)(t.x / dn), (float)(t.y / dn));
-                if ((Xc + Yc + Z) & 1) v = make_float2(-v.x, -v.y);
-            }
-            fbuf[g * padded_len(D) + pad_idx(Z)] = v;
-        }
-        __syncthreads();
-        fft_smem<D, +1>(fbuf + tr * padded_len(D), j, tw);
-        for (int i = tid; i < G * D; i += kGC) {
-            const int g = i / D, Z = i % D, col = c0 + g;
-            const int Xc = X0 + col % kGX, Yc = Y0 + col / kGX;
-            vol[((size_t)Yc * D + Xc) * D + Z] = fbuf[g * padded_len(D) + pad_idx(Z)];
-        }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -211,24 +214,63 @@ struct PassCfg {
     static constexpr int B = (1024 / T) < 16 ? (1024 / T) : 16;
 };
 
+// inverse FFT along z (contiguous) for B consecutive columns of the [y][x][z]
+// volume; planes outside the cap band are zero and are not read.
+// The OTF mask (Re != 0 after normalisation, main.cpp:262-267) is written
+// here, from the spectrum values this pass reads: B consecutive columns are B
+// consecutive x at one y.
+template <int D>
+__global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
+k_zpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int band, uint8_t* __restrict__ otf) {
+    using C = PassCfg<D>;
+    constexpr int B = C::B, NT = B * C::T;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const size_t c0 = (size_t)blockIdx.x * B;
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i / D, Z = i % D;
+        float2 v = make_float2(0.f, 0.f);
+        if (Z >= zmin && Z < zmin + band) v = vol[(c0 + t) * D + Z];
+        sm[t * tstride(D) + pad_idx(Z)] = v;
+    }
+    __syncthreads();
+    if (otf) {  // reads only; the first FFT stage writes after its own barrier
+#pragma unroll
+        for (int r = 0; r < B * D / NT; ++r) {
+            const int i = threadIdx.x + r * NT, t = i % B, Z = i / B;
+            const size_t c = c0 + t;  // y * D + x
+            otf[(size_t)Z * D * D + c] = sm[t * tstride(D) + pad_idx(Z)].x != 0.0f ? 1 : 0;
+        }
+    }
+    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i / D, Z = i % D;
+        vol[(c0 + t) * D + Z] = sm[t * tstride(D) + pad_idx(Z)];
+    }
+}
+
 // inverse FFT along y, in place, for B consecutive z at fixed x
 template <int D>
 __global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
 k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
     using C = PassCfg<D>;
-    constexpr int B = C::B;
+    constexpr int B = C::B, NT = B * C::T;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
     const int z0 = blockIdx.x * B, X = blockIdx.y;
-    for (int i = threadIdx.x; i < B * D; i += blockDim.x) {
-        const int t = i % B, Y = i / B;
-        sm[t * padded_len(D) + pad_idx(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, Y = i / B;
+        sm[t * tstride(D) + pad_idx(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
     }
     __syncthreads();
-    fft_smem<D, +1>(sm + tr * padded_len(D), j, tw);
-    for (int i = threadIdx.x; i < B * D; i += blockDim.x) {
-        const int t = i % B, Y = i / B;
-        vol[((size_t)Y * D + X) * D + z0 + t] = sm[t * padded_len(D) + pad_idx(Y)];
+    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, Y = i / B;
+        vol[((size_t)Y * D + X) * D + z0 + t] = sm[t * tstride(D) + pad_idx(Y)];
     }
 }
 
@@ -239,24 +281,26 @@ __global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
 k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float scale, float* __restrict__ re,
         float* __restrict__ im) {
     using C = PassCfg<D>;
-    constexpr int B = C::B;
+    constexpr int B = C::B, NT = B * C::T;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
     const int z0 = blockIdx.x * B, Y = blockIdx.y;
-    for (int i = threadIdx.x; i < B * D; i += blockDim.x) {
-        const int t = i % B, X = i / B;
-        sm[t * padded_len(D) + pad_idx(X)] = vol[((size_t)Y * D + X) * D + z0 + t];
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, X = i / B;
+        sm[t * tstride(D) + pad_idx(X)] = vol[((size_t)Y * D + X) * D + z0 + t];
     }
     __syncthreads();
-    fft_smem<D, +1>(sm + tr * padded_len(D), j, tw);
+    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
     const int par = (3 * (D / 2)) & 1;
-    for (int i = threadIdx.x; i < B * D; i += blockDim.x) {
-        const int t = i / D, X = i % D, Z = z0 + t;
-        const float2 v = sm[t * padded_len(D) + pad_idx(X)];
-        const float s = ((X + Y + Z + par) & 1) ? -scale : scale;
+#pragma unroll
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i / D, X = i % D, Z = z0 + t;
+        const float2 v = sm[t * tstride(D) + pad_idx(X)];
+        const float sg = ((X + Y + Z + par) & 1) ? -scale : scale;
         const size_t o = ((size_t)Z * D + Y) * D + X;
-        if (re) re[o] = v.x * s;
-        if (im) im[o] = v.y * s;
+        if (re) re[o] = v.x * sg;
+        if (im) im[o] = v.y * sg;
     }
 }
 
@@ -264,7 +308,7 @@ template <int F>
 int cap_impl(tdm_ctx* c, int n) {
     using C = CapCfg<F>;
     Buffers& b = c->b;
-    const size_t sm = (size_t)C::B * padded_len(F) * sizeof(float2);
+    const size_t sm = (size_t)C::B * tstride(F) * sizeof(float2);
     if (allow_smem(k_cap_rows<F>, sm) || allow_smem(k_cap_cols<F>, sm)) return TDM_ECUDA;
     {
         Launch l(c, K_FZM0);
@@ -280,8 +324,7 @@ int cap_impl(tdm_ctx* c, int n) {
         {
             Launch l(c, K_CAP_COLS);
             k_cap_cols<F><<<dim3(F / C::B, m), C::B * C::T, sm, c->stream>>>(
-                b.r1, b.posspec + g0, b.fzm0 + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec_val + g0 * FF,
-                b.rec_z + g0 * FF, b.err);
+                b.r1, b.posspec + g0, b.fzm0 + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec + g0 * FF, b.err);
         }
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
@@ -292,20 +335,28 @@ int volume_impl(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t*
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    constexpr int T = D / 8, G = kGC / T;
-    const size_t sm_g = (size_t)G * padded_len(D) * sizeof(float2) + (size_t)n * sizeof(int2) +
-                        (size_t)p.band * kGC * sizeof(uint16_t);
-    const size_t sm_p = (size_t)P::B * padded_len(D) * sizeof(float2);
-    if (sm_g > 227 * 1024) return TDM_EUNSUPPORTED;
-    if (allow_smem(k_gather<D>, sm_g) || allow_smem(k_ypass<D>, sm_p) || allow_smem(k_xpass<D>, sm_p))
+    const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
+                        (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
+    const size_t sm_p = (size_t)P::B * tstride(D) * sizeof(float2);
+    if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
+    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_p) || allow_smem(k_ypass<D>, sm_p) ||
+        allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
+    if (cnt) {  // planes outside the cap band carry no hits
+        const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
+        cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), c->stream);
+        cudaMemsetAsync(cnt + hi, 0, ((size_t)D * plane - hi) * sizeof(uint32_t), c->stream);
+    }
     cudaEventRecord(c->ev_stage[4], c->stream);
     {
         Launch l(c, K_GATHER);
-        k_gather<D><<<dim3(D / kGX, D / kGY), kGC, sm_g, c->stream>>>(b.rec_val, b.rec_z, b.posspec, n, p, b.acc,
-                                                                      b.tw, b.vol, otf, cnt);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(b.rec, b.posspec, n, p, b.vol, cnt);
     }
     cudaEventRecord(c->ev_stage[5], c->stream);
+    {
+        Launch l(c, K_ZPASS);
+        k_zpass<D><<<dim3(D * D / P::B), P::B * P::T, sm_p, c->stream>>>(b.vol, b.tw, p.zmin, p.band, otf);
+    }
     {
         Launch l(c, K_YPASS);
         k_ypass<D><<<dim3(D / P::B, D), P::B * P::T, sm_p, c->stream>>>(b.vol, b.tw);

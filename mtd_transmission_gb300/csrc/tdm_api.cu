@@ -15,7 +15,7 @@ namespace tdm {
 const char* const kKernelNames[K_COUNT] = {
     "extract_rows", "extract_cols", "argmax", "field_rows", "field_cols", "volkov_rows", "volkov_cols",
     "volkov_integ_rows", "volkov_integ_cols", "aber_fit", "form", "fzm0", "cap_rows", "cap_cols", "gather",
-    "ypass", "xpass", "posspec"};
+    "ypass", "xpass", "posspec", "zpass", "aber_reduce"};
 
 cudaEvent_t prof_event(tdm_ctx* c) {
     if (!c->ev_pool.empty()) {
@@ -79,7 +79,7 @@ void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.fzm0, b.I1, b.phase, b.amp, b.gx, b.qc, b.tq, b.unwrapped, b.beta, b.fields,
-                    b.r1, b.rec_val, b.rec_z, b.acc, b.vol, b.out_re, b.out_im, b.out_otf, b.out_cnt,
+                    b.r1, b.rec, b.fit_part, b.vol, b.out_re, b.out_im, b.out_otf, b.out_cnt,
                     b.samp_idx, b.samp_q, b.rinv, b.err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -323,16 +323,15 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.I1, CH * FF));
     TRY(dev_alloc(c, &b.phase, CH * FF));
     TRY(dev_alloc(c, &b.amp, CH * FF));
-    TRY(dev_alloc(c, &b.gx, CH * L * L));
-    TRY(dev_alloc(c, &b.qc, CH * L * L));
+    TRY(dev_alloc(c, &b.gx, CH * FF));
+    TRY(dev_alloc(c, &b.qc, CH * L * F));
     TRY(dev_alloc(c, &b.tq, CH * L * F));
     TRY(dev_alloc(c, &b.unwrapped, CH * FF));
     TRY(dev_alloc(c, &b.beta, CH * 2 * kNC));
     TRY(dev_alloc(c, &b.fields, M * FF));
     TRY(dev_alloc(c, &b.r1, CH * FF));
-    TRY(dev_alloc(c, &b.rec_val, M * FF));
-    TRY(dev_alloc(c, &b.rec_z, M * FF));
-    TRY(dev_alloc(c, &b.acc, (size_t)D * D * p.band));
+    TRY(dev_alloc(c, &b.rec, M * FF));
+    TRY(dev_alloc(c, &b.fit_part, CH * 2 * kFitSlices * kNC));
     TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
     TRY(dev_alloc(c, &b.err, 4));

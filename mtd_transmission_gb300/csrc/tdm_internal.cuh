@@ -12,6 +12,7 @@
 namespace tdm {
 
 constexpr int kNC = 15;  // degree-4 2D polynomial: 15 monomials
+constexpr int kFitSlices = 8;  // sample slices per fit (one CTA each)
 
 // Device-side parameters of one volume, fixed at context creation.
 struct Params {
@@ -42,16 +43,15 @@ struct Buffers {
     float2* I1 = nullptr;          // chunk x F*F
     float* phase = nullptr;        // chunk x F*F
     float* amp = nullptr;          // chunk x F*F
-    float* gx = nullptr;           // chunk x L*L
-    float2* qc = nullptr;          // chunk x L*L
+    float* gx = nullptr;           // chunk x F*F (right half of the mirror's gx, per image row)
+    float2* qc = nullptr;          // chunk x L*F (FFT along y of Q, columns X >= F)
     float2* tq = nullptr;          // chunk x L*F
     float* unwrapped = nullptr;    // chunk x F*F
     double* beta = nullptr;        // chunk x 2 x kNC
+    double* fit_part = nullptr;    // chunk x 2 x kFitSlices x kNC partial sums of the fits
     float2* fields = nullptr;      // max_angles x F*F
     float2* r1 = nullptr;          // chunk x F*F
-    float2* rec_val = nullptr;     // max_angles x F*F
-    int16_t* rec_z = nullptr;      // max_angles x F*F
-    double2* acc = nullptr;        // (D*D/128) x band x 128 gather accumulators (scratch)
+    float4* rec = nullptr;         // max_angles x F*F cap records (contribution re, im; plane; unused)
     float2* vol = nullptr;         // D^3 complex, [y][x][z] layout
     float* out_re = nullptr;       // D^3 staging when the caller's output is in host memory
     float* out_im = nullptr;
@@ -67,7 +67,7 @@ struct Buffers {
 enum KernelId {
     K_EXTRACT_ROWS, K_EXTRACT_COLS, K_ARGMAX, K_FIELD_ROWS, K_FIELD_COLS, K_VOLKOV_ROWS, K_VOLKOV_COLS,
     K_VOLKOV_INTEG_ROWS, K_VOLKOV_INTEG_COLS, K_ABER_FIT, K_FORM, K_FZM0, K_CAP_ROWS, K_CAP_COLS, K_GATHER,
-    K_YPASS, K_XPASS, K_POSSPEC, K_COUNT
+    K_YPASS, K_XPASS, K_POSSPEC, K_ZPASS, K_ABER_REDUCE, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 

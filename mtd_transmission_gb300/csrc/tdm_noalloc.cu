@@ -89,8 +89,8 @@ template <int H>
 int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F, int x0, int y0,
         cudaStream_t st) {
     using C = ExtractCfg<H>;
-    const size_t sm_rows = (size_t)C::PAIRS * padded_len(H) * sizeof(float2);
-    const size_t sm_cols = (size_t)C::COLS * padded_len(H) * sizeof(float2);
+    const size_t sm_rows = (size_t)C::PAIRS * tstride(H) * sizeof(float2);
+    const size_t sm_cols = (size_t)C::COLS * tstride(H) * sizeof(float2);
     if (sm_rows > 48 * 1024 &&
         cudaFuncSetAttribute(k_extract_rows<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
         return TDM_ECUDA;
