@@ -295,66 +295,64 @@ k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, co
     }
 }
 
-// Pass 3: rows of FFT2(Q), paired with their mirror rows; integ_grad4's
-// tampon; inverse FFT along x; only the quadrant-4 columns are kept.
+// Pass 3: rows ky in [0, L/2] of FFT2(Q); integ_grad4's tampon; inverse FFT
+// along x; only the quadrant-4 columns are kept.  The mirror symmetries of Q
+// give conj(Q^(-k)) = -exp(2 pi i (kx+ky)/L) conj(Q^(k)) (the Hermitian
+// partner needed to separate gx and gy), and the tampon rows obey
+// tam(kx, -ky) = exp(-2 pi i ky/L) tam(kx, ky), so pass 4 rebuilds the rows
+// ky > L/2.  The row's left half comes from the stored right half of row -ky.
 template <int L>
 __global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
 k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw, float2* __restrict__ tq) {
     using C = VolkovCfg<L>;
     constexpr int F = L / 2;
-    static_assert(C::B % 2 == 0, "rows are processed in pairs");
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    const int a = blockIdx.y;
-    const int q = blockIdx.x * (C::B / 2) + (tr >> 1), which = tr & 1;
-    int r, ptr;
-    if (q == 0) {          // rows 0 and L/2 are their own mirrors
-        r = which ? L / 2 : 0;
-        ptr = tr;
-    } else {
-        r = which ? L - q : q;
-        ptr = tr ^ 1;
-    }
+    const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
+    const bool active = r <= L / 2;
     float2* s = sm + tr * tstride(L);
-    const float2* sp = sm + ptr * tstride(L);
-    // Qc holds columns X >= F; Qc[ky][X] = -conj(Qc[-ky][L-1-X]) for X < F
-    const int rp = (L - r) & (L - 1);
+    if (active) {
+        const int rp = (L - r) & (L - 1);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int X = j + t * C::T;
-        if (X >= F) {
-            s[pad_idx(X)] = qc[((size_t)a * L + r) * F + (X - F)];
-        } else {
-            const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
-            s[pad_idx(X)] = make_float2(-u.x, u.y);
+        for (int t = 0; t < 8; ++t) {
+            const int X = j + t * C::T;
+            if (X >= F) {
+                s[pad_idx(X)] = qc[((size_t)a * L + r) * F + (X - F)];
+            } else {
+                const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
+                s[pad_idx(X)] = make_float2(-u.x, u.y);
+            }
         }
     }
     __syncthreads();
-    fft_smem<L, -1>(s, j, tw);
-    const float nrm = 1.0f / ((float)L * (float)L);
-    const float ky = kappa(r, L);
-    float2 tam[8];
+    fft_smem<L, -1>(s, j, tw, active);
+    if (active) {
+        const float nrm = 1.0f / ((float)L * (float)L);
+        const float ky = kappa(r, L);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int kx = j + t * C::T, kxm = (L - kx) & (L - 1);
-        const float2 Q = s[pad_idx(kx)], Qm = sp[pad_idx(kxm)];
-        const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y - Qm.y) * nrm);
-        const float2 Gy = make_float2(0.5f * (Q.y + Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
-        const float kxv = kappa(kx, L);
-        const float k2 = kxv * kxv + ky * ky;
-        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
-        const float den = kTwoPi * k2;
-        tam[t] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
+        for (int t = 0; t < 8; ++t) {
+            const int kx = j + t * C::T;
+            const float2 Q = s[pad_idx(kx)];
+            const float2 w = __ldg(&tw[((kx + r) & (L - 1)) * (kTwN / L)]);  // exp(-2 pi i (kx+ky)/L)
+            // Qm = conj(Q^(-k)) = -exp(+2 pi i (kx+ky)/L) conj(Q)
+            const float2 Qm = make_float2(-(w.x * Q.x - w.y * Q.y), -(-w.y * Q.x - w.x * Q.y));
+            const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y + Qm.y) * nrm);
+            const float2 Gy = make_float2(0.5f * (Q.y - Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
+            const float kxv = kappa(kx, L);
+            const float k2 = kxv * kxv + ky * ky;
+            const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
+            const float den = kTwoPi * k2;
+            s[pad_idx(kx)] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
+        }
     }
     __syncthreads();
+    fft_smem<L, +1>(s, j, tw, active);
+    if (active) {
 #pragma unroll
-    for (int t = 0; t < 8; ++t) s[pad_idx(j + t * C::T)] = tam[t];
-    __syncthreads();
-    fft_smem<L, +1>(s, j, tw);
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int X = j + t * C::T;
-        if (X >= F) tq[((size_t)a * L + r) * F + (X - F)] = s[pad_idx(X)];
+        for (int t = 0; t < 8; ++t) {
+            const int X = j + t * C::T;
+            if (X >= F) tq[((size_t)a * L + r) * F + (X - F)] = s[pad_idx(X)];
+        }
     }
 }
 
@@ -372,7 +370,15 @@ k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ pha
 #pragma unroll
     for (int r = 0; r < B * L / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
-        sm[t * tstride(L) + pad_idx(ky)] = tq[((size_t)a * L + ky) * F + c0 + t];
+        float2 v;
+        if (ky <= L / 2) {
+            v = tq[((size_t)a * L + ky) * F + c0 + t];
+        } else {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
+            const float2 u = tq[((size_t)a * L + (L - ky)) * F + c0 + t];
+            const float2 w = __ldg(&tw[ky * (kTwN / L)]);  // exp(-2 pi i ky/L)
+            v = make_float2(w.x * u.x + w.y * u.y, w.x * u.y - w.y * u.x);
+        }
+        sm[t * tstride(L) + pad_idx(ky)] = v;
     }
     __syncthreads();
     fft_smem<L, +1>(sm + tr * tstride(L), j, tw);
@@ -534,7 +540,8 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_ROWS);
-                k_volkov_integ_rows<L><<<dim3(L / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(b.qc, b.tw, b.tq);
+                k_volkov_integ_rows<L><<<dim3((L / 2 + VC::B) / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(
+                    b.qc, b.tw, b.tq);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
