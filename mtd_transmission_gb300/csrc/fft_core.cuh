@@ -23,6 +23,14 @@ namespace tdm {
 
 constexpr int kTwN = 4096;  // twiddle table size: exp(-2 pi i k / 4096)
 
+// Points per lane of the warp-resident FFT of size n (fft_warp.cuh).
+__host__ __device__ constexpr int warp_fft_e(int n) { return n >= 2048 ? 64 : n >= 512 ? 32 : n >= 128 ? 16 : 8; }
+// Offset of the per-lane twiddle factors of the n-point warp FFT in the
+// device twiddle table (after the kTwN-entry table): one n-entry block per
+// size 64, 128, ..., 2048.
+__host__ __device__ constexpr int twr_offset(int n) { return kTwN + n - 64; }
+constexpr int kTwTotal = kTwN + 4096 - 64;
+
 __host__ __device__ constexpr int pad_idx(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4); }
 // Distance between consecutive transforms of a CTA in shared memory: odd, so

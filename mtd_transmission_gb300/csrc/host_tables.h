@@ -4,7 +4,32 @@
 #include <cmath>
 #include <vector>
 
+#include "fft_core.cuh"
+
 namespace tdm {
+
+// Twiddle table uploaded to the device: exp(-2 pi i k / kTwN) for k < kTwN,
+// then, for each warp-FFT size N = 64 .. 2048 at offset twr_offset(N), the
+// factors exp(-2 pi i j k1 / N) laid out [k1][j] for k1 < E(N), j < T(N),
+// so that the T lanes of a transform read consecutive entries.  Computed in
+// long double and rounded once to float.
+inline std::vector<float2> twiddle_table() {
+    const long double two_pi = 2.0L * 3.14159265358979323846264338327950288L;
+    std::vector<float2> tw(kTwTotal);
+    for (int k = 0; k < kTwN; ++k) {
+        const long double a = -two_pi * k / kTwN;
+        tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    for (int n = 64; n <= 2048; n *= 2) {
+        const int e = warp_fft_e(n), t = n / e;
+        for (int k1 = 0; k1 < e; ++k1)
+            for (int j = 0; j < t; ++j) {
+                const long double a = -two_pi * (long double)((j * k1) % n) / n;
+                tw[twr_offset(n) + k1 * t + j] = make_float2((float)std::cos(a), (float)std::sin(a));
+            }
+    }
+    return tw;
+}
 
 // Tukey window factor, same float arithmetic as tukey2D
 // (pretraitement_hors_axe_CPU/FFT_fonctions.cpp:61-87): the 2D window is the

@@ -7,7 +7,8 @@
 //     crop[ky][kx] = (-1)^(kx+ky) / H^2 * FFT2((-1)^(x+y) w(x) w(y) h)[ky][kx]
 // with (kx, ky) in the crop window.  The row pass packs two real rows into one
 // complex FFT and keeps only the crop's kx band; the column pass transforms
-// only those F columns and keeps only the crop's ky rows.
+// only those F columns and keeps only the crop's ky rows.  Kernels in
+// extract_kernels.cuh.
 #include "extract_kernels.cuh"
 
 namespace tdm {
@@ -25,8 +26,7 @@ template <int H>
 int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
     using C = ExtractCfg<H>;
     const Params& p = c->p;
-    const size_t sm_rows = (size_t)C::PAIRS * tstride(H) * sizeof(float2);
-    const size_t sm_cols = (size_t)C::COLS * tstride(H) * sizeof(float2);
+    const size_t sm_rows = C::smem_rows(p.F), sm_cols = C::smem_cols(p.F);
     if (allow_smem(k_extract_rows<H>, sm_rows) != cudaSuccess) return TDM_ECUDA;
     if (allow_smem(k_extract_cols<H>, sm_cols) != cudaSuccess) return TDM_ECUDA;
     const size_t bytes_per = (size_t)H * H * (bits == 16 ? 2 : 1);
@@ -35,12 +35,12 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
         const char* src = static_cast<const char*>(holos) + (size_t)h0 * bytes_per;
         {
             Launch l(c, K_EXTRACT_ROWS);
-            k_extract_rows<H><<<dim3(H / 2 / C::PAIRS, m), C::PAIRS * C::T, sm_rows, c->stream>>>(
-                src, bits, c->b.tuk_h, c->b.tw, c->b.inter, p.F, p.x0);
+            k_extract_rows<H><<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->b.tw,
+                                                                             c->b.inter, p.F, p.x0);
         }
         {
             Launch l(c, K_EXTRACT_COLS);
-            k_extract_cols<H><<<dim3(p.F / C::COLS, m), C::COLS * C::T, sm_cols, c->stream>>>(
+            k_extract_cols<H><<<C::grid_cols(p.F, m), C::NT, sm_cols, c->stream>>>(
                 c->b.inter, c->b.tw, c->b.spectra + (size_t)(a0 + h0) * p.F * p.F, p.F, p.x0, p.y0);
         }
     }

@@ -18,6 +18,7 @@
 //             orthonormal over the sample points (same projection as the
 //             reference's normal equations, better conditioned).
 #include "tdm_internal.cuh"
+#include "fft_warp.cuh"
 
 namespace tdm {
 namespace {
@@ -79,19 +80,27 @@ __global__ void __launch_bounds__(1024) k_argmax(const float2* __restrict__ spec
 }
 
 // ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
+// All FFT passes below run on the warp-resident FFT (fft_warp.cuh).  A row
+// pass loads and stores its lanes' elements directly (lane-minor order is
+// contiguous along a row); a column pass stages B columns in shared memory
+// with CTA-wide coalesced loads and stores around the transforms.
 template <int F>
 struct FieldCfg {
-    static constexpr int T = F / 8;
-    static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;
+    using W = WarpFFT<F>;
+    static constexpr int B = 8 * W::G;       // transforms per CTA
+    static constexpr int NT = B * W::T;      // 256 threads
+    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
 template <int F>
-__global__ void __launch_bounds__(FieldCfg<F>::B * (F / 8))
+__global__ void __launch_bounds__(FieldCfg<F>::NT)
 k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspec, const float2* __restrict__ specval,
              int normalize, const float2* __restrict__ tw, float2* __restrict__ I1) {
     using C = FieldCfg<F>;
+    using W = typename C::W;
+    constexpr int T = W::T, E = W::E;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
     const int2 p = posspec[a];
     float2 nrm = make_float2(1.0f, 0.0f);
@@ -100,46 +109,45 @@ k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspe
         const float mod = sqrtf(s0.y * s0.y + s0.x * s0.x);
         nrm = make_float2(s0.x / mod, -s0.y / mod);
     }
-    float2* s = sm + tr * tstride(F);
     const float2* src = spectra + ((size_t)a * F + ((r + p.y) & (F - 1))) * F;
+    float2 x[E];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int kx = j + t * C::T;
-        float2 v = src[(kx + p.x) & (F - 1)];
-        if (normalize) v = c_mul(v, nrm);
-        s[pad_idx(kx)] = v;
+    for (int n1 = 0; n1 < E; ++n1) {
+        float2 v = src[(j + n1 * T + p.x) & (F - 1)];
+        x[n1] = normalize ? c_mul(v, nrm) : v;
     }
-    __syncthreads();
-    fft_smem<F, +1>(s, j, tw);
+    fft_warp_regs<F, +1>(x, sm + tr * W::STRIDE, j, tw);
+    float2* dst = I1 + ((size_t)a * F + r) * F;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int x = j + t * C::T;
-        I1[((size_t)a * F + r) * F + x] = s[pad_idx(x)];
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) dst[j + q * T + E * k2] = x[q * T + k2];
     }
 }
 
 // mode 1: phase/amplitude (C_ABER); mode 0: the field itself is the result.
 template <int F>
-__global__ void __launch_bounds__(FieldCfg<F>::B * (F / 8))
+__global__ void __launch_bounds__(FieldCfg<F>::NT)
 k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ tw, float* __restrict__ phase,
              float* __restrict__ amp, float2* __restrict__ fields) {
     using C = FieldCfg<F>;
-    constexpr int B = C::B;
+    using W = typename C::W;
+    constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    constexpr int NT = B * C::T;
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, x0 = blockIdx.x * B;
-#pragma unroll
+#pragma unroll 8
     for (int r0 = 0; r0 < B * F / NT; ++r0) {
         const int i = threadIdx.x + r0 * NT, t = i % B, r = i / B;
-        sm[t * tstride(F) + pad_idx(r)] = I1[((size_t)a * F + r) * F + x0 + t];
+        sm[t * W::STRIDE + W::pad(r)] = I1[((size_t)a * F + r) * F + x0 + t];
     }
     __syncthreads();
-    fft_smem<F, +1>(sm + tr * tstride(F), j, tw);
-#pragma unroll
+    fft_warp<F, +1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
+#pragma unroll 8
     for (int r0 = 0; r0 < B * F / NT; ++r0) {
         const int i = threadIdx.x + r0 * NT, t = i % B, y = i / B;
-        const float2 u = sm[t * tstride(F) + pad_idx(y)];
+        const float2 u = sm[t * W::STRIDE + W::pad(y)];
         const int yo = (y + F / 2) & (F - 1), xo = (x0 + t + F / 2) & (F - 1);
         const size_t o = ((size_t)a * F + yo) * F + xo;
         if (mode) {
@@ -152,75 +160,80 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
 }
 
 // ---------------------------------------------------------------- Volkov unwrap
+// i 2 pi kappa(k) / L: the spectral derivative factor of gradient_fft4.
 template <int L>
-struct VolkovCfg {
-    static constexpr int T = L / 8;
-    static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;  // rows/columns per CTA
+struct DerivMul {
+    __device__ __forceinline__ float2 operator()(int k, float2 z) const {
+        const float c = kTwoPi * kappa(k, L) / (float)L;
+        return make_float2(-c * z.y, c * z.x);
+    }
+};
+
+// Transforms of the two Volkov derivative passes: per pair of image rows (or
+// columns), the Z = exp(i phi) transform of each, then one transform of both
+// phases packed as phi_a + i phi_b.  The 2P Z transforms come first so that
+// a warp never mixes the two kinds.
+template <int L>
+struct VCfg {
+    using W = WarpFFT<L>;
+    static constexpr int P = 4;                 // row or column pairs per CTA
+    static constexpr int B = 3 * P;             // transforms per CTA
+    static constexpr int NT = B * W::T;
+    static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
 // row, and the spectral x derivative of a mirror row is odd about the row's
 // centre (its Nyquist bin is zero), so only image rows y are transformed and
 // only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi is kept:
-// gx[Y][X] = sign(X) gxh[m(Y)][m(X)].  Per pair of image rows: the Z row of
-// each, and both phase rows packed into one complex row (their derivatives
-// are real).
+// gx[Y][X] = sign(X) gxh[m(Y)][m(X)].
 template <int L>
-struct V1Cfg {
-    static constexpr int T = L / 8;
-    static constexpr int P = (384 / (3 * T)) >= 1 ? 384 / (3 * T) : 1;  // row pairs per CTA
-};
-
-template <int L>
-__global__ void __launch_bounds__(3 * V1Cfg<L>::P * (L / 8))
+__global__ void __launch_bounds__(VCfg<L>::NT)
 k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, float* __restrict__ gxh) {
-    using C = V1Cfg<L>;
-    constexpr int F = L / 2, T = C::T;
+    using C = VCfg<L>;
+    using W = typename C::W;
+    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
-    const int pair = tr / 3, kind = tr % 3;  // kind 0: Z of row a, 1: Z of row b, 2: phases packed
+    const bool zk = tr < 2 * P;                       // Z transform of one row, else packed phases of a pair
+    const int pair = zk ? tr >> 1 : tr - 2 * P, ab = tr & 1;
     const int a = blockIdx.y;
-    const int ya = blockIdx.x * 2 * C::P + 2 * pair, yb = ya + 1;
-    float2* s = sm + tr * tstride(L);
+    const int ya = blockIdx.x * 2 * P + 2 * pair, yb = ya + 1;
+    float2* s = sm + tr * W::STRIDE;
     const float* pa = phase + ((size_t)a * F + ya) * F;
     const float* pb = phase + ((size_t)a * F + yb) * F;
-    float v[8];
+    float2 x[E];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int X = j + t * T, mx = mirror(X, F);
-        const float fa = pa[mx], fb = pb[mx];
-        if (kind == 2) {
-            s[pad_idx(X)] = make_float2(fa, fb);
-        } else {
-            v[t] = kind == 0 ? fa : fb;
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int mx = mirror(j + n1 * T, F);
+        if (zk) {
             float sn, cs;
-            sincosf(v[t], &sn, &cs);
-            s[pad_idx(X)] = make_float2(cs, sn);
+            sincosf((ab ? pb : pa)[mx], &sn, &cs);
+            x[n1] = make_float2(cs, sn);
+        } else {
+            x[n1] = make_float2(pa[mx], pb[mx]);
         }
     }
-    __syncthreads();
-    fft_smem<L, -1>(s, j, tw);
+    fft_warp_filter<L, -1>(x, s, j, tw, DerivMul<L>{});
+    if (!zk) {  // dphi/dx of both rows, right half X >= F (n1 >= E/2)
+        __syncwarp();
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int k = j + t * T;
-        const float c = kTwoPi * kappa(k, L) / (float)L;
-        const float2 z = s[pad_idx(k)];
-        s[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
+        for (int n1 = E / 2; n1 < E; ++n1) s[j + n1 * (T + 1)] = x[n1];
     }
     __syncthreads();
-    fft_smem<L, +1>(s, j, tw);
-    if (kind < 2) {
-        const float2* sp = sm + (3 * pair + 2) * tstride(L);
-        float* out = gxh + ((size_t)a * F + (kind == 0 ? ya : yb)) * F;
+    if (zk) {
+        const float2* sp = sm + (2 * P + pair) * W::STRIDE;
+        const float* pr = ab ? pb : pa;
+        float* out = gxh + ((size_t)a * F + (ab ? yb : ya)) * F;
 #pragma unroll
-        for (int t = 4; t < 8; ++t) {  // X = j + t T >= F
-            const int X = j + t * T;
+        for (int n1 = E / 2; n1 < E; ++n1) {
+            const int X = j + n1 * T;
             float sn, cs;
-            sincosf(v[t], &sn, &cs);
-            const float2 g = s[pad_idx(X)];
+            sincosf(pr[X - F], &sn, &cs);  // mirror(X) = X - F on the right half
+            const float2 g = x[n1];
             const float ax = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);  // Re(-i g / Z)
-            const float2 q = sp[pad_idx(X)];
-            out[X - F] = (ax - (kind == 0 ? q.x : q.y)) * kInvTwoPi;
+            const float2 q = sp[j + n1 * (T + 1)];
+            out[X - F] = (ax - (ab ? q.y : q.x)) * kInvTwoPi;
         }
     }
 }
@@ -230,24 +243,19 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, fl
 // columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
 // pass 3.
 template <int L>
-struct V2Cfg {
-    static constexpr int T = L / 8;
-    static constexpr int P = (768 / (3 * T)) >= 1 ? 768 / (3 * T) : 1;  // column pairs per CTA
-};
-
-template <int L>
-__global__ void __launch_bounds__(3 * V2Cfg<L>::P * (L / 8))
+__global__ void __launch_bounds__(VCfg<L>::NT)
 k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, const float2* __restrict__ tw,
               float2* __restrict__ qc) {
-    using C = V2Cfg<L>;
-    constexpr int F = L / 2, T = C::T, P = C::P, NC = 2 * P, NT = 3 * P * T, LS = L + 1;
+    using C = VCfg<L>;
+    using W = typename C::W;
+    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P, NC = 2 * P, NT = C::NT, LS = L + 1;
     extern __shared__ float2 sm[];
-    float* sph = reinterpret_cast<float*>(sm + 3 * P * tstride(L));  // NC x LS phase along the mirror column
-    float* sgx = sph + NC * LS;                                      // NC x LS gx along the mirror column
+    float* sph = reinterpret_cast<float*>(sm + C::B * W::STRIDE);  // NC x LS phase along the mirror column
+    float* sgx = sph + NC * LS;                                    // NC x LS gx along the mirror column
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
-    const int pair = tr / 3, kind = tr % 3;
+    const bool zk = tr < NC;
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
-#pragma unroll 6
+#pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, Y = i / NC;
         const size_t src = ((size_t)a * F + mirror(Y, F)) * F + x0 + c;
@@ -256,42 +264,47 @@ k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, co
         sgx[c * LS + Y] = gxh[src];
         float sn, cs;
         sincosf(v, &sn, &cs);
-        const int pp = c >> 1, ab = c & 1;
-        sm[(3 * pp + ab) * tstride(L) + pad_idx(Y)] = make_float2(cs, sn);
-        reinterpret_cast<float*>(&sm[(3 * pp + 2) * tstride(L) + pad_idx(Y)])[ab] = v;
+        sm[c * W::STRIDE + W::pad(Y)] = make_float2(cs, sn);
+        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * W::STRIDE + W::pad(Y)])[c & 1] = v;
     }
     __syncthreads();
-    float2* s = sm + tr * tstride(L);
-    fft_smem<L, -1>(s, j, tw);
+    float2* s = sm + tr * W::STRIDE;
+    float2 x[E];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int k = j + t * T;
-        const float c = kTwoPi * kappa(k, L) / (float)L;
-        const float2 z = s[pad_idx(k)];
-        s[pad_idx(k)] = make_float2(-c * z.y, c * z.x);
+    for (int n1 = 0; n1 < E; ++n1) x[n1] = s[j + n1 * (T + 1)];
+    fft_warp_filter<L, -1>(x, s, j, tw, DerivMul<L>{});
+    if (!zk) {
+        __syncwarp();
+#pragma unroll
+        for (int n1 = 0; n1 < E; ++n1) s[j + n1 * (T + 1)] = x[n1];
     }
     __syncthreads();
-    fft_smem<L, +1>(s, j, tw);
-    if (kind < 2) {
-        const int c = 2 * pair + kind;
-        const float2* sp = sm + (3 * pair + 2) * tstride(L);
+    if (zk) {  // warp-uniform
+        const int c = tr;
+        const float2* sp = sm + (NC + (c >> 1)) * W::STRIDE;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int Y = j + t * T;
+        for (int n1 = 0; n1 < E; ++n1) {
+            const int Y = j + n1 * T;
             float sn, cs;
             sincosf(sph[c * LS + Y], &sn, &cs);
-            const float2 g = s[pad_idx(Y)];
+            const float2 g = x[n1];
             const float ay = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);
-            const float2 q = sp[pad_idx(Y)];
-            s[pad_idx(Y)] = make_float2(sgx[c * LS + Y], (ay - (kind == 0 ? q.x : q.y)) * kInvTwoPi);
+            const float2 q = sp[j + n1 * (T + 1)];
+            x[n1] = make_float2(sgx[c * LS + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
+        }
+        fft_warp_regs<L, -1>(x, s, j, tw);
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+            for (int k2 = 0; k2 < T; ++k2) s[warp_out_pos<L>(j, q, k2)] = x[q * T + k2];
         }
     }
     __syncthreads();
-    fft_smem<L, -1>(s, j, tw, kind < 2);
-#pragma unroll 6
+#pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, ky = i / NC;
-        qc[((size_t)a * L + ky) * F + x0 + c] = sm[(3 * (c >> 1) + (c & 1)) * tstride(L) + pad_idx(ky)];
+        qc[((size_t)a * L + ky) * F + x0 + c] = sm[c * W::STRIDE + W::pad(ky)];
     }
 }
 
@@ -302,72 +315,79 @@ k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, co
 // tam(kx, -ky) = exp(-2 pi i ky/L) tam(kx, ky), so pass 4 rebuilds the rows
 // ky > L/2.  The row's left half comes from the stored right half of row -ky.
 template <int L>
-__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+struct TamMul {
+    const float2* tw;
+    int r;
+    float nrm, ky;
+    __device__ __forceinline__ float2 operator()(int kx, float2 Q) const {
+        const float2 w = __ldg(&tw[((kx + r) & (L - 1)) * (kTwN / L)]);  // exp(-2 pi i (kx+ky)/L)
+        // Qm = conj(Q^(-k)) = -exp(+2 pi i (kx+ky)/L) conj(Q)
+        const float2 Qm = make_float2(-(w.x * Q.x - w.y * Q.y), -(-w.y * Q.x - w.x * Q.y));
+        const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y + Qm.y) * nrm);
+        const float2 Gy = make_float2(0.5f * (Q.y - Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
+        const float kxv = kappa(kx, L);
+        const float k2 = kxv * kxv + ky * ky;
+        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
+        const float den = kTwoPi * k2;
+        return (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
+    }
+};
+
+template <int L>
+struct ICfg {
+    using W = WarpFFT<L>;
+    static constexpr int B = 8 * W::G;   // rows or columns per CTA
+    static constexpr int NT = B * W::T;
+    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
+};
+
+template <int L>
+__global__ void __launch_bounds__(ICfg<L>::NT)
 k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw, float2* __restrict__ tq) {
-    using C = VolkovCfg<L>;
-    constexpr int F = L / 2;
+    using C = ICfg<L>;
+    using W = typename C::W;
+    constexpr int F = L / 2, T = W::T, E = W::E;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
-    const bool active = r <= L / 2;
-    float2* s = sm + tr * tstride(L);
-    if (active) {
-        const int rp = (L - r) & (L - 1);
+    const bool active = r <= L / 2;  // rows past L/2 only keep their warp company
+    const int rp = (L - r) & (L - 1);
+    float2 x[E];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int X = j + t * C::T;
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int X = j + n1 * T;
+        float2 v = make_float2(0.f, 0.f);
+        if (active) {
             if (X >= F) {
-                s[pad_idx(X)] = qc[((size_t)a * L + r) * F + (X - F)];
+                v = qc[((size_t)a * L + r) * F + (X - F)];
             } else {
                 const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
-                s[pad_idx(X)] = make_float2(-u.x, u.y);
+                v = make_float2(-u.x, u.y);
             }
         }
+        x[n1] = v;
     }
-    __syncthreads();
-    fft_smem<L, -1>(s, j, tw, active);
+    fft_warp_filter<L, -1>(x, sm + tr * W::STRIDE, j, tw,
+                           TamMul<L>{tw, r, 1.0f / ((float)L * (float)L), kappa(r, L)});
     if (active) {
-        const float nrm = 1.0f / ((float)L * (float)L);
-        const float ky = kappa(r, L);
+        float2* dst = tq + ((size_t)a * L + r) * F - F;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int kx = j + t * C::T;
-            const float2 Q = s[pad_idx(kx)];
-            const float2 w = __ldg(&tw[((kx + r) & (L - 1)) * (kTwN / L)]);  // exp(-2 pi i (kx+ky)/L)
-            // Qm = conj(Q^(-k)) = -exp(+2 pi i (kx+ky)/L) conj(Q)
-            const float2 Qm = make_float2(-(w.x * Q.x - w.y * Q.y), -(-w.y * Q.x - w.x * Q.y));
-            const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y + Qm.y) * nrm);
-            const float2 Gy = make_float2(0.5f * (Q.y - Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
-            const float kxv = kappa(kx, L);
-            const float k2 = kxv * kxv + ky * ky;
-            const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
-            const float den = kTwoPi * k2;
-            s[pad_idx(kx)] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
-        }
-    }
-    __syncthreads();
-    fft_smem<L, +1>(s, j, tw, active);
-    if (active) {
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int X = j + t * C::T;
-            if (X >= F) tq[((size_t)a * L + r) * F + (X - F)] = s[pad_idx(X)];
-        }
+        for (int n1 = E / 2; n1 < E; ++n1) dst[j + n1 * T] = x[n1];
     }
 }
 
 // Pass 4: columns of quadrant 4: inverse FFT along y, real part, phi + 2 pi IntM.
 template <int L>
-__global__ void __launch_bounds__(VolkovCfg<L>::B * (L / 8))
+__global__ void __launch_bounds__(ICfg<L>::NT)
 k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ phase, const float2* __restrict__ tw,
                     float* __restrict__ unwrapped) {
-    using C = VolkovCfg<L>;
-    constexpr int F = L / 2, B = C::B;
+    using C = ICfg<L>;
+    using W = typename C::W;
+    constexpr int F = L / 2, B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    constexpr int NT = B * C::T;
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, c0 = blockIdx.x * B;
-#pragma unroll
+#pragma unroll 8
     for (int r = 0; r < B * L / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
         float2 v;
@@ -378,15 +398,16 @@ k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ pha
             const float2 w = __ldg(&tw[ky * (kTwN / L)]);  // exp(-2 pi i ky/L)
             v = make_float2(w.x * u.x + w.y * u.y, w.x * u.y - w.y * u.x);
         }
-        sm[t * tstride(L) + pad_idx(ky)] = v;
+        sm[t * W::STRIDE + W::pad(ky)] = v;
     }
     __syncthreads();
-    fft_smem<L, +1>(sm + tr * tstride(L), j, tw);
-#pragma unroll
+    fft_warp<L, +1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
+#pragma unroll 8
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, y = i / B;
         const size_t o = ((size_t)a * F + y) * F + c0 + t;
-        unwrapped[o] = phase[o] + kTwoPi * sm[t * tstride(L) + pad_idx(F + y)].x;
+        unwrapped[o] = phase[o] + kTwoPi * sm[t * W::STRIDE + W::pad(F + y)].x;
     }
 }
 
@@ -494,19 +515,16 @@ template <int F>
 int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp) {
     constexpr int L = 2 * F;
     using FC = FieldCfg<F>;
-    using VC = VolkovCfg<L>;
+    using VC = VCfg<L>;
+    using IC = ICfg<L>;
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
-    const size_t sm_field = (size_t)FC::B * tstride(F) * sizeof(float2);
-    using V1 = V1Cfg<L>;
-    using V2 = V2Cfg<L>;
-    const size_t sm_vrows = (size_t)3 * V1::P * tstride(L) * sizeof(float2);
-    const size_t sm_vcols = (size_t)3 * V2::P * tstride(L) * sizeof(float2) + (size_t)2 * 2 * V2::P * (L + 1) * sizeof(float);
-    const size_t sm_vir = (size_t)VC::B * tstride(L) * sizeof(float2);
-    if (allow_smem(k_field_rows<F>, sm_field) || allow_smem(k_field_cols<F>, sm_field) ||
+    const size_t sm_vrows = (size_t)VC::B * VC::W::STRIDE * sizeof(float2);
+    const size_t sm_vcols = sm_vrows + (size_t)2 * 2 * VC::P * (L + 1) * sizeof(float);
+    if (allow_smem(k_field_rows<F>, FC::SMEM) || allow_smem(k_field_cols<F>, FC::SMEM) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
-        allow_smem(k_volkov_integ_rows<L>, sm_vir) || allow_smem(k_volkov_integ_cols<L>, sm_vir))
+        allow_smem(k_volkov_integ_rows<L>, IC::SMEM) || allow_smem(k_volkov_integ_cols<L>, IC::SMEM))
         return TDM_ECUDA;
     {
         Launch l(c, K_ARGMAX);
@@ -517,12 +535,12 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         const float2* spec = b.spectra + (size_t)g0 * FF;
         {
             Launch l(c, K_FIELD_ROWS);
-            k_field_rows<F><<<dim3(F / FC::B, m), FC::B * FC::T, sm_field, c->stream>>>(
+            k_field_rows<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
                 spec, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
         }
         {
             Launch l(c, K_FIELD_COLS);
-            k_field_cols<F><<<dim3(F / FC::B, m), FC::B * FC::T, sm_field, c->stream>>>(
+            k_field_cols<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
                 b.I1, p.c_aber, b.tw, b.phase, b.amp, b.fields + (size_t)g0 * FF);
         }
         if (!p.c_aber) continue;
@@ -530,22 +548,22 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                k_volkov_rows<L><<<dim3(F / (2 * V1::P), m), 3 * V1::P * V1::T, sm_vrows, c->stream>>>(b.phase, b.tw,
+                k_volkov_rows<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vrows, c->stream>>>(b.phase, b.tw,
                                                                                                      b.gx);
             }
             {
                 Launch l(c, K_VOLKOV_COLS);
-                k_volkov_cols<L><<<dim3(F / (2 * V2::P), m), 3 * V2::P * V2::T, sm_vcols, c->stream>>>(b.phase, b.gx,
+                k_volkov_cols<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vcols, c->stream>>>(b.phase, b.gx,
                                                                                                      b.tw, b.qc);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_ROWS);
-                k_volkov_integ_rows<L><<<dim3((L / 2 + VC::B) / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(
+                k_volkov_integ_rows<L><<<dim3((L / 2 + IC::B) / IC::B, m), IC::NT, IC::SMEM, c->stream>>>(
                     b.qc, b.tw, b.tq);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
-                k_volkov_integ_cols<L><<<dim3(F / VC::B, m), VC::B * VC::T, sm_vir, c->stream>>>(b.tq, b.phase, b.tw,
+                k_volkov_integ_cols<L><<<dim3(F / IC::B, m), IC::NT, IC::SMEM, c->stream>>>(b.tq, b.phase, b.tw,
                                                                                                   b.unwrapped);
             }
             unw = b.unwrapped;

@@ -21,6 +21,7 @@
 // The z transform is done by the gather CTA on its columns, then a y pass and
 // an x pass that writes the index and absorption volumes.
 #include "tdm_internal.cuh"
+#include "fft_warp.cuh"
 
 namespace tdm {
 namespace {
@@ -33,8 +34,10 @@ cudaError_t allow_smem(K kernel, size_t bytes) {
 
 template <int F>
 struct CapCfg {
-    static constexpr int T = F / 8;
-    static constexpr int B = (256 / T) >= 1 ? 256 / T : 1;
+    using W = WarpFFT<F>;
+    static constexpr int B = 8 * W::G;    // transforms per CTA
+    static constexpr int NT = B * W::T;   // 256 threads
+    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
 // fzm0 per angle (fonctions.cpp:893-899); negative when the angle is skipped.
@@ -47,48 +50,51 @@ __global__ void k_fzm0(const int2* __restrict__ posspec, int n, int N, double ra
 }
 
 template <int F>
-__global__ void __launch_bounds__(CapCfg<F>::B * (F / 8))
+__global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, const float2* __restrict__ tw,
            float2* __restrict__ r1) {
     using C = CapCfg<F>;
+    using W = typename C::W;
+    constexpr int T = W::T, E = W::E;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, y = blockIdx.x * C::B + tr;
-    float2* s = sm + tr * tstride(F);
     const float wy = tuk[y];
     const float2* src = fields + ((size_t)a * F + y) * F;
+    float2 x[E];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int x = j + t * C::T;
-        s[pad_idx(x)] = c_scale(src[x], tuk[x] * wy);
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int xx = j + n1 * T;
+        x[n1] = c_scale(src[xx], __ldg(&tuk[xx]) * wy);
     }
-    __syncthreads();
-    fft_smem<F, -1>(s, j, tw);
+    fft_warp_regs<F, -1>(x, sm + tr * W::STRIDE, j, tw);
+    float2* dst = r1 + ((size_t)a * F + y) * F;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        const int k = j + t * C::T;
-        r1[((size_t)a * F + y) * F + k] = s[pad_idx(k)];
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) dst[j + q * T + E * k2] = x[q * T + k2];
     }
 }
 
 template <int F>
-__global__ void __launch_bounds__(CapCfg<F>::B * (F / 8))
+__global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ fzm0,
            const double* __restrict__ s_tab, const float* __restrict__ s_tabf, Params p,
            const float2* __restrict__ tw, float4* __restrict__ rec, int* __restrict__ err) {
     using C = CapCfg<F>;
-    constexpr int B = C::B;
+    using W = typename C::W;
+    constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
-    constexpr int NT = B * C::T;
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, kx0 = blockIdx.x * B;
-#pragma unroll
+#pragma unroll 8
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
-        sm[t * tstride(F) + pad_idx(ky)] = r1[((size_t)a * F + ky) * F + kx0 + t];
+        sm[t * W::STRIDE + W::pad(ky)] = r1[((size_t)a * F + ky) * F + kx0 + t];
     }
     __syncthreads();
-    fft_smem<F, -1>(sm + tr * tstride(F), j, tw);
+    fft_warp<F, -1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
     const int2 ps = posspec[a];
     const double fz = fzm0[a];
     const float fzf = (float)fz;
@@ -113,7 +119,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
                 atomicOr(err, 1);
                 z = -1;
             } else {
-                float2 v = sm[t * tstride(F) + pad_idx(ky)];
+                float2 v = sm[t * W::STRIDE + W::pad(ky)];
                 const float sg = ((kx + ky) & 1) ? -p.dx2 : p.dx2;
                 const float Bc = p.cap_scale * (sf * (float)p.inv_rayon) * sg;  // (k0/pi)(-2pi) sdz dx^2 (+-1)
                 val = make_float2(-Bc * v.y, Bc * v.x);
@@ -208,95 +214,108 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
     }
 }
 
+// Volume passes: B transforms of D points per CTA on the warp-resident FFT.
 template <int D>
 struct PassCfg {
-    static constexpr int T = D / 8;
-    static constexpr int B = (1024 / T) < 16 ? (1024 / T) : 16;
+    using W = WarpFFT<D>;
+    static constexpr int B = 16;           // transforms per CTA
+    static constexpr int NT = B * W::T;    // threads per CTA
+    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
-// inverse FFT along z (contiguous) for B consecutive columns of the [y][x][z]
-// volume; planes outside the cap band are zero and are not read.
-// The OTF mask (Re != 0 after normalisation, main.cpp:262-267) is written
-// here, from the spectrum values this pass reads: B consecutive columns are B
-// consecutive x at one y.
+// Inverse FFT along z (contiguous) for B consecutive columns of the [y][x][z]
+// volume; planes outside the cap band are zero and are not read.  Each lane
+// loads and stores its elements directly (lane-minor order is contiguous in
+// z).  The OTF mask (Re != 0 after normalisation, main.cpp:262-267) is taken
+// from the spectrum values loaded here: B consecutive columns are B
+// consecutive x at one y, written as one 16-byte row per plane.
 template <int D>
-__global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
+__global__ void __launch_bounds__(PassCfg<D>::NT)
 k_zpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int band, uint8_t* __restrict__ otf) {
     using C = PassCfg<D>;
-    constexpr int B = C::B, NT = B * C::T;
+    using W = typename C::W;
+    constexpr int B = C::B, T = W::T, E = W::E;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    uint8_t* flags = reinterpret_cast<uint8_t*>(sm + B * W::STRIDE);  // D x B
+    const int t = threadIdx.x / T, j = threadIdx.x % T;
     const size_t c0 = (size_t)blockIdx.x * B;
+    float2* col = vol + (c0 + t) * D;
+    float2 x[E];
 #pragma unroll
-    for (int r = 0; r < B * D / NT; ++r) {
-        const int i = threadIdx.x + r * NT, t = i / D, Z = i % D;
-        float2 v = make_float2(0.f, 0.f);
-        if (Z >= zmin && Z < zmin + band) v = vol[(c0 + t) * D + Z];
-        sm[t * tstride(D) + pad_idx(Z)] = v;
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int Z = j + n1 * T;
+        x[n1] = (Z >= zmin && Z < zmin + band) ? col[Z] : make_float2(0.f, 0.f);
+        if (otf) flags[Z * B + t] = x[n1].x != 0.0f ? 1 : 0;
     }
-    __syncthreads();
-    if (otf) {  // reads only; the first FFT stage writes after its own barrier
+    fft_warp_regs<D, +1>(x, sm + t * W::STRIDE, j, tw);
 #pragma unroll
-        for (int r = 0; r < B * D / NT; ++r) {
-            const int i = threadIdx.x + r * NT, t = i % B, Z = i / B;
-            const size_t c = c0 + t;  // y * D + x
-            otf[(size_t)Z * D * D + c] = sm[t * tstride(D) + pad_idx(Z)].x != 0.0f ? 1 : 0;
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) col[j + q * T + E * k2] = x[q * T + k2];
+    }
+    if (otf) {
+        __syncthreads();
+        uint8_t* o = otf + c0;
+        const size_t plane = (size_t)D * D;
+        if ((reinterpret_cast<uintptr_t>(otf) & 15) == 0) {
+            for (int Z = threadIdx.x; Z < D; Z += C::NT)
+                *reinterpret_cast<uint4*>(o + Z * plane) = *reinterpret_cast<const uint4*>(flags + Z * B);
+        } else {
+            for (int i = threadIdx.x; i < D * B; i += C::NT) o[(i / B) * plane + i % B] = flags[i];
         }
     }
-    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
-#pragma unroll
-    for (int r = 0; r < B * D / NT; ++r) {
-        const int i = threadIdx.x + r * NT, t = i / D, Z = i % D;
-        vol[(c0 + t) * D + Z] = sm[t * tstride(D) + pad_idx(Z)];
-    }
 }
 
-// inverse FFT along y, in place, for B consecutive z at fixed x
+// Inverse FFT along y, in place, for B consecutive z at fixed x.
 template <int D>
-__global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
+__global__ void __launch_bounds__(PassCfg<D>::NT)
 k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
     using C = PassCfg<D>;
-    constexpr int B = C::B, NT = B * C::T;
+    using W = typename C::W;
+    constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int z0 = blockIdx.x * B, X = blockIdx.y;
-#pragma unroll
+#pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, Y = i / B;
-        sm[t * tstride(D) + pad_idx(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
+        sm[t * W::STRIDE + W::pad(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
     }
     __syncthreads();
-    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
-#pragma unroll
+    fft_warp<D, +1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
+#pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, Y = i / B;
-        vol[((size_t)Y * D + X) * D + z0 + t] = sm[t * tstride(D) + pad_idx(Y)];
+        vol[((size_t)Y * D + X) * D + z0 + t] = sm[t * W::STRIDE + W::pad(Y)];
     }
 }
 
-// inverse FFT along x for B consecutive z at fixed y, scaled and sign-modulated,
+// Inverse FFT along x for B consecutive z at fixed y, scaled and sign-modulated,
 // written as the index (real) and absorption (imaginary) volumes, x fastest.
 template <int D>
-__global__ void __launch_bounds__(PassCfg<D>::B * (D / 8))
+__global__ void __launch_bounds__(PassCfg<D>::NT)
 k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float scale, float* __restrict__ re,
         float* __restrict__ im) {
     using C = PassCfg<D>;
-    constexpr int B = C::B, NT = B * C::T;
+    using W = typename C::W;
+    constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / C::T, j = threadIdx.x % C::T;
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int z0 = blockIdx.x * B, Y = blockIdx.y;
-#pragma unroll
+#pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, X = i / B;
-        sm[t * tstride(D) + pad_idx(X)] = vol[((size_t)Y * D + X) * D + z0 + t];
+        sm[t * W::STRIDE + W::pad(X)] = vol[((size_t)Y * D + X) * D + z0 + t];
     }
     __syncthreads();
-    fft_smem<D, +1>(sm + tr * tstride(D), j, tw);
+    fft_warp<D, +1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
     const int par = (3 * (D / 2)) & 1;
-#pragma unroll
+#pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i / D, X = i % D, Z = z0 + t;
-        const float2 v = sm[t * tstride(D) + pad_idx(X)];
+        const float2 v = sm[t * W::STRIDE + W::pad(X)];
         const float sg = ((X + Y + Z + par) & 1) ? -scale : scale;
         const size_t o = ((size_t)Z * D + Y) * D + X;
         if (re) re[o] = v.x * sg;
@@ -308,8 +327,7 @@ template <int F>
 int cap_impl(tdm_ctx* c, int n) {
     using C = CapCfg<F>;
     Buffers& b = c->b;
-    const size_t sm = (size_t)C::B * tstride(F) * sizeof(float2);
-    if (allow_smem(k_cap_rows<F>, sm) || allow_smem(k_cap_cols<F>, sm)) return TDM_ECUDA;
+    if (allow_smem(k_cap_rows<F>, C::SMEM) || allow_smem(k_cap_cols<F>, C::SMEM)) return TDM_ECUDA;
     {
         Launch l(c, K_FZM0);
         k_fzm0<<<(n + 255) / 256, 256, 0, c->stream>>>(b.posspec, n, c->p.N, c->p.rayon, b.fzm0);
@@ -319,11 +337,11 @@ int cap_impl(tdm_ctx* c, int n) {
         const int m = n - g0 < c->chunk ? n - g0 : c->chunk;
         {
             Launch l(c, K_CAP_ROWS);
-            k_cap_rows<F><<<dim3(F / C::B, m), C::B * C::T, sm, c->stream>>>(b.fields + g0 * FF, b.tuk_f, b.tw, b.r1);
+            k_cap_rows<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(b.fields + g0 * FF, b.tuk_f, b.tw, b.r1);
         }
         {
             Launch l(c, K_CAP_COLS);
-            k_cap_cols<F><<<dim3(F / C::B, m), C::B * C::T, sm, c->stream>>>(
+            k_cap_cols<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(
                 b.r1, b.posspec + g0, b.fzm0 + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec + g0 * FF, b.err);
         }
     }
@@ -337,9 +355,9 @@ int volume_impl(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t*
     const Params& p = c->p;
     const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
                         (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
-    const size_t sm_p = (size_t)P::B * tstride(D) * sizeof(float2);
+    const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
-    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_p) || allow_smem(k_ypass<D>, sm_p) ||
+    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
     if (cnt) {  // planes outside the cap band carry no hits
@@ -355,15 +373,15 @@ int volume_impl(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t*
     cudaEventRecord(c->ev_stage[5], c->stream);
     {
         Launch l(c, K_ZPASS);
-        k_zpass<D><<<dim3(D * D / P::B), P::B * P::T, sm_p, c->stream>>>(b.vol, b.tw, p.zmin, p.band, otf);
+        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, c->stream>>>(b.vol, b.tw, p.zmin, p.band, otf);
     }
     {
         Launch l(c, K_YPASS);
-        k_ypass<D><<<dim3(D / P::B, D), P::B * P::T, sm_p, c->stream>>>(b.vol, b.tw);
+        k_ypass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
     }
     {
         Launch l(c, K_XPASS);
-        k_xpass<D><<<dim3(D / P::B, D), P::B * P::T, sm_p, c->stream>>>(b.vol, b.tw, p.out_scale, re, im);
+        k_xpass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw, p.out_scale, re, im);
     }
     cudaEventRecord(c->ev_stage[6], c->stream);
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;

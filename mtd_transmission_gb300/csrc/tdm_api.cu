@@ -309,7 +309,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk, L = p.L;
     c->holo_chunk = 16;
-    TRY(dev_alloc(c, &b.tw, kTwN));
+    TRY(dev_alloc(c, &b.tw, kTwTotal));
     TRY(dev_alloc(c, &b.tuk_h, p.H));
     TRY(dev_alloc(c, &b.tuk_f, F));
     TRY(dev_alloc(c, &b.s_tab, FF));
@@ -336,15 +336,11 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
     TRY(dev_alloc(c, &b.err, 4));
     // tables
-    std::vector<float2> tw(kTwN);
-    for (int k = 0; k < kTwN; ++k) {
-        const long double a = -2.0L * 3.14159265358979323846264338327950288L * k / kTwN;
-        tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
+    const std::vector<float2> tw = twiddle_table();
     std::vector<double> th = tukey_factor(p.H, 0.05f), tf = tukey_factor(F, 0.1f);
     std::vector<float> thf(th.begin(), th.end()), tff(tf.begin(), tf.end());
     std::vector<float> stabf(stab.begin(), stab.end());
-    if (cudaMemcpy(b.tw, tw.data(), kTwN * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+    if (cudaMemcpy(b.tw, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.tuk_h, thf.data(), p.H * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.tuk_f, tff.data(), F * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tab, stab.data(), FF * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||

@@ -29,13 +29,13 @@ struct Params {
 
 // Device buffers (all owned by the context).
 struct Buffers {
-    float2* tw = nullptr;          // kTwN twiddles
+    float2* tw = nullptr;          // kTwTotal twiddles (twiddle_table)
     float* tuk_h = nullptr;        // H, hologram Tukey alpha 0.05 (1D factor)
     float* tuk_f = nullptr;        // F, field Tukey alpha 0.1 (1D factor)
     double* s_tab = nullptr;       // F*F, sqrt(rayon^2 - fd^2) at [fdy+N][fdx+N]
     float* s_tabf = nullptr;       // float copy
     uint8_t* holo_stage = nullptr; // host staging: 2 x chunk x H*H*2 bytes
-    float2* inter = nullptr;       // chunk x H x F (extraction row pass)
+    float2* inter = nullptr;       // chunk x F x H (extraction row pass, kx band column-major)
     float2* spectra = nullptr;     // max_angles x F*F
     int2* posspec = nullptr;       // max_angles
     float2* specval = nullptr;     // max_angles

@@ -26,7 +26,7 @@ constexpr int kMaxH = 2048;
 constexpr int kTukeyLen = 256 + 512 + 1024 + 2048;  // one table per supported CCD_ROIX
 
 static __device__ __align__(256) float2 g_scratch[kScratchBytes / sizeof(float2)];
-static __device__ __align__(256) float2 g_twiddle[kTwN];
+static __device__ __align__(256) float2 g_twiddle[kTwTotal];
 static __device__ __align__(256) float g_tukey[kTukeyLen];
 
 int tukey_offset(int H) { return H - 256; }  // 256 -> 0, 512 -> 256, 1024 -> 768, 2048 -> 1792
@@ -55,17 +55,13 @@ int device_symbols(int dev, Symbols& out) {
             cudaGetLastError();
             return TDM_ECUDA;
         }
-        std::vector<float2> tw(kTwN);
-        for (int k = 0; k < kTwN; ++k) {
-            const long double a = -2.0L * 3.14159265358979323846264338327950288L * k / kTwN;
-            tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
-        }
+        const std::vector<float2> tw = twiddle_table();
         std::vector<float> tk(kTukeyLen);
         for (int H = 256; H <= kMaxH; H *= 2) {
             const std::vector<double> t = tukey_factor(H, 0.05f);  // hologram window, main.cpp:105
             for (int i = 0; i < H; ++i) tk[tukey_offset(H) + i] = (float)t[i];
         }
-        if (cudaMemcpy(s.twiddle, tw.data(), kTwN * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+        if (cudaMemcpy(s.twiddle, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(s.tukey, tk.data(), kTukeyLen * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
             cudaGetLastError();
             return TDM_ECUDA;
@@ -89,8 +85,7 @@ template <int H>
 int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F, int x0, int y0,
         cudaStream_t st) {
     using C = ExtractCfg<H>;
-    const size_t sm_rows = (size_t)C::PAIRS * tstride(H) * sizeof(float2);
-    const size_t sm_cols = (size_t)C::COLS * tstride(H) * sizeof(float2);
+    const size_t sm_rows = C::smem_rows(F), sm_cols = C::smem_cols(F);
     if (sm_rows > 48 * 1024 &&
         cudaFuncSetAttribute(k_extract_rows<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
         return TDM_ECUDA;
@@ -102,10 +97,10 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
     const size_t in_bytes = (size_t)H * H * (bits == 16 ? 2 : 1);
     for (int h0 = 0; h0 < n; h0 += chunk) {
         const int m = n - h0 < chunk ? n - h0 : chunk;
-        k_extract_rows<H><<<dim3(H / 2 / C::PAIRS, m), C::PAIRS * C::T, sm_rows, st>>>(
+        k_extract_rows<H><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
             static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), s.twiddle, s.scratch, F,
             x0);
-        k_extract_cols<H><<<dim3(F / C::COLS, m), C::COLS * C::T, sm_cols, st>>>(
+        k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
             s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0);
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
