@@ -172,6 +172,30 @@ struct WarpFFT {
     __host__ __device__ static constexpr int pad(int i) { return i + (i >> LOG_T); }
 };
 
+// x[k1] *= W_N^(DIR j k1), k1 = 1 .. E-1, from the [k1][j] table.  The loads
+// are issued in groups of 8 behind a compiler barrier so that they do not all
+// become live at once (E - 1 twiddles would otherwise double the registers).
+template <int N, int DIR>
+__device__ __forceinline__ void twiddle_lane(float2 (&x)[WarpFFT<N>::E], const float2* __restrict__ twr, int j) {
+    using W = WarpFFT<N>;
+    constexpr int E = W::E, T = W::T;
+#pragma unroll
+    for (int g = 0; g < E; g += 8) {
+        float2 w[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (g + i > 0) w[i] = __ldg(&twr[(g + i) * T + j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (g + i > 0) {
+                if constexpr (DIR > 0) w[i].y = -w[i].y;
+                x[g + i] = c_mul(x[g + i], w[i]);
+            }
+        }
+        asm volatile("" ::: "memory");
+    }
+}
+
 // Register form.  On entry x[n1] holds element j + T n1 of the transform; on
 // return x[q T + k2] holds element (j + q T) + E k2.  s is the transform's
 // padded shared-memory array (WarpFFT<N>::LEN slots), used for the exchange.
@@ -183,12 +207,7 @@ __device__ __forceinline__ void fft_warp_regs(float2 (&x)[WarpFFT<N>::E], float2
     constexpr int E = W::E, T = W::T;
     const float2* twr = tw + twr_offset(N);
     dft<E, DIR>(x);
-#pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) {
-        float2 w = __ldg(&twr[k1 * T + j]);
-        if constexpr (DIR > 0) w.y = -w.y;
-        x[k1] = c_mul(x[k1], w);
-    }
+    twiddle_lane<N, DIR>(x, twr, j);
     __syncwarp();  // earlier readers of s are done
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) s[k1 * (T + 1) + j] = x[k1];  // pad(k1 T + j)
@@ -228,12 +247,7 @@ __device__ __forceinline__ void fft_warp_regs_rev(float2 (&x)[WarpFFT<N>::E], fl
     __syncwarp();
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) x[k1] = s[k1 * (T + 1) + j];
-#pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) {
-        float2 w = __ldg(&twr[k1 * T + j]);
-        if constexpr (DIR > 0) w.y = -w.y;
-        x[k1] = c_mul(x[k1], w);
-    }
+    twiddle_lane<N, DIR>(x, twr, j);
     dft<E, DIR>(x);
 }
 
@@ -278,6 +292,31 @@ __device__ __forceinline__ void fft_warp(float2* s, int j, const float2* __restr
 #pragma unroll
         for (int k2 = 0; k2 < T; ++k2) s[warp_out_pos<N>(j, q, k2)] = x[q * T + k2];
     }
+}
+
+// Out-of-line copy of fft_warp: one body per (N, DIR) however many call
+// sites a kernel has, which bounds the code size and the register count of
+// kernels that chain several transforms.
+template <int N, int DIR>
+__device__ __noinline__ void fft_warp_call(float2* s, int j, const float2* __restrict__ tw) {
+    fft_warp<N, DIR>(s, j, tw);
+}
+
+// Shared-memory filter on the out-of-line transforms: s (natural order) is
+// replaced by FFT_{-DIR}(mul(k, FFT_DIR(s)[k])), unnormalised.
+template <int N, int DIR, class Mul>
+__device__ __forceinline__ void fft_warp_filter_call(float2* s, int j, const float2* __restrict__ tw, Mul&& mul) {
+    using W = WarpFFT<N>;
+    constexpr int E = W::E, T = W::T;
+    fft_warp_call<N, DIR>(s, j, tw);
+    __syncwarp();
+#pragma unroll 8
+    for (int n1 = 0; n1 < E; ++n1) {
+        float2* p = &s[j + n1 * (T + 1)];  // pad(j + T n1)
+        *p = mul(j + n1 * T, *p);
+    }
+    __syncwarp();
+    fft_warp_call<N, -DIR>(s, j, tw);
 }
 
 }  // namespace tdm

@@ -129,7 +129,7 @@ k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspe
 template <int F>
 __global__ void __launch_bounds__(FieldCfg<F>::NT)
 k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ tw, float* __restrict__ phase,
-             float* __restrict__ amp, float2* __restrict__ fields) {
+             float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields) {
     using C = FieldCfg<F>;
     using W = typename C::W;
     constexpr int B = C::B, NT = C::NT;
@@ -151,8 +151,11 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
         const int yo = (y + F / 2) & (F - 1), xo = (x0 + t + F / 2) & (F - 1);
         const size_t o = ((size_t)a * F + yo) * F + xo;
         if (mode) {
+            const float m = hypotf(u.x, u.y);
             phase[o] = atan2f(u.y, u.x);
-            amp[o] = hypotf(u.x, u.y);
+            amp[o] = m;
+            // exp(i phase) without the round trip through the angle; atan2(0, 0) = 0
+            zph[o] = m > 0.0f ? make_float2(u.x / m, u.y / m) : make_float2(1.0f, 0.0f);
         } else {
             fields[o] = u;
         }
@@ -189,7 +192,8 @@ struct VCfg {
 // gx[Y][X] = sign(X) gxh[m(Y)][m(X)].
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT)
-k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, float* __restrict__ gxh) {
+k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ tw,
+              float* __restrict__ gxh) {
     using C = VCfg<L>;
     using W = typename C::W;
     constexpr int F = L / 2, T = W::T, E = W::E, P = C::P;
@@ -200,38 +204,30 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, fl
     const int a = blockIdx.y;
     const int ya = blockIdx.x * 2 * P + 2 * pair, yb = ya + 1;
     float2* s = sm + tr * W::STRIDE;
-    const float* pa = phase + ((size_t)a * F + ya) * F;
-    const float* pb = phase + ((size_t)a * F + yb) * F;
-    float2 x[E];
-#pragma unroll
-    for (int n1 = 0; n1 < E; ++n1) {
-        const int mx = mirror(j + n1 * T, F);
-        if (zk) {
-            float sn, cs;
-            sincosf((ab ? pb : pa)[mx], &sn, &cs);
-            x[n1] = make_float2(cs, sn);
-        } else {
-            x[n1] = make_float2(pa[mx], pb[mx]);
+    const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
+    const float2* zr = zph + (ab ? rb : ra);
+    if (zk) {
+#pragma unroll 8
+        for (int n1 = 0; n1 < E; ++n1) s[j + n1 * (T + 1)] = zr[mirror(j + n1 * T, F)];
+    } else {
+#pragma unroll 8
+        for (int n1 = 0; n1 < E; ++n1) {
+            const int mx = mirror(j + n1 * T, F);
+            s[j + n1 * (T + 1)] = make_float2(phase[ra + mx], phase[rb + mx]);
         }
     }
-    fft_warp_filter<L, -1>(x, s, j, tw, DerivMul<L>{});
-    if (!zk) {  // dphi/dx of both rows, right half X >= F (n1 >= E/2)
-        __syncwarp();
-#pragma unroll
-        for (int n1 = E / 2; n1 < E; ++n1) s[j + n1 * (T + 1)] = x[n1];
-    }
+    __syncwarp();
+    fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
     __syncthreads();
     if (zk) {
         const float2* sp = sm + (2 * P + pair) * W::STRIDE;
-        const float* pr = ab ? pb : pa;
-        float* out = gxh + ((size_t)a * F + (ab ? yb : ya)) * F;
+        float* out = gxh + (ab ? rb : ra);
 #pragma unroll
         for (int n1 = E / 2; n1 < E; ++n1) {
             const int X = j + n1 * T;
-            float sn, cs;
-            sincosf(pr[X - F], &sn, &cs);  // mirror(X) = X - F on the right half
-            const float2 g = x[n1];
-            const float ax = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);  // Re(-i g / Z)
+            const float2 z = zr[X - F];  // mirror(X) = X - F on the right half
+            const float2 g = s[j + n1 * (T + 1)];
+            const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
             const float2 q = sp[j + n1 * (T + 1)];
             out[X - F] = (ax - (ab ? q.y : q.x)) * kInvTwoPi;
         }
@@ -244,14 +240,14 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ tw, fl
 // pass 3.
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT)
-k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, const float2* __restrict__ tw,
-              float2* __restrict__ qc) {
+k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
+              const float2* __restrict__ tw, float2* __restrict__ qc) {
     using C = VCfg<L>;
     using W = typename C::W;
     constexpr int F = L / 2, T = W::T, E = W::E, P = C::P, NC = 2 * P, NT = C::NT, LS = L + 1;
     extern __shared__ float2 sm[];
-    float* sph = reinterpret_cast<float*>(sm + C::B * W::STRIDE);  // NC x LS phase along the mirror column
-    float* sgx = sph + NC * LS;                                    // NC x LS gx along the mirror column
+    float2* szp = sm + C::B * W::STRIDE;                        // NC x LS exp(i phase) along the mirror column
+    float* sgx = reinterpret_cast<float*>(szp + NC * LS);       // NC x LS gx along the mirror column
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const bool zk = tr < NC;
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
@@ -259,46 +255,30 @@ k_volkov_cols(const float* __restrict__ phase, const float* __restrict__ gxh, co
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, Y = i / NC;
         const size_t src = ((size_t)a * F + mirror(Y, F)) * F + x0 + c;
-        const float v = phase[src];
-        sph[c * LS + Y] = v;
+        const float2 z = zph[src];
+        szp[c * LS + Y] = z;
         sgx[c * LS + Y] = gxh[src];
-        float sn, cs;
-        sincosf(v, &sn, &cs);
-        sm[c * W::STRIDE + W::pad(Y)] = make_float2(cs, sn);
-        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * W::STRIDE + W::pad(Y)])[c & 1] = v;
+        sm[c * W::STRIDE + W::pad(Y)] = z;
+        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * W::STRIDE + W::pad(Y)])[c & 1] = phase[src];
     }
     __syncthreads();
     float2* s = sm + tr * W::STRIDE;
-    float2 x[E];
-#pragma unroll
-    for (int n1 = 0; n1 < E; ++n1) x[n1] = s[j + n1 * (T + 1)];
-    fft_warp_filter<L, -1>(x, s, j, tw, DerivMul<L>{});
-    if (!zk) {
-        __syncwarp();
-#pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) s[j + n1 * (T + 1)] = x[n1];
-    }
+    fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
     __syncthreads();
     if (zk) {  // warp-uniform
         const int c = tr;
         const float2* sp = sm + (NC + (c >> 1)) * W::STRIDE;
-#pragma unroll
+#pragma unroll 8
         for (int n1 = 0; n1 < E; ++n1) {
             const int Y = j + n1 * T;
-            float sn, cs;
-            sincosf(sph[c * LS + Y], &sn, &cs);
-            const float2 g = x[n1];
-            const float ay = (g.y * cs - g.x * sn) / (cs * cs + sn * sn);
+            const float2 z = szp[c * LS + Y];
+            const float2 g = s[j + n1 * (T + 1)];
+            const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
             const float2 q = sp[j + n1 * (T + 1)];
-            x[n1] = make_float2(sgx[c * LS + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
+            s[j + n1 * (T + 1)] = make_float2(sgx[c * LS + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
         }
-        fft_warp_regs<L, -1>(x, s, j, tw);
         __syncwarp();
-#pragma unroll
-        for (int q = 0; q < E / T; ++q) {
-#pragma unroll
-            for (int k2 = 0; k2 < T; ++k2) s[warp_out_pos<L>(j, q, k2)] = x[q * T + k2];
-        }
+        fft_warp_call<L, -1>(s, j, tw);
     }
     __syncthreads();
 #pragma unroll 4
@@ -521,7 +501,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
     const size_t sm_vrows = (size_t)VC::B * VC::W::STRIDE * sizeof(float2);
-    const size_t sm_vcols = sm_vrows + (size_t)2 * 2 * VC::P * (L + 1) * sizeof(float);
+    const size_t sm_vcols = sm_vrows + (size_t)2 * VC::P * (L + 1) * (sizeof(float2) + sizeof(float));
     if (allow_smem(k_field_rows<F>, FC::SMEM) || allow_smem(k_field_cols<F>, FC::SMEM) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
         allow_smem(k_volkov_integ_rows<L>, IC::SMEM) || allow_smem(k_volkov_integ_cols<L>, IC::SMEM))
@@ -541,19 +521,19 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         {
             Launch l(c, K_FIELD_COLS);
             k_field_cols<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
-                b.I1, p.c_aber, b.tw, b.phase, b.amp, b.fields + (size_t)g0 * FF);
+                b.I1, p.c_aber, b.tw, b.phase, b.amp, b.zph, b.fields + (size_t)g0 * FF);
         }
         if (!p.c_aber) continue;
         const float* unw = b.phase;
         if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                k_volkov_rows<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vrows, c->stream>>>(b.phase, b.tw,
+                k_volkov_rows<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vrows, c->stream>>>(b.phase, b.zph, b.tw,
                                                                                                      b.gx);
             }
             {
                 Launch l(c, K_VOLKOV_COLS);
-                k_volkov_cols<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vcols, c->stream>>>(b.phase, b.gx,
+                k_volkov_cols<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vcols, c->stream>>>(b.phase, b.zph, b.gx,
                                                                                                      b.tw, b.qc);
             }
             {

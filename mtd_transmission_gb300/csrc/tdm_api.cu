@@ -78,7 +78,7 @@ int dev_alloc(tdm_ctx* c, T** p, size_t count) {
 void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
-                    b.specval, b.fzm0, b.I1, b.phase, b.amp, b.gx, b.qc, b.tq, b.unwrapped, b.beta, b.fields,
+                    b.specval, b.fzm0, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta, b.fields,
                     b.r1, b.rec, b.fit_part, b.vol, b.out_re, b.out_im, b.out_otf, b.out_cnt,
                     b.samp_idx, b.samp_q, b.rinv, b.err};
     for (void* p : ptrs)
@@ -323,6 +323,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.I1, CH * FF));
     TRY(dev_alloc(c, &b.phase, CH * FF));
     TRY(dev_alloc(c, &b.amp, CH * FF));
+    TRY(dev_alloc(c, &b.zph, CH * FF));
     TRY(dev_alloc(c, &b.gx, CH * FF));
     TRY(dev_alloc(c, &b.qc, CH * L * F));
     TRY(dev_alloc(c, &b.tq, CH * L * F));

@@ -43,6 +43,7 @@ struct Buffers {
     float2* I1 = nullptr;          // chunk x F*F
     float* phase = nullptr;        // chunk x F*F
     float* amp = nullptr;          // chunk x F*F
+    float2* zph = nullptr;         // chunk x F*F unit phasor exp(i phase) (Volkov input)
     float* gx = nullptr;           // chunk x F*F (right half of the mirror's gx, per image row)
     float2* qc = nullptr;          // chunk x L*F (FFT along y of Q, columns X >= F)
     float2* tq = nullptr;          // chunk x L*F
