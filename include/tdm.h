@@ -156,7 +156,9 @@ void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */
 uint64_t tdm_launch_count(const tdm_ctx* ctx); /* kernels launched so far */
 /* Device-side elapsed time of the last tdm_* call's dominant kernel group
  * (milliseconds per stage) for profiling: names are "extract", "fields",
- * "map", "volume"; returns a negative value for an unknown name. */
+ * "map", "volume"; returns a negative value for an unknown name.  After
+ * tdm_pipeline, which streams extraction, fields and cap mapping chunk by
+ * chunk, "extract" covers all three and "fields" and "map" read 0. */
 double tdm_stage_ms(const tdm_ctx* ctx, const char* stage);
 
 /* Opt-in per-kernel timing: when enabled, every kernel launch is bracketed by

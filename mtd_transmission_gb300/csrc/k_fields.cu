@@ -38,45 +38,63 @@ __device__ __forceinline__ float kappa(int k, int L) {  // init_kvect_shift, FFT
 __device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F - 1 - X; }
 
 // ---------------------------------------------------------------- argmax
-__global__ void __launch_bounds__(1024) k_argmax(const float2* __restrict__ spectra, int F, int2* __restrict__ posspec,
-                                                 float2* __restrict__ specval) {
-    const int a = blockIdx.x;
+// coordSpec (fonctions.cpp:88-101): |z|^2 at index 0, |z| elsewhere, first
+// maximum in row-major order wins.  k_argmax_part reduces kArgSlices slices of
+// each spectrum; k_field_rows, the first consumer, reduces the slices' winners.
+constexpr int kArgSlices = 32;
+
+__device__ __forceinline__ void argmax_merge(float& best, int& bi, float ob, int oi) {
+    if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+    }
+}
+
+__device__ __forceinline__ void argmax_warp(float& best, int& bi) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+        argmax_merge(best, bi, __shfl_down_sync(0xffffffffu, best, off), __shfl_down_sync(0xffffffffu, bi, off));
+}
+
+__global__ void __launch_bounds__(256) k_argmax_part(const float2* __restrict__ spectra, int F,
+                                                     float2* __restrict__ part) {
+    const int a = blockIdx.y, sl = blockIdx.x;
+    const int per = F * F / kArgSlices, i0 = sl * per;
     const float2* s = spectra + (size_t)a * F * F;
     float best = -1.0f;
     int bi = 0x7fffffff;
-    for (int i = threadIdx.x; i < F * F; i += blockDim.x) {
+    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) {
         const float2 z = s[i];
         const float sq = z.x * z.x + z.y * z.y;
         const float m = (i == 0) ? sq : sqrtf(sq);
         if (m > best) { best = m; bi = i; }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float ob = __shfl_down_sync(0xffffffffu, best, off);
-        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    __shared__ float sb[32];
-    __shared__ int si[32];
+    argmax_warp(best, bi);
+    __shared__ float sb[8];
+    __shared__ int si[8];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) { sb[w] = best; si[w] = bi; }
     __syncthreads();
     if (w == 0) {
-        const int nw = blockDim.x >> 5;
-        best = l < nw ? sb[l] : -1.0f;
-        bi = l < nw ? si[l] : 0x7fffffff;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ob = __shfl_down_sync(0xffffffffu, best, off);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (l == 0) {
-            if (bi == 0x7fffffff) bi = 0;  // all NaN: the reference keeps index 0
-            posspec[a] = make_int2(bi % F, bi / F);
-            specval[a] = s[bi];
-        }
+        best = l < 8 ? sb[l] : -1.0f;
+        bi = l < 8 ? si[l] : 0x7fffffff;
+        argmax_warp(best, bi);
+        if (l == 0) part[(size_t)a * kArgSlices + sl] = make_float2(best, __int_as_float(bi));
     }
+}
+
+// Winner over the slices of angle a, read by every warp of the caller (lane i
+// takes slice i; the result is broadcast to all lanes).
+__device__ __forceinline__ int argmax_final(const float2* __restrict__ part, int a) {
+    static_assert(kArgSlices == 32, "one slice per lane");
+    const float2 q = part[(size_t)a * kArgSlices + (threadIdx.x & 31)];
+    float best = q.x;
+    int bi = __float_as_int(q.y);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, off), __shfl_xor_sync(0xffffffffu, bi, off));
+    }
+    return bi == 0x7fffffff ? 0 : bi;  // all NaN: the reference keeps index 0
 }
 
 // ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
@@ -94,18 +112,24 @@ struct FieldCfg {
 
 template <int F>
 __global__ void __launch_bounds__(FieldCfg<F>::NT)
-k_field_rows(const float2* __restrict__ spectra, const int2* __restrict__ posspec, const float2* __restrict__ specval,
-             int normalize, const float2* __restrict__ tw, float2* __restrict__ I1) {
+k_field_rows(const float2* __restrict__ spectra, const float2* __restrict__ argpart, int2* __restrict__ posspec,
+             float2* __restrict__ specval, int normalize, const float2* __restrict__ tw, float2* __restrict__ I1) {
     using C = FieldCfg<F>;
     using W = typename C::W;
     constexpr int T = W::T, E = W::E;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
-    const int2 p = posspec[a];
+    const int bi = argmax_final(argpart, a);
+    const int2 p = make_int2(bi % F, bi / F);
+    const float2* spec = spectra + (size_t)a * F * F;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        posspec[a] = p;
+        specval[a] = spec[bi];
+    }
     float2 nrm = make_float2(1.0f, 0.0f);
     if (normalize) {  // TF_UBorn * conj(spec) / |spec| (main.cpp:332-335)
-        const float2 s0 = specval[a];
+        const float2 s0 = spec[bi];
         const float mod = sqrtf(s0.y * s0.y + s0.x * s0.x);
         nrm = make_float2(s0.x / mod, -s0.y / mod);
     }
@@ -392,63 +416,75 @@ k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ pha
 }
 
 // ---------------------------------------------------------------- aberration fit
-// Partial sums c_k = sum_s q_k(s) b(s) of the least-squares projection of
-// image img (0: unwrapped phase, 1: amplitude) over slice blockIdx.z of the
-// background samples, in FP64.
-__global__ void __launch_bounds__(256) k_aber_partial(const float* __restrict__ unwrapped, const float* __restrict__ amp,
-                                                      const int* __restrict__ samp_idx, const float* __restrict__ samp_q,
-                                                      int nsamp, int F, double* __restrict__ part) {
-    const int a = blockIdx.x, im = blockIdx.y, sl = blockIdx.z;
+// The least-squares projections c_k = sum_s q_k(s) b(s) of image b (0: the
+// unwrapped phase, 1: the amplitude) onto the basis orthonormal over the
+// background samples, then the monomial coefficients beta = Rinv c (scaled
+// coordinates).  kFitSlices CTAs per (angle, image) each sum one slice of the
+// samples in FP32 (per thread, then per warp); the last CTA of the group to
+// finish adds the slices' partial sums in FP64 in slice order and forms beta,
+// so the result does not depend on the CTAs' timing.  With |q_k(s)| of order
+// nsamp^-1/2 the FP32 rounding is a few ulps of |b|.
+constexpr int kFitThreads = 256;
+constexpr int kFitSlices = 8;
+
+__global__ void __launch_bounds__(kFitThreads) k_aber_fit(const float* __restrict__ unwrapped,
+                                                          const float* __restrict__ amp,
+                                                          const int* __restrict__ samp_idx,
+                                                          const float* __restrict__ samp_q, int nsamp, int F,
+                                                          const double* __restrict__ rinv, float* __restrict__ part,
+                                                          unsigned* __restrict__ done, double* __restrict__ beta) {
+    const int sl = blockIdx.x, im = blockIdx.y, a = blockIdx.z, g = a * 2 + im;
     const float* img = (im == 0 ? unwrapped : amp) + (size_t)a * F * F;
     const int per = (nsamp + kFitSlices - 1) / kFitSlices;
     const int s0 = sl * per, s1 = min(nsamp, s0 + per);
-    double acc[kNC];
+    float acc[kNC];
 #pragma unroll
-    for (int k = 0; k < kNC; ++k) acc[k] = 0.0;
-    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-        const double v = (double)img[samp_idx[s]];
+    for (int k = 0; k < kNC; ++k) acc[k] = 0.0f;
+#pragma unroll 2
+    for (int s = s0 + threadIdx.x; s < s1; s += kFitThreads) {
+        const float v = img[samp_idx[s]];
         const float* q = samp_q + (size_t)s * kNC;
 #pragma unroll
-        for (int k = 0; k < kNC; ++k) acc[k] = fma((double)q[k], v, acc[k]);
+        for (int k = 0; k < kNC; ++k) acc[k] = fmaf(q[k], v, acc[k]);
     }
-    __shared__ double red[8][kNC];
+    constexpr int NW = kFitThreads / 32;
+    __shared__ float red[NW][kNC];
+    __shared__ double cf[kNC];
+    __shared__ bool last;
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < kNC; ++k) {
-        double x = acc[k];
+        float x = acc[k];
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
         if (l == 0) red[w][k] = x;
     }
     __syncthreads();
     if (threadIdx.x < kNC) {
-        double x = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) x += red[i][threadIdx.x];
-        part[(((size_t)a * 2 + im) * kFitSlices + sl) * kNC + threadIdx.x] = x;
-    }
-}
-
-// beta[a][img][:] = Rinv * c: monomial coefficients (scaled coordinates) of
-// the fit, summing the slices in a fixed order.
-__global__ void k_aber_reduce(const double* __restrict__ part, const double* __restrict__ rinv,
-                              double* __restrict__ beta) {
-    const int a = blockIdx.x;
-    __shared__ double cf[2][kNC];
-    const int t = threadIdx.x;
-    if (t < 2 * kNC) {
-        const int im = t / kNC, k = t % kNC;
-        double x = 0.0;
-        for (int sl = 0; sl < kFitSlices; ++sl) x += part[(((size_t)a * 2 + im) * kFitSlices + sl) * kNC + k];
-        cf[im][k] = x;
+        float x = 0.0f;
+        for (int i = 0; i < NW; ++i) x += red[i][threadIdx.x];
+        part[((size_t)g * kFitSlices + sl) * kNC + threadIdx.x] = x;
+        __threadfence();
     }
     __syncthreads();
-    if (t < 2 * kNC) {
-        const int im = t / kNC, k = t % kNC;
+    if (threadIdx.x == 0) last = atomicAdd(&done[g], 1u) == kFitSlices - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < kNC) {
+        double x = 0.0;
+        for (int i = 0; i < kFitSlices; ++i) x += (double)__ldcg(&part[((size_t)g * kFitSlices + i) * kNC + threadIdx.x]);
+        cf[threadIdx.x] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNC) {
+        const int k = threadIdx.x;
         double x = 0.0;
 #pragma unroll
-        for (int i = 0; i < kNC; ++i) x = fma(rinv[k * kNC + i], cf[im][i], x);
-        beta[((size_t)a * 2 + im) * kNC + k] = x;
+        for (int i = 0; i < kNC; ++i) x = fma(rinv[k * kNC + i], cf[i], x);
+        beta[(size_t)g * kNC + k] = x;
     }
+    if (threadIdx.x == 0) done[g] = 0;  // ready for the next chunk
 }
 
 // Evaluates the fits, corrects phase and amplitude and forms the Born or Rytov field.
@@ -506,17 +542,17 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
         allow_smem(k_volkov_integ_rows<L>, IC::SMEM) || allow_smem(k_volkov_integ_cols<L>, IC::SMEM))
         return TDM_ECUDA;
-    {
-        Launch l(c, K_ARGMAX);
-        k_argmax<<<n, 1024, 0, c->stream>>>(b.spectra + (size_t)a0 * FF, F, b.posspec + a0, b.specval + a0);
-    }
     for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
         const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
         const float2* spec = b.spectra + (size_t)g0 * FF;
         {
+            Launch l(c, K_ARGMAX);
+            k_argmax_part<<<dim3(kArgSlices, m), 256, 0, c->stream>>>(spec, F, b.argpart);
+        }
+        {
             Launch l(c, K_FIELD_ROWS);
             k_field_rows<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
-                spec, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
+                spec, b.argpart, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
         }
         {
             Launch l(c, K_FIELD_COLS);
@@ -550,12 +586,8 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         }
         {
             Launch l(c, K_ABER_FIT);
-            k_aber_partial<<<dim3(m, 2, kFitSlices), 256, 0, c->stream>>>(unw, b.amp, b.samp_idx, b.samp_q, c->nsamp,
-                                                                          F, b.fit_part);
-        }
-        {
-            Launch l(c, K_ABER_REDUCE);
-            k_aber_reduce<<<m, 32, 0, c->stream>>>(b.fit_part, b.rinv, b.beta);
+            k_aber_fit<<<dim3(kFitSlices, 2, m), kFitThreads, 0, c->stream>>>(
+                unw, b.amp, b.samp_idx, b.samp_q, c->nsamp, F, b.rinv, b.fit_part, b.fit_done, b.beta);
         }
         {
             Launch l(c, K_FORM);

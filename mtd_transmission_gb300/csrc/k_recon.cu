@@ -37,15 +37,6 @@ struct CapCfg {
     static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
-// fzm0 per angle (fonctions.cpp:893-899); negative when the angle is skipped.
-__global__ void k_fzm0(const int2* __restrict__ posspec, int n, int N, double rayon, double* __restrict__ fzm0) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    const int fxm0 = posspec[a].x - N, fym0 = posspec[a].y - N;
-    const double c = rayon * rayon - fxm0 * fxm0 - fym0 * fym0;
-    fzm0[a] = (round(c) >= 0) ? sqrt(c) : -1.0;
-}
-
 template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, const float2* __restrict__ tw,
@@ -75,15 +66,22 @@ k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, con
 
 template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
-k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ fzm0,
-           const double* __restrict__ s_tab, const float* __restrict__ s_tabf, Params p,
-           const float2* __restrict__ tw, float4* __restrict__ rec, int* __restrict__ err) {
+k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ s_tab,
+           const float* __restrict__ s_tabf, Params p, const float2* __restrict__ tw, float4* __restrict__ rec,
+           int* __restrict__ err) {
     using C = CapCfg<F>;
     using W = typename C::W;
     constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
+    __shared__ double s_fz;
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, kx0 = blockIdx.x * B;
+    const int2 ps = posspec[a];
+    if (threadIdx.x == 0) {  // fzm0 (fonctions.cpp:893-899); negative when the angle is skipped
+        const int fxm0 = ps.x - p.N, fym0 = ps.y - p.N;
+        const double c = p.rayon * p.rayon - fxm0 * fxm0 - fym0 * fym0;
+        s_fz = (round(c) >= 0) ? sqrt(c) : -1.0;
+    }
 #pragma unroll 8
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
@@ -92,8 +90,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
     __syncthreads();
     fft_warp<F, -1>(sm + tr * W::STRIDE, j, tw);
     __syncthreads();
-    const int2 ps = posspec[a];
-    const double fz = fzm0[a];
+    const double fz = s_fz;
     const float fzf = (float)fz;
     const int N = p.N;
 #pragma unroll 2
@@ -294,14 +291,14 @@ k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
 // written as the index (real) and absorption (imaginary) volumes, x fastest.
 template <int D>
 __global__ void __launch_bounds__(PassCfg<D>::NT)
-k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float scale, float* __restrict__ re,
+k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float scale, int zblock0, float* __restrict__ re,
         float* __restrict__ im) {
     using C = PassCfg<D>;
     using W = typename C::W;
     constexpr int B = C::B, NT = C::NT;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
-    const int z0 = blockIdx.x * B, Y = blockIdx.y;
+    const int z0 = (zblock0 + blockIdx.x) * B, Y = blockIdx.y;
 #pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, X = i / B;
@@ -323,17 +320,13 @@ k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float sca
 }
 
 template <int F>
-int cap_impl(tdm_ctx* c, int n) {
+int cap_impl(tdm_ctx* c, int a0, int n) {
     using C = CapCfg<F>;
     Buffers& b = c->b;
     if (allow_smem(k_cap_rows<F>, C::SMEM) || allow_smem(k_cap_cols<F>, C::SMEM)) return TDM_ECUDA;
-    {
-        Launch l(c, K_FZM0);
-        k_fzm0<<<(n + 255) / 256, 256, 0, c->stream>>>(b.posspec, n, c->p.N, c->p.rayon, b.fzm0);
-    }
     const size_t FF = (size_t)F * F;
-    for (int g0 = 0; g0 < n; g0 += c->chunk) {
-        const int m = n - g0 < c->chunk ? n - g0 : c->chunk;
+    for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
+        const int m = a0 + n - g0 < c->chunk ? a0 + n - g0 : c->chunk;
         {
             Launch l(c, K_CAP_ROWS);
             k_cap_rows<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(b.fields + g0 * FF, b.tuk_f, b.tw, b.r1);
@@ -341,14 +334,27 @@ int cap_impl(tdm_ctx* c, int n) {
         {
             Launch l(c, K_CAP_COLS);
             k_cap_cols<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(
-                b.r1, b.posspec + g0, b.fzm0 + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec + g0 * FF, b.err);
+                b.r1, b.posspec + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec + g0 * FF, b.err);
         }
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
+// Download of bytes from a device buffer to host memory on the copy stream,
+// after the work queued so far on c->stream.
+static cudaError_t download_after(tdm_ctx* c, cudaEvent_t ev, void* host, const void* dev, size_t bytes) {
+    cudaError_t e = cudaEventRecord(ev, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, ev, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->copy_stream);
+    return e;
+}
+
 template <int D>
-int volume_impl(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
+int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
+    float* re = out.re;
+    float* im = out.im;
+    uint8_t* otf = out.otf;
+    uint32_t* cnt = out.cnt;
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
@@ -370,50 +376,75 @@ int volume_impl(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t*
         k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(b.rec, b.posspec, n, p, b.vol, cnt);
     }
     cudaEventRecord(c->ev_stage[5], c->stream);
+    const size_t NT = (size_t)D * D * D;
+    bool downloads = false;
+    if (out.host_cnt) {
+        if (download_after(c, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t))) return TDM_ECUDA;
+        downloads = true;
+    }
     {
         Launch l(c, K_ZPASS);
         k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, c->stream>>>(b.vol, b.tw, p.zmin, p.band, otf);
+    }
+    if (out.host_otf) {
+        if (download_after(c, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT)) return TDM_ECUDA;
+        downloads = true;
     }
     {
         Launch l(c, K_YPASS);
         k_ypass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
     }
-    {
-        Launch l(c, K_XPASS);
-        k_xpass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw, p.out_scale, re, im);
+    // x pass by slabs of z blocks; a slab's planes are final once it has run
+    const bool host_vol = out.host_re || out.host_im;
+    const int zblocks = D / P::B, nslab = host_vol ? (zblocks < kOutSlabs ? zblocks : kOutSlabs) : 1;
+    for (int sl = 0; sl < nslab; ++sl) {
+        const int zb0 = sl * zblocks / nslab, zb1 = (sl + 1) * zblocks / nslab;
+        {
+            Launch l(c, K_XPASS);
+            k_xpass<D><<<dim3(zb1 - zb0, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw, p.out_scale, zb0, re, im);
+        }
+        if (host_vol) {
+            const size_t off = (size_t)zb0 * P::B * D * D, len = (size_t)(zb1 - zb0) * P::B * D * D;
+            if (cudaEventRecord(c->ev_out[sl], c->stream) || cudaStreamWaitEvent(c->copy_stream, c->ev_out[sl], 0))
+                return TDM_ECUDA;
+            if (out.host_re && cudaMemcpyAsync(out.host_re + off, re + off, len * sizeof(float),
+                                               cudaMemcpyDeviceToHost, c->copy_stream))
+                return TDM_ECUDA;
+            if (out.host_im && cudaMemcpyAsync(out.host_im + off, im + off, len * sizeof(float),
+                                               cudaMemcpyDeviceToHost, c->copy_stream))
+                return TDM_ECUDA;
+            downloads = true;
+        }
     }
     cudaEventRecord(c->ev_stage[6], c->stream);
+    if (downloads) {  // later work on c->stream (and its synchronisation) follows the downloads
+        if (cudaEventRecord(c->ev_out[kOutSlabs + 2], c->copy_stream) ||
+            cudaStreamWaitEvent(c->stream, c->ev_out[kOutSlabs + 2], 0))
+            return TDM_ECUDA;
+    }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
 }  // namespace
 
-int launch_cap(tdm_ctx* c, int n) {
+int launch_cap(tdm_ctx* c, int a0, int n) {
     switch (c->p.F) {
-        case 64: return cap_impl<64>(c, n);
-        case 128: return cap_impl<128>(c, n);
-        case 256: return cap_impl<256>(c, n);
-        case 512: return cap_impl<512>(c, n);
+        case 64: return cap_impl<64>(c, a0, n);
+        case 128: return cap_impl<128>(c, a0, n);
+        case 256: return cap_impl<256>(c, a0, n);
+        case 512: return cap_impl<512>(c, a0, n);
         default: return TDM_EUNSUPPORTED;
     }
 }
 
-int launch_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out) {
     switch (c->p.D) {
-        case 128: return volume_impl<128>(c, n, re, im, otf, cnt);
-        case 256: return volume_impl<256>(c, n, re, im, otf, cnt);
-        case 512: return volume_impl<512>(c, n, re, im, otf, cnt);
-        case 1024: return volume_impl<1024>(c, n, re, im, otf, cnt);
+        case 128: return volume_impl<128>(c, n, out);
+        case 256: return volume_impl<256>(c, n, out);
+        case 512: return volume_impl<512>(c, n, out);
+        case 1024: return volume_impl<1024>(c, n, out);
         default: return TDM_EUNSUPPORTED;
     }
-}
-
-int launch_fzm0(tdm_ctx* c, int n) {
-    {
-        Launch l(c, K_FZM0);
-        k_fzm0<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, c->p.N, c->p.rayon, c->b.fzm0);
-    }
-    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
 }  // namespace tdm

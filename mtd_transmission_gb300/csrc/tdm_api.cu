@@ -14,8 +14,8 @@ using namespace tdm;
 namespace tdm {
 const char* const kKernelNames[K_COUNT] = {
     "extract_rows", "extract_cols", "argmax", "field_rows", "field_cols", "volkov_rows", "volkov_cols",
-    "volkov_integ_rows", "volkov_integ_cols", "aber_fit", "form", "fzm0", "cap_rows", "cap_cols", "gather",
-    "ypass", "xpass", "posspec", "zpass", "aber_reduce"};
+    "volkov_integ_rows", "volkov_integ_cols", "aber_fit", "form", "cap_rows", "cap_cols", "gather",
+    "ypass", "xpass", "posspec", "zpass"};
 
 cudaEvent_t prof_event(tdm_ctx* c) {
     if (!c->ev_pool.empty()) {
@@ -78,9 +78,9 @@ int dev_alloc(tdm_ctx* c, T** p, size_t count) {
 void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
-                    b.specval, b.fzm0, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta, b.fields,
-                    b.r1, b.rec, b.fit_part, b.vol, b.out_re, b.out_im, b.out_otf, b.out_cnt,
-                    b.samp_idx, b.samp_q, b.rinv, b.err};
+                    b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
+                    b.fit_part, b.fit_done, b.fields, b.r1, b.rec, b.vol, b.out_re, b.out_im, b.out_otf,
+                    b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = Buffers{};
@@ -306,6 +306,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaEventCreateWithFlags(&c->ev_free[i], cudaEventDisableTiming);
     }
     for (auto& e : c->ev_stage) cudaEventCreate(&e);
+    for (auto& e : c->ev_out) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk, L = p.L;
     c->holo_chunk = 16;
@@ -319,7 +320,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.spectra, M * FF));
     TRY(dev_alloc(c, &b.posspec, M));
     TRY(dev_alloc(c, &b.specval, M));
-    TRY(dev_alloc(c, &b.fzm0, M));
+    TRY(dev_alloc(c, &b.argpart, CH * 32));
     TRY(dev_alloc(c, &b.I1, CH * FF));
     TRY(dev_alloc(c, &b.phase, CH * FF));
     TRY(dev_alloc(c, &b.amp, CH * FF));
@@ -329,10 +330,11 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.tq, CH * L * F));
     TRY(dev_alloc(c, &b.unwrapped, CH * FF));
     TRY(dev_alloc(c, &b.beta, CH * 2 * kNC));
+    TRY(dev_alloc(c, &b.fit_part, CH * 2 * 8 * kNC));
+    TRY(dev_alloc(c, &b.fit_done, CH * 2));
     TRY(dev_alloc(c, &b.fields, M * FF));
     TRY(dev_alloc(c, &b.r1, CH * FF));
     TRY(dev_alloc(c, &b.rec, M * FF));
-    TRY(dev_alloc(c, &b.fit_part, CH * 2 * kFitSlices * kNC));
     TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
     TRY(dev_alloc(c, &b.err, 4));
@@ -346,7 +348,8 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaMemcpy(b.tuk_f, tff.data(), F * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tab, stab.data(), FF * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tabf, stabf.data(), FF * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(b.err, 0, 4 * sizeof(int)) != cudaSuccess)
+        cudaMemset(b.err, 0, 4 * sizeof(int)) != cudaSuccess ||
+        cudaMemset(b.fit_done, 0, CH * 2 * sizeof(unsigned)) != cudaSuccess)
         TRY(cuda_fail(c, cudaGetLastError(), "table upload"));
     if (p.c_aber) TRY(build_aberration(c, nullptr));
 #undef TRY
@@ -365,6 +368,8 @@ int tdm_destroy(tdm_ctx* c) {
         if (c->ev_free[i]) cudaEventDestroy(c->ev_free[i]);
     }
     for (auto& e : c->ev_stage)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->ev_out)
         if (e) cudaEventDestroy(e);
     prof_release(c);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -541,11 +546,13 @@ int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_o
     return run_fields(c, spectra_in, n, fields_out, posspec_out, phase_out, unwrapped_out, amp_out);
 }
 
-// Cap mapping and volume; outputs may be host or device memory.
-static int run_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
+// Volume stage (and, with cap = true, the cap mapping of fields [0, n)
+// first); outputs may be host or device memory.  Host outputs are written to
+// device staging buffers and downloaded while the later passes run.
+static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
     const Params& p = c->p;
     const size_t NT = (size_t)p.D * p.D * p.D;
-    if (int rc = launch_cap(c, n)) return fail(c, rc, "cap mapping launch failed");
+    if (cap && launch_cap(c, 0, n)) return fail(c, TDM_ECUDA, "cap mapping launch failed");
     TDM_CU(cudaEventRecord(c->ev_stage[3], c->stream));
     Buffers& b = c->b;
     auto dev_or_stage = [&](auto* user, auto*& stage) -> decltype(user) {
@@ -556,18 +563,19 @@ static int run_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uin
         }
         return stage;
     };
-    float* dre = dev_or_stage(re, b.out_re);
-    float* dim = dev_or_stage(im, b.out_im);
-    uint8_t* dotf = dev_or_stage(otf, b.out_otf);
-    uint32_t* dcnt = dev_or_stage(cnt, b.out_cnt);
-    if ((re && !dre) || (im && !dim) || (otf && !dotf) || (cnt && !dcnt))
+    VolumeOut out;
+    out.re = dev_or_stage(re, b.out_re);
+    out.im = dev_or_stage(im, b.out_im);
+    out.otf = dev_or_stage(otf, b.out_otf);
+    out.cnt = dev_or_stage(cnt, b.out_cnt);
+    if ((re && !out.re) || (im && !out.im) || (otf && !out.otf) || (cnt && !out.cnt))
         return fail(c, TDM_ENOMEM, "output staging allocation failed");
-    if (int rc = launch_volume(c, n, dre, dim, dotf, dcnt)) return fail(c, rc, "volume launch failed");
-    bool host = false;
-    if (re && dre != re) { TDM_CU(cudaMemcpyAsync(re, dre, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream)); host = true; }
-    if (im && dim != im) { TDM_CU(cudaMemcpyAsync(im, dim, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream)); host = true; }
-    if (otf && dotf != otf) { TDM_CU(cudaMemcpyAsync(otf, dotf, NT, cudaMemcpyDeviceToHost, c->stream)); host = true; }
-    if (cnt && dcnt != cnt) { TDM_CU(cudaMemcpyAsync(cnt, dcnt, NT * 4, cudaMemcpyDeviceToHost, c->stream)); host = true; }
+    if (re && out.re != re) out.host_re = re;
+    if (im && out.im != im) out.host_im = im;
+    if (otf && out.otf != otf) out.host_otf = otf;
+    if (cnt && out.cnt != cnt) out.host_cnt = cnt;
+    if (int rc = launch_volume(c, n, out)) return fail(c, rc, "volume launch failed");
+    const bool host = out.host_re || out.host_im || out.host_otf || out.host_cnt;
     return host ? tdm_synchronize(c) : TDM_OK;
 }
 
@@ -596,9 +604,38 @@ int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_i
         }
     }
     TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
-    int rc = run_volume(c, n, indice_out, absorption_out, otf_out, counts_out);
+    int rc = run_volume(c, n, true, indice_out, absorption_out, otf_out, counts_out);
     if (rc) return rc;
     if (fields_in && !is_device_ptr(fields_in)) return tdm_synchronize(c);
+    return TDM_OK;
+}
+
+// Per-angle stages of the pipeline, streamed by hologram chunk: for each
+// chunk, extraction, field formation and cap mapping run back to back (the
+// chunk's spectra and fields stay in L2), and with host holograms the upload
+// of the next chunk overlaps them.
+static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
+    const Params& p = c->p;
+    const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
+    const bool dev = is_device_ptr(holos);
+    const size_t stage_bytes = (size_t)c->holo_chunk * p.H * p.H * 2;
+    for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
+        const int m = std::min(c->holo_chunk, n - h0);
+        const void* src = static_cast<const char*>(holos) + h0 * per;
+        const int buf = k & 1;
+        if (!dev) {
+            uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
+            if (k >= 2) TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));
+            TDM_CU(cudaMemcpyAsync(dst, src, m * per, cudaMemcpyHostToDevice, c->copy_stream));
+            TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
+            TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf], 0));
+            src = dst;
+        }
+        if (int rc = launch_extract(c, src, bits, m, h0)) return fail(c, rc, "extraction launch failed");
+        if (!dev) TDM_CU(cudaEventRecord(c->ev_free[buf], c->stream));
+        if (int rc = launch_fields(c, h0, m, nullptr, nullptr, nullptr)) return fail(c, rc, "fields launch failed");
+        if (int rc = launch_cap(c, h0, m)) return fail(c, rc, "cap mapping launch failed");
+    }
     return TDM_OK;
 }
 
@@ -608,17 +645,16 @@ int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_o
         return fail(c, TDM_EINVAL, "tdm_pipeline: invalid argument");
     cudaSetDevice(c->device);
     TDM_CU(cudaEventRecord(c->ev_stage[0], c->stream));
-    if (int rc = stage_extract(c, holos, bits, n)) return rc;
-    TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));
-    c->n_spectra = n;
-    if (int rc = launch_fields(c, 0, n, nullptr, nullptr, nullptr)) return fail(c, rc, "fields launch failed");
+    if (int rc = stage_angles(c, holos, bits, n)) return rc;
+    TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));  // extract, fields and map are interleaved
     TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
+    c->n_spectra = n;
     c->n_fields = n;
     if (posspec_out && is_device_ptr(posspec_out)) {
         Launch l(c, K_POSSPEC);
         k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
     }
-    int rc = run_volume(c, n, indice_out, absorption_out, otf_out, counts_out);
+    int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out);
     if (rc) return rc;
     if (posspec_out && !is_device_ptr(posspec_out)) {
         std::vector<int2> tmp(n);

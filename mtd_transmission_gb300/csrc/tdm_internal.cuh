@@ -12,7 +12,8 @@
 namespace tdm {
 
 constexpr int kNC = 15;  // degree-4 2D polynomial: 15 monomials
-constexpr int kFitSlices = 8;  // sample slices per fit (one CTA each)
+constexpr int kOutSlabs = 8;  // x-pass slabs whose outputs are downloaded while the next slab runs
+constexpr int kOutEvents = kOutSlabs + 3;
 
 // Device-side parameters of one volume, fixed at context creation.
 struct Params {
@@ -39,7 +40,7 @@ struct Buffers {
     float2* spectra = nullptr;     // max_angles x F*F
     int2* posspec = nullptr;       // max_angles
     float2* specval = nullptr;     // max_angles
-    double* fzm0 = nullptr;        // max_angles (negative: angle skipped)
+    float2* argpart = nullptr;     // chunk x 32 partial maxima of the specular search (value, index bits)
     float2* I1 = nullptr;          // chunk x F*F
     float* phase = nullptr;        // chunk x F*F
     float* amp = nullptr;          // chunk x F*F
@@ -49,7 +50,8 @@ struct Buffers {
     float2* tq = nullptr;          // chunk x L*F
     float* unwrapped = nullptr;    // chunk x F*F
     double* beta = nullptr;        // chunk x 2 x kNC
-    double* fit_part = nullptr;    // chunk x 2 x kFitSlices x kNC partial sums of the fits
+    float* fit_part = nullptr;     // chunk x 2 x 8 x kNC slice sums of the fits
+    unsigned* fit_done = nullptr;  // chunk x 2 finished-slice counters (zero between launches)
     float2* fields = nullptr;      // max_angles x F*F
     float2* r1 = nullptr;          // chunk x F*F
     float4* rec = nullptr;         // max_angles x F*F cap records (contribution re, im; plane; unused)
@@ -67,8 +69,8 @@ struct Buffers {
 // Kernel names for the opt-in per-launch profiler (tdm_profile).
 enum KernelId {
     K_EXTRACT_ROWS, K_EXTRACT_COLS, K_ARGMAX, K_FIELD_ROWS, K_FIELD_COLS, K_VOLKOV_ROWS, K_VOLKOV_COLS,
-    K_VOLKOV_INTEG_ROWS, K_VOLKOV_INTEG_COLS, K_ABER_FIT, K_FORM, K_FZM0, K_CAP_ROWS, K_CAP_COLS, K_GATHER,
-    K_YPASS, K_XPASS, K_POSSPEC, K_ZPASS, K_ABER_REDUCE, K_COUNT
+    K_VOLKOV_INTEG_ROWS, K_VOLKOV_INTEG_COLS, K_ABER_FIT, K_FORM, K_CAP_ROWS, K_CAP_COLS, K_GATHER,
+    K_YPASS, K_XPASS, K_POSSPEC, K_ZPASS, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 
@@ -96,6 +98,7 @@ struct tdm_ctx {
     cudaEvent_t ev_copy[2] = {nullptr, nullptr};
     cudaEvent_t ev_free[2] = {nullptr, nullptr};
     cudaEvent_t ev_stage[8] = {};
+    cudaEvent_t ev_out[tdm::kOutEvents] = {};  // downloads of the volume outputs (copy stream)
     uint64_t launches = 0;
     bool prof = false;
     std::vector<tdm::ProfRec> prof_recs;
@@ -129,10 +132,23 @@ struct Launch {
 int launch_extract(tdm_ctx* c, const void* holos_dev, int bits, int n, int a0);
 // per-angle field formation for spectra [a0, a0 + n)
 int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp);
-// per-field spectra and cap contributions for fields [0, n)
-int launch_cap(tdm_ctx* c, int n);
-// gather, normalisation and 3D inverse FFT into the output buffers
-int launch_volume(tdm_ctx* c, int n, float* re, float* im, uint8_t* otf, uint32_t* cnt);
-// one-off kernels
-int launch_fzm0(tdm_ctx* c, int n);
+// per-field spectra and cap contributions for fields [a0, a0 + n)
+int launch_cap(tdm_ctx* c, int a0, int n);
+// Outputs of the volume stage: the device buffers the kernels write and, for
+// each caller buffer in host memory, the host destination its device copy is
+// downloaded to on the copy stream as soon as the pass that completes it has
+// run (the index and absorption volumes slab by slab during the x pass).
+struct VolumeOut {
+    float* re = nullptr;
+    float* im = nullptr;
+    uint8_t* otf = nullptr;
+    uint32_t* cnt = nullptr;
+    float* host_re = nullptr;
+    float* host_im = nullptr;
+    uint8_t* host_otf = nullptr;
+    uint32_t* host_cnt = nullptr;
+};
+// gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs;
+// on return c->stream is ordered after the downloads
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out);
 }  // namespace tdm
