@@ -8,7 +8,10 @@ inverted.  One step reconstructs one volume from its 600 holograms.
 
   value  volumes/s with the holograms already in HBM (device buffers)
   e2e    volumes/s through the C ABI with pinned host holograms and host
-         outputs (index, absorption, OTF mask), copies inside the timed region
+         outputs (index, absorption, OTF mask), copies inside the timed region:
+         consecutive volumes queued with tdm_pipeline_async (a volume's
+         downloads overlap the next one's uploads and kernels); sync_value is
+         the same with one blocking tdm_pipeline call per volume
 
 Multi-GPU (torchrun): independent replicas, one volume per rank per step,
 no data-path collective; value is the whole-job volumes/s.
@@ -35,8 +38,8 @@ if ROOT not in sys.path:
 METRIC = "512³ volumes/s (600 holos): plain vs batched/TV-adjoint; rel-L2≤1e-4 vs FP64"
 UNIT = "volumes/s"
 
-# Algorithmic bytes per launch unit (compulsory input + output of the kernel):
-# see DESIGN.md, section "Roofline".
+# Algorithmic bytes per launch unit: the compulsory input and output bytes of
+# each kernel (what it must read and write at least once).
 def algorithmic_bytes(name, acq, hits_per_angle):
     H, F, D = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final
     L = 2 * F
@@ -206,7 +209,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rytov_1024")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=12)
     ap.add_argument("--ref-sample", type=int, default=8)
@@ -298,24 +301,38 @@ def main():
     ms_max = float(t_max.item())
     value = world * args.steps / (ms_max / 1e3)
 
-    # end to end: pinned host holograms and outputs through the C ABI
+    # end to end: pinned host holograms and outputs through the C ABI.  Sync:
+    # tdm_pipeline per step (returns with the volume in host memory).
+    # Pipelined: tdm_pipeline_async per step into alternating host output
+    # sets and one tdm_synchronize, so that a step's downloads overlap the
+    # next step's uploads and kernels; every step's upload and download is
+    # inside the timed region either way.
     h_holos = torch.empty(holos.shape, dtype=holos.dtype, pin_memory=True)
     h_holos.copy_(holos)
-    h_re = torch.empty((D, D, D), dtype=torch.float32, pin_memory=True)
-    h_im = torch.empty((D, D, D), dtype=torch.float32, pin_memory=True)
-    h_otf = torch.empty((D, D, D), dtype=torch.uint8, pin_memory=True)
-    e2e_s = 0.0
+    h_outs = [(torch.empty((D, D, D), dtype=torch.float32, pin_memory=True),
+               torch.empty((D, D, D), dtype=torch.float32, pin_memory=True),
+               torch.empty((D, D, D), dtype=torch.uint8, pin_memory=True)) for _ in range(2)]
+    e2e_s = e2e_sync_s = 0.0
     if args.e2e_steps > 0:
+        h_re, h_im, h_otf = h_outs[0]
         ctx.pipeline(h_holos, indice=h_re, absorption=h_im, otf=h_otf)  # warm-up of the host path
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             ctx.pipeline(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
+        e2e_sync_s = time.perf_counter() - t0
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            h_re, h_im, h_otf = h_outs[k % 2]
+            ctx.pipeline_async(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
+        ctx.synchronize()
         e2e_s = time.perf_counter() - t0
-    t_e = torch.tensor([e2e_s], device="cuda")
+    t_e = torch.tensor([e2e_s, e2e_sync_s], device="cuda")
     if world > 1:
         dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
-    e2e_value = world * args.e2e_steps / float(t_e.item()) if args.e2e_steps > 0 else None
+    e2e_value = world * args.e2e_steps / float(t_e[0].item()) if args.e2e_steps > 0 else None
+    e2e_sync = world * args.e2e_steps / float(t_e[1].item()) if args.e2e_steps > 0 else None
     h2d = int(h_holos.numel() * h_holos.element_size())
     d2h = int(2 * D ** 3 * 4 + D ** 3)
 
@@ -354,7 +371,11 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(acq, args),
             "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "mode": "pipelined: tdm_pipeline_async per step (pinned host holograms in, pinned host "
+                            "volumes out, alternating output sets), one tdm_synchronize at the end",
+                    "sync_value": round(e2e_sync, 3) if e2e_sync else None,
+                    "sync_mode": "tdm_pipeline per step, each call returns with the volume in host memory"},
             "gpu_launches": int(launches),
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -135,6 +135,16 @@ int tdm_reconstruct(tdm_ctx* ctx, const float* fields_in, const int32_t* posspec
 int tdm_pipeline(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
                  uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out);
 
+/* tdm_pipeline that returns once the work is queued, for a sequence of
+ * volumes (time-lapse acquisition).  No counterpart in the reference.  Host
+ * buffers should be page-locked (cudaHostAlloc / cudaHostRegister) for the
+ * copies to run asynchronously, and must stay untouched until
+ * tdm_synchronize(ctx) returns; the outputs are complete only then.  Calls on
+ * one context run in order; a call's uploads and kernels overlap the
+ * previous call's output downloads (separate copy engines). */
+int tdm_pipeline_async(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                       uint8_t* otf_out, uint32_t* counts_out);
+
 /* Off-axis extraction that allocates nothing.  No counterpart in the
  * reference: it is for callers that cannot allocate GPU memory, such as a
  * camera acquisition loop that must not stall on cudaMalloc between bursts of

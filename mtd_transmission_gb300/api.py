@@ -27,7 +27,7 @@ EXPORTS = (
     "tdm_fields", "tdm_fields_debug", "tdm_reconstruct", "tdm_pipeline", "tdm_synchronize", "tdm_stream",
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
-    "tdm_extract_noalloc",
+    "tdm_extract_noalloc", "tdm_pipeline_async",
 )
 
 
@@ -86,6 +86,7 @@ def lib():
     L.tdm_fields_debug.argtypes = [P, P, I, P, P, P, P, P]
     L.tdm_reconstruct.argtypes = [P, P, P, I, P, P, P, P]
     L.tdm_pipeline.argtypes = [P, P, I, I, P, P, P, P, P]
+    L.tdm_pipeline_async.argtypes = [P, P, I, I, P, P, P, P]
     L.tdm_synchronize.argtypes = [P]
     L.tdm_stream.argtypes = [P]
     L.tdm_stream.restype = P
@@ -234,6 +235,13 @@ class Context:
         n = holos.shape[0] if n is None else n
         self._check(lib().tdm_pipeline(self._h, ptr(holos), self._bits(holos), n, ptr(indice), ptr(absorption),
                                        ptr(otf), ptr(counts), ptr(posspec)), "tdm_pipeline")
+
+    def pipeline_async(self, holos, indice=None, absorption=None, otf=None, counts=None, n=None):
+        """tdm_pipeline_async: queues one volume and returns; outputs are complete after synchronize().
+        Host buffers should be pinned and must stay untouched until then."""
+        n = holos.shape[0] if n is None else n
+        self._check(lib().tdm_pipeline_async(self._h, ptr(holos), self._bits(holos), n, ptr(indice),
+                                             ptr(absorption), ptr(otf), ptr(counts)), "tdm_pipeline_async")
 
 
 def extract_noalloc(geom: Geometry, holos, spectra_out, stream: int = 0, n=None) -> int:

@@ -340,12 +340,12 @@ int cap_impl(tdm_ctx* c, int a0, int n) {
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
-// Download of bytes from a device buffer to host memory on the copy stream,
-// after the work queued so far on c->stream.
+// Download of bytes from a device buffer to host memory on the download
+// stream, after the work queued so far on c->stream.
 static cudaError_t download_after(tdm_ctx* c, cudaEvent_t ev, void* host, const void* dev, size_t bytes) {
     cudaError_t e = cudaEventRecord(ev, c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, ev, 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->dl_stream, ev, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->dl_stream);
     return e;
 }
 
@@ -365,6 +365,9 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
+    const bool host_out = out.host_re || out.host_im || out.host_otf || out.host_cnt;
+    // the staging buffers may still be downloading the previous volume
+    if (host_out && cudaStreamWaitEvent(c->stream, c->ev_dl_done, 0)) return TDM_ECUDA;
     if (cnt) {  // planes outside the cap band carry no hits
         const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
         cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), c->stream);
@@ -405,23 +408,19 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
         }
         if (host_vol) {
             const size_t off = (size_t)zb0 * P::B * D * D, len = (size_t)(zb1 - zb0) * P::B * D * D;
-            if (cudaEventRecord(c->ev_out[sl], c->stream) || cudaStreamWaitEvent(c->copy_stream, c->ev_out[sl], 0))
+            if (cudaEventRecord(c->ev_out[sl], c->stream) || cudaStreamWaitEvent(c->dl_stream, c->ev_out[sl], 0))
                 return TDM_ECUDA;
             if (out.host_re && cudaMemcpyAsync(out.host_re + off, re + off, len * sizeof(float),
-                                               cudaMemcpyDeviceToHost, c->copy_stream))
+                                               cudaMemcpyDeviceToHost, c->dl_stream))
                 return TDM_ECUDA;
             if (out.host_im && cudaMemcpyAsync(out.host_im + off, im + off, len * sizeof(float),
-                                               cudaMemcpyDeviceToHost, c->copy_stream))
+                                               cudaMemcpyDeviceToHost, c->dl_stream))
                 return TDM_ECUDA;
             downloads = true;
         }
     }
     cudaEventRecord(c->ev_stage[6], c->stream);
-    if (downloads) {  // later work on c->stream (and its synchronisation) follows the downloads
-        if (cudaEventRecord(c->ev_out[kOutSlabs + 2], c->copy_stream) ||
-            cudaStreamWaitEvent(c->stream, c->ev_out[kOutSlabs + 2], 0))
-            return TDM_ECUDA;
-    }
+    if (downloads && cudaEventRecord(c->ev_dl_done, c->dl_stream)) return TDM_ECUDA;
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 

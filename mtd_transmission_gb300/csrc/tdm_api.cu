@@ -297,7 +297,9 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     } while (0)
     cudaGetDevice(&c->device);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_dl_done, cudaEventDisableTiming) != cudaSuccess) {
         delete c;
         return TDM_ECUDA;
     }
@@ -362,6 +364,7 @@ int tdm_destroy(tdm_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
     free_all(c);
     for (int i = 0; i < 2; ++i) {
         if (c->ev_copy[i]) cudaEventDestroy(c->ev_copy[i]);
@@ -375,6 +378,8 @@ int tdm_destroy(tdm_ctx* c) {
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
+    if (c->ev_dl_done) cudaEventDestroy(c->ev_dl_done);
     delete c;
     return TDM_OK;
 }
@@ -404,6 +409,7 @@ int tdm_set_mask(tdm_ctx* c, const uint8_t* mask) {
 int tdm_synchronize(tdm_ctx* c) {
     if (!c) return TDM_EINVAL;
     TDM_CU(cudaStreamSynchronize(c->copy_stream));
+    TDM_CU(cudaStreamSynchronize(c->dl_stream));
     TDM_CU(cudaStreamSynchronize(c->stream));
     int err = 0;
     TDM_CU(cudaMemcpy(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -474,7 +480,7 @@ static int stage_extract(tdm_ctx* c, const void* holos, int bits, int n) {
         const int m = std::min(c->holo_chunk, n - h0);
         const int buf = k & 1;
         uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
-        if (k >= 2) TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));
+        TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));  // no-op before its first record
         TDM_CU(cudaMemcpyAsync(dst, static_cast<const char*>(holos) + h0 * per, m * per, cudaMemcpyHostToDevice,
                                c->copy_stream));
         TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
@@ -549,7 +555,8 @@ int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_o
 // Volume stage (and, with cap = true, the cap mapping of fields [0, n)
 // first); outputs may be host or device memory.  Host outputs are written to
 // device staging buffers and downloaded while the later passes run.
-static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt) {
+static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt,
+                      bool wait = true) {
     const Params& p = c->p;
     const size_t NT = (size_t)p.D * p.D * p.D;
     if (cap && launch_cap(c, 0, n)) return fail(c, TDM_ECUDA, "cap mapping launch failed");
@@ -576,7 +583,7 @@ static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t
     if (cnt && out.cnt != cnt) out.host_cnt = cnt;
     if (int rc = launch_volume(c, n, out)) return fail(c, rc, "volume launch failed");
     const bool host = out.host_re || out.host_im || out.host_otf || out.host_cnt;
-    return host ? tdm_synchronize(c) : TDM_OK;
+    return host && wait ? tdm_synchronize(c) : TDM_OK;
 }
 
 int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_in, int n, float* indice_out,
@@ -625,7 +632,7 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
         const int buf = k & 1;
         if (!dev) {
             uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
-            if (k >= 2) TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));
+            TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));  // no-op before its first record
             TDM_CU(cudaMemcpyAsync(dst, src, m * per, cudaMemcpyHostToDevice, c->copy_stream));
             TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
             TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf], 0));
@@ -639,8 +646,8 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
     return TDM_OK;
 }
 
-int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
-                 uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out) {
+static int pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                    uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out, bool wait) {
     if (!c || !holos || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
         return fail(c, TDM_EINVAL, "tdm_pipeline: invalid argument");
     cudaSetDevice(c->device);
@@ -654,7 +661,7 @@ int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_o
         Launch l(c, K_POSSPEC);
         k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
     }
-    int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out);
+    int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out, wait);
     if (rc) return rc;
     if (posspec_out && !is_device_ptr(posspec_out)) {
         std::vector<int2> tmp(n);
@@ -665,8 +672,18 @@ int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_o
             posspec_out[n + a] = tmp[a].y;
         }
     }
-    if (!is_device_ptr(holos)) return tdm_synchronize(c);
+    if (wait && !is_device_ptr(holos)) return tdm_synchronize(c);
     return TDM_OK;
+}
+
+int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                 uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out) {
+    return pipeline(c, holos, bits, n, indice_out, absorption_out, otf_out, counts_out, posspec_out, true);
+}
+
+int tdm_pipeline_async(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
+                       uint8_t* otf_out, uint32_t* counts_out) {
+    return pipeline(c, holos, bits, n, indice_out, absorption_out, otf_out, counts_out, nullptr, false);
 }
 
 }  // extern "C"

@@ -13,7 +13,7 @@ namespace tdm {
 
 constexpr int kNC = 15;  // degree-4 2D polynomial: 15 monomials
 constexpr int kOutSlabs = 8;  // x-pass slabs whose outputs are downloaded while the next slab runs
-constexpr int kOutEvents = kOutSlabs + 3;
+constexpr int kOutEvents = kOutSlabs + 2;
 
 // Device-side parameters of one volume, fixed at context creation.
 struct Params {
@@ -94,7 +94,9 @@ struct tdm_ctx {
     int n_fields = 0;            // angles held in b.fields / b.posspec
     int n_spectra = 0;           // angles held in b.spectra
     cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // hologram uploads
+    cudaStream_t dl_stream = nullptr;    // output downloads (a second copy engine)
+    cudaEvent_t ev_dl_done = nullptr;    // last download of the previous volume
     cudaEvent_t ev_copy[2] = {nullptr, nullptr};
     cudaEvent_t ev_free[2] = {nullptr, nullptr};
     cudaEvent_t ev_stage[8] = {};
@@ -148,7 +150,8 @@ struct VolumeOut {
     uint8_t* host_otf = nullptr;
     uint32_t* host_cnt = nullptr;
 };
-// gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs;
-// on return c->stream is ordered after the downloads
+// gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs.
+// Downloads run on c->dl_stream and end with c->ev_dl_done; the staging
+// buffers are not written before the previous volume's downloads are done.
 int launch_volume(tdm_ctx* c, int n, const VolumeOut& out);
 }  // namespace tdm

@@ -137,6 +137,31 @@ def test_pipeline_end_to_end(born):
     assert rel_l2(im, ref["indice"].imag) <= TOL
 
 
+def test_pipeline_async_sequence(born):
+    """tdm_pipeline_async: three volumes queued back to back with pinned host
+    buffers (uploads, kernels and downloads of consecutive calls overlap) give
+    the synchronous pipeline's outputs once tdm_synchronize returns."""
+    import torch
+    acq, cfg, d, spec, fields, pos, dbg = born
+    D, M = acq.dim_final, spec.shape[0]
+    holos = torch.from_numpy(np.ascontiguousarray(d["holos"])).pin_memory()
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        re0 = np.zeros((D, D, D), np.float32)
+        im0 = np.zeros((D, D, D), np.float32)
+        otf0 = np.zeros((D, D, D), np.uint8)
+        ctx.pipeline(holos, indice=re0, absorption=im0, otf=otf0)
+        outs = [(torch.full((D, D, D), float("nan")).pin_memory(), torch.full((D, D, D), float("nan")).pin_memory(),
+                 torch.zeros((D, D, D), dtype=torch.uint8).pin_memory()) for _ in range(3)]
+        for re, im, otf in outs:
+            ctx.pipeline_async(holos, indice=re, absorption=im, otf=otf)
+        ctx.synchronize()
+    for re, im, otf in outs:
+        np.testing.assert_array_equal(re.numpy(), re0)
+        np.testing.assert_array_equal(im.numpy(), im0)
+        np.testing.assert_array_equal(otf.numpy(), otf0)
+
+
 def test_reconstruct_edge_positions():
     """Specular positions at the crop edges and corners (corner angles fall
     outside the Ewald sphere and are skipped by the reference)."""
