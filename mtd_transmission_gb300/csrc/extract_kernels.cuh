@@ -14,7 +14,8 @@ namespace extract {
 // keeps the crop's kx band, written column-major (inter[a][c][y]) through a
 // shared-memory tile so that each column's 2P rows leave as one contiguous
 // segment; the column pass then reads whole columns contiguously and writes
-// the crop rows through a second tile.
+// the crop rows through a second tile (and, on request, the crop's partial
+// specular-peak winners, one record per CTA).
 template <int H>
 struct ExtractCfg {
     using W = WarpFFT<H>;
@@ -87,7 +88,7 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
 template <int H>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT)
 k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, float2* __restrict__ spectra,
-               int F, int x0, int y0) {
+               int F, int x0, int y0, float2* __restrict__ argpart) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, C = Cf::C, TC = C + 1;
@@ -117,9 +118,17 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     }
     __syncthreads();
     float2* dst = spectra + (size_t)a * F * F + c0;
+    float best = -1.0f;
+    int bi = 0x7fffffff;
     for (int i = threadIdx.x; i < F * C; i += Cf::NT) {
         const int r = i / C, t = i % C;
-        dst[(size_t)r * F + t] = tile[r * TC + t];
+        const float2 z = tile[r * TC + t];
+        dst[(size_t)r * F + t] = z;
+        if (argpart) argmax_take(best, bi, z, r * F + c0 + t);
+    }
+    if (argpart) {  // this CTA's partial winner of the specular search (gridDim.x records per angle)
+        argmax_block(best, bi);
+        if (threadIdx.x == 0) argpart[(size_t)a * gridDim.x + blockIdx.x] = make_float2(best, __int_as_float(bi));
     }
 }
 

@@ -23,7 +23,7 @@ cudaError_t allow_smem(K kernel, size_t bytes) {
 }
 
 template <int H>
-int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
+int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool argmax) {
     using C = ExtractCfg<H>;
     const Params& p = c->p;
     const size_t sm_rows = C::smem_rows(p.F), sm_cols = C::smem_cols(p.F);
@@ -41,20 +41,23 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
         {
             Launch l(c, K_EXTRACT_COLS);
             k_extract_cols<H><<<C::grid_cols(p.F, m), C::NT, sm_cols, c->stream>>>(
-                c->b.inter, c->b.tw, c->b.spectra + (size_t)(a0 + h0) * p.F * p.F, p.F, p.x0, p.y0);
+                c->b.inter, c->b.tw, c->b.spectra + (size_t)(a0 + h0) * p.F * p.F, p.F, p.x0, p.y0,
+                argmax ? c->b.argpart : nullptr);
         }
     }
-    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+    if (cudaGetLastError() != cudaSuccess) return TDM_ECUDA;
+    return argmax ? (int)C::grid_cols(p.F, 1).x : TDM_OK;
 }
 
 }  // namespace
 
-int launch_extract(tdm_ctx* c, const void* holos, int bits, int n, int a0) {
+int launch_extract(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool argmax) {
+    if (argmax && (n > c->holo_chunk || n > c->chunk)) return TDM_EINVAL;  // partials of one chunk only
     switch (c->p.H) {
-        case 256: return extract_impl<256>(c, holos, bits, n, a0);
-        case 512: return extract_impl<512>(c, holos, bits, n, a0);
-        case 1024: return extract_impl<1024>(c, holos, bits, n, a0);
-        case 2048: return extract_impl<2048>(c, holos, bits, n, a0);
+        case 256: return extract_impl<256>(c, holos, bits, n, a0, argmax);
+        case 512: return extract_impl<512>(c, holos, bits, n, a0, argmax);
+        case 1024: return extract_impl<1024>(c, holos, bits, n, a0, argmax);
+        case 2048: return extract_impl<2048>(c, holos, bits, n, a0, argmax);
         default: return TDM_EUNSUPPORTED;
     }
 }

@@ -19,6 +19,8 @@
 //             reference's normal equations, better conditioned).
 #include "tdm_internal.cuh"
 #include "fft_warp.cuh"
+#include "form.cuh"
+#include "argmax.cuh"
 
 namespace tdm {
 namespace {
@@ -38,24 +40,10 @@ __device__ __forceinline__ float kappa(int k, int L) {  // init_kvect_shift, FFT
 __device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F - 1 - X; }
 
 // ---------------------------------------------------------------- argmax
-// coordSpec (fonctions.cpp:88-101): |z|^2 at index 0, |z| elsewhere, first
-// maximum in row-major order wins.  k_argmax_part reduces kArgSlices slices of
-// each spectrum; k_field_rows, the first consumer, reduces the slices' winners.
-constexpr int kArgSlices = 32;
-
-__device__ __forceinline__ void argmax_merge(float& best, int& bi, float ob, int oi) {
-    if (ob > best || (ob == best && oi < bi)) {
-        best = ob;
-        bi = oi;
-    }
-}
-
-__device__ __forceinline__ void argmax_warp(float& best, int& bi) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-        argmax_merge(best, bi, __shfl_down_sync(0xffffffffu, best, off), __shfl_down_sync(0xffffffffu, bi, off));
-}
-
+// coordSpec (fonctions.cpp:88-101) in two steps: partial winners over slices
+// of each spectrum (k_argmax_part here, or the extraction column pass when
+// the spectra come straight from the holograms), then argmax_final in
+// k_field_rows, the first consumer.
 __global__ void __launch_bounds__(256) k_argmax_part(const float2* __restrict__ spectra, int F,
                                                      float2* __restrict__ part) {
     const int a = blockIdx.y, sl = blockIdx.x;
@@ -63,38 +51,9 @@ __global__ void __launch_bounds__(256) k_argmax_part(const float2* __restrict__ 
     const float2* s = spectra + (size_t)a * F * F;
     float best = -1.0f;
     int bi = 0x7fffffff;
-    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) {
-        const float2 z = s[i];
-        const float sq = z.x * z.x + z.y * z.y;
-        const float m = (i == 0) ? sq : sqrtf(sq);
-        if (m > best) { best = m; bi = i; }
-    }
-    argmax_warp(best, bi);
-    __shared__ float sb[8];
-    __shared__ int si[8];
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) { sb[w] = best; si[w] = bi; }
-    __syncthreads();
-    if (w == 0) {
-        best = l < 8 ? sb[l] : -1.0f;
-        bi = l < 8 ? si[l] : 0x7fffffff;
-        argmax_warp(best, bi);
-        if (l == 0) part[(size_t)a * kArgSlices + sl] = make_float2(best, __int_as_float(bi));
-    }
-}
-
-// Winner over the slices of angle a, read by every warp of the caller (lane i
-// takes slice i; the result is broadcast to all lanes).
-__device__ __forceinline__ int argmax_final(const float2* __restrict__ part, int a) {
-    static_assert(kArgSlices == 32, "one slice per lane");
-    const float2 q = part[(size_t)a * kArgSlices + (threadIdx.x & 31)];
-    float best = q.x;
-    int bi = __float_as_int(q.y);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, off), __shfl_xor_sync(0xffffffffu, bi, off));
-    }
-    return bi == 0x7fffffff ? 0 : bi;  // all NaN: the reference keeps index 0
+    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) argmax_take(best, bi, s[i], i);
+    argmax_block(best, bi);
+    if (threadIdx.x == 0) part[(size_t)a * kArgSlices + sl] = make_float2(best, __int_as_float(bi));
 }
 
 // ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
@@ -112,15 +71,16 @@ struct FieldCfg {
 
 template <int F>
 __global__ void __launch_bounds__(FieldCfg<F>::NT)
-k_field_rows(const float2* __restrict__ spectra, const float2* __restrict__ argpart, int2* __restrict__ posspec,
-             float2* __restrict__ specval, int normalize, const float2* __restrict__ tw, float2* __restrict__ I1) {
+k_field_rows(const float2* __restrict__ spectra, const float2* __restrict__ argpart, int nparts,
+             int2* __restrict__ posspec, float2* __restrict__ specval, int normalize, const float2* __restrict__ tw,
+             float2* __restrict__ I1) {
     using C = FieldCfg<F>;
     using W = typename C::W;
     constexpr int T = W::T, E = W::E;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
-    const int bi = argmax_final(argpart, a);
+    const int bi = argmax_final(argpart + (size_t)a * nparts, nparts);
     const int2 p = make_int2(bi % F, bi / F);
     const float2* spec = spectra + (size_t)a * F * F;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -498,37 +458,13 @@ __global__ void __launch_bounds__(256) k_form(const float* __restrict__ unwrappe
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= F * F) return;
     const int x = idx % F, y = idx / F;
-    const float h = 0.5f * (float)(F - 1);
-    const float u = ((float)x - h) / h, v = ((float)y - h) / h;
-    float sp = 0.0f, sa = 0.0f, up = 1.0f;
-    int k = 0;
-#pragma unroll
-    for (int px = 0; px <= 4; ++px) {
-        float pp = 0.0f, pa = 0.0f, vp = 1.0f;
-#pragma unroll
-        for (int py = 0; px + py <= 4; ++py) {
-            pp = fmaf(bf[k], vp, pp);
-            pa = fmaf(bf[kNC + k], vp, pa);
-            vp *= v;
-            ++k;
-        }
-        sp = fmaf(pp, up, sp);
-        sa = fmaf(pa, up, sa);
-        up *= u;
-    }
     const size_t o = (size_t)a * F * F + idx;
-    const float pf = unwrapped[o] - sp;
-    float af = amp[o] / (sa + 0.00000001f);
-    if (af > 10.0f) af = 1.0f;
-    if (af < -10.0f) af = 1.0f;
-    float sn, cs;
-    sincosf(pf, &sn, &cs);
-    const float m = fabsf(af);  // sqrt(A^2)
-    fields[o] = born ? make_float2(m * cs - 1.0f, m * sn) : make_float2(logf(m), pf);
+    fields[o] = form_value(form_row(bf, y, F), x, F, unwrapped[o], amp[o], born);
 }
 
 template <int F>
-int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp) {
+int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp, int argparts,
+                bool form) {
     constexpr int L = 2 * F;
     using FC = FieldCfg<F>;
     using VC = VCfg<L>;
@@ -545,14 +481,16 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
         const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
         const float2* spec = b.spectra + (size_t)g0 * FF;
-        {
+        int nparts = argparts;
+        if (!nparts) {
             Launch l(c, K_ARGMAX);
             k_argmax_part<<<dim3(kArgSlices, m), 256, 0, c->stream>>>(spec, F, b.argpart);
+            nparts = kArgSlices;
         }
         {
             Launch l(c, K_FIELD_ROWS);
             k_field_rows<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
-                spec, b.argpart, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
+                spec, b.argpart, nparts, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.tw, b.I1);
         }
         {
             Launch l(c, K_FIELD_COLS);
@@ -589,7 +527,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
             k_aber_fit<<<dim3(kFitSlices, 2, m), kFitThreads, 0, c->stream>>>(
                 unw, b.amp, b.samp_idx, b.samp_q, c->nsamp, F, b.rinv, b.fit_part, b.fit_done, b.beta);
         }
-        {
+        if (form) {
             Launch l(c, K_FORM);
             k_form<<<dim3((unsigned)((FF + 255) / 256), m), 256, 0, c->stream>>>(unw, b.amp, b.beta, F, p.born,
                                                                                 b.fields + (size_t)g0 * FF);
@@ -606,12 +544,13 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
 
 }  // namespace
 
-int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp) {
+int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp, int argparts,
+                  bool form) {
     switch (c->p.F) {
-        case 64: return fields_impl<64>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
-        case 128: return fields_impl<128>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
-        case 256: return fields_impl<256>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
-        case 512: return fields_impl<512>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp);
+        case 64: return fields_impl<64>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
+        case 128: return fields_impl<128>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
+        case 256: return fields_impl<256>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
+        case 512: return fields_impl<512>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
         default: return TDM_EUNSUPPORTED;
     }
 }

@@ -19,6 +19,7 @@
 // A z pass, a y pass and an x pass that writes the index and absorption volumes.
 #include "tdm_internal.cuh"
 #include "fft_warp.cuh"
+#include "form.cuh"
 
 namespace tdm {
 namespace {
@@ -57,6 +58,43 @@ k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, con
     }
     fft_warp_regs<F, -1>(x, sm + tr * W::STRIDE, j, tw);
     float2* dst = r1 + ((size_t)a * F + y) * F;
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) dst[j + q * T + E * k2] = x[q * T + k2];
+    }
+}
+
+// k_cap_rows with the field formed on the fly from the chunk's unwrapped
+// phase, amplitude and fits (the field stage's k_form, same arithmetic); the
+// field is also stored, as k_form would.
+template <int F>
+__global__ void __launch_bounds__(CapCfg<F>::NT)
+k_cap_rows_form(const float* __restrict__ unwrapped, const float* __restrict__ amp, const double* __restrict__ beta,
+                int born, const float* __restrict__ tuk, const float2* __restrict__ tw, float2* __restrict__ fields,
+                float2* __restrict__ r1) {
+    using C = CapCfg<F>;
+    using W = typename C::W;
+    constexpr int T = W::T, E = W::E;
+    extern __shared__ float2 sm[];
+    __shared__ float bf[2 * kNC];
+    if (threadIdx.x < 2 * kNC) bf[threadIdx.x] = (float)beta[(size_t)blockIdx.y * 2 * kNC + threadIdx.x];
+    __syncthreads();
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    const int a = blockIdx.y, y = blockIdx.x * C::B + tr;
+    const float wy = tuk[y];
+    const size_t row = ((size_t)a * F + y) * F;
+    const FormRow fr = form_row(bf, y, F);
+    float2 x[E];
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int xx = j + n1 * T;
+        const float2 f = form_value(fr, xx, F, unwrapped[row + xx], amp[row + xx], born);
+        fields[row + xx] = f;
+        x[n1] = c_scale(f, __ldg(&tuk[xx]) * wy);
+    }
+    fft_warp_regs<F, -1>(x, sm + tr * W::STRIDE, j, tw);
+    float2* dst = r1 + row;
 #pragma unroll
     for (int q = 0; q < E / T; ++q) {
 #pragma unroll
@@ -320,14 +358,21 @@ k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float sca
 }
 
 template <int F>
-int cap_impl(tdm_ctx* c, int a0, int n) {
+int cap_impl(tdm_ctx* c, int a0, int n, bool form) {
     using C = CapCfg<F>;
     Buffers& b = c->b;
-    if (allow_smem(k_cap_rows<F>, C::SMEM) || allow_smem(k_cap_cols<F>, C::SMEM)) return TDM_ECUDA;
+    if (allow_smem(k_cap_rows<F>, C::SMEM) || allow_smem(k_cap_rows_form<F>, C::SMEM) ||
+        allow_smem(k_cap_cols<F>, C::SMEM))
+        return TDM_ECUDA;
+    if (form && n > c->chunk) return TDM_EINVAL;  // the chunk buffers hold one chunk
     const size_t FF = (size_t)F * F;
     for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
         const int m = a0 + n - g0 < c->chunk ? a0 + n - g0 : c->chunk;
-        {
+        if (form) {
+            Launch l(c, K_CAP_ROWS);
+            k_cap_rows_form<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(
+                c->p.deroul ? b.unwrapped : b.phase, b.amp, b.beta, c->p.born, b.tuk_f, b.tw, b.fields + g0 * FF, b.r1);
+        } else {
             Launch l(c, K_CAP_ROWS);
             k_cap_rows<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(b.fields + g0 * FF, b.tuk_f, b.tw, b.r1);
         }
@@ -426,12 +471,12 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
 
 }  // namespace
 
-int launch_cap(tdm_ctx* c, int a0, int n) {
+int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
     switch (c->p.F) {
-        case 64: return cap_impl<64>(c, a0, n);
-        case 128: return cap_impl<128>(c, a0, n);
-        case 256: return cap_impl<256>(c, a0, n);
-        case 512: return cap_impl<512>(c, a0, n);
+        case 64: return cap_impl<64>(c, a0, n, form);
+        case 128: return cap_impl<128>(c, a0, n, form);
+        case 256: return cap_impl<256>(c, a0, n, form);
+        case 512: return cap_impl<512>(c, a0, n, form);
         default: return TDM_EUNSUPPORTED;
     }
 }

@@ -322,7 +322,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.spectra, M * FF));
     TRY(dev_alloc(c, &b.posspec, M));
     TRY(dev_alloc(c, &b.specval, M));
-    TRY(dev_alloc(c, &b.argpart, CH * 32));
+    TRY(dev_alloc(c, &b.argpart, CH * kArgPartsMax));
     TRY(dev_alloc(c, &b.I1, CH * FF));
     TRY(dev_alloc(c, &b.phase, CH * FF));
     TRY(dev_alloc(c, &b.amp, CH * FF));
@@ -638,10 +638,15 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
             TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf], 0));
             src = dst;
         }
-        if (int rc = launch_extract(c, src, bits, m, h0)) return fail(c, rc, "extraction launch failed");
+        // the extraction leaves the specular search's partial winners for the
+        // field stage; with C_ABER the cap row pass forms the fields
+        const int parts = launch_extract(c, src, bits, m, h0, true);
+        if (parts <= 0) return fail(c, parts ? parts : TDM_ECUDA, "extraction launch failed");
         if (!dev) TDM_CU(cudaEventRecord(c->ev_free[buf], c->stream));
-        if (int rc = launch_fields(c, h0, m, nullptr, nullptr, nullptr)) return fail(c, rc, "fields launch failed");
-        if (int rc = launch_cap(c, h0, m)) return fail(c, rc, "cap mapping launch failed");
+        const bool form_in_cap = p.c_aber != 0;
+        if (int rc = launch_fields(c, h0, m, nullptr, nullptr, nullptr, parts, !form_in_cap))
+            return fail(c, rc, "fields launch failed");
+        if (int rc = launch_cap(c, h0, m, form_in_cap)) return fail(c, rc, "cap mapping launch failed");
     }
     return TDM_OK;
 }

@@ -8,6 +8,7 @@
 
 #include "../../include/tdm.h"
 #include "fft_core.cuh"
+#include "argmax.cuh"
 
 namespace tdm {
 
@@ -40,7 +41,7 @@ struct Buffers {
     float2* spectra = nullptr;     // max_angles x F*F
     int2* posspec = nullptr;       // max_angles
     float2* specval = nullptr;     // max_angles
-    float2* argpart = nullptr;     // chunk x 32 partial maxima of the specular search (value, index bits)
+    float2* argpart = nullptr;     // chunk x kArgPartsMax partial winners of the specular search
     float2* I1 = nullptr;          // chunk x F*F
     float* phase = nullptr;        // chunk x F*F
     float* amp = nullptr;          // chunk x F*F
@@ -130,12 +131,21 @@ struct Launch {
         c->launches++;
     }
 };
-// extraction of holograms [0, n) from device memory into spectra[a0, a0 + n)
-int launch_extract(tdm_ctx* c, const void* holos_dev, int bits, int n, int a0);
-// per-angle field formation for spectra [a0, a0 + n)
-int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp);
-// per-field spectra and cap contributions for fields [a0, a0 + n)
-int launch_cap(tdm_ctx* c, int a0, int n);
+// Extraction of holograms [0, n) from device memory into spectra[a0, a0 + n).
+// With argmax = true (n at most one chunk), the column pass also leaves the
+// specular search's partial winners of each angle in b.argpart; the return
+// value is then the number of partial records per angle (> 0).
+int launch_extract(tdm_ctx* c, const void* holos_dev, int bits, int n, int a0, bool argmax = false);
+// Per-angle field formation for spectra [a0, a0 + n).  argparts > 0: the
+// extraction left that many partial winners per angle (one chunk only);
+// form = false (C_ABER pipeline): the fields are formed by the cap row pass.
+int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp,
+                  int argparts = 0, bool form = true);
+// Per-field spectra and cap contributions for fields [a0, a0 + n); with
+// form = true (one chunk, after launch_fields(..., form = false)) the fields
+// are formed from the chunk's unwrapped phase, amplitude and fits on the fly
+// (and stored in b.fields).
+int launch_cap(tdm_ctx* c, int a0, int n, bool form = false);
 // Outputs of the volume stage: the device buffers the kernels write and, for
 // each caller buffer in host memory, the host destination its device copy is
 // downloaded to on the copy stream as soon as the pass that completes it has

@@ -101,7 +101,7 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
             static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), s.twiddle, s.scratch, F,
             x0);
         k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
-            s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0);
+            s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0, nullptr);
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
