@@ -10,7 +10,7 @@
 namespace tdm {
 
 constexpr int kArgSlices = 32;     // slices per spectrum of the standalone partial pass
-constexpr int kArgPartsMax = 64;   // partial records per angle, any producer
+constexpr int kArgPartsMax = 512;  // partial records per angle, any producer
 
 __device__ __forceinline__ void argmax_merge(float& best, int& bi, float ob, int oi) {
     if (ob > best || (ob == best && oi < bi)) {

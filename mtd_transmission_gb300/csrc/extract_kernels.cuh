@@ -5,6 +5,7 @@
 
 #include "tdm_internal.cuh"
 #include "fft_warp.cuh"
+#include "bulk_copy.cuh"
 
 namespace tdm {
 namespace extract {
@@ -15,7 +16,7 @@ namespace extract {
 // shared-memory tile so that each column's 2P rows leave as one contiguous
 // segment; the column pass then reads whole columns contiguously and writes
 // the crop rows through a second tile (and, on request, the crop's partial
-// specular-peak winners, one record per CTA).
+// specular-peak winners, one record per warp).
 template <int H>
 struct ExtractCfg {
     using W = WarpFFT<H>;
@@ -28,14 +29,19 @@ struct ExtractCfg {
     static dim3 grid_cols(int F, int m) { return dim3(F / C, m); }
 };
 
-template <int H>
+// Row pass.  BULK: each warp's 2G rows (its G row pairs, consecutive in
+// memory) are staged in shared memory by one bulk copy and read from there;
+// requires a 16-byte aligned stack.  Otherwise the lanes load the pixels
+// directly.  A bulk copy that does not complete within the poll bound sets
+// bit 1 of *err (the call then fails).
+template <int H, bool BULK>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT)
 k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk,
-               const float2* __restrict__ tw, float2* __restrict__ inter, int F, int x0) {
+               const float2* __restrict__ tw, float2* __restrict__ inter, int F, int x0, int* __restrict__ err) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, P = Cf::P, TP = 2 * P + 1;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2* tile = sm + P * W::STRIDE;  // F x TP: [c][row in CTA]
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y;
@@ -43,10 +49,35 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
     float2* s = sm + tr * W::STRIDE;
     const float wa = tuk[ya], wb = tuk[yb];
     const float sx = (j & 1) ? -1.0f : 1.0f;  // (-1)^x for x = j + T n1, T even; ya even, yb odd
-    const size_t base = (size_t)a * H * H;
+    const size_t bpp = bits == 16 ? 2 : 1;
+    const char* row = static_cast<const char*>(holos) + ((size_t)a * H * H + (size_t)ya * H) * bpp;
+    if constexpr (BULK) {
+        __shared__ uint64_t bar[Cf::NT / 32];
+        const int w = threadIdx.x >> 5;
+        static_assert(2 * W::G * H * 2 + 8 <= W::STRIDE * 8, "staged rows fit the first array");
+        // the warp's rows land at the first 16-byte boundary of its first
+        // transform's array (8 (H + E + 1) bytes, so 2G H bpp + 8 fit), which
+        // the transforms overwrite only after all lanes have read their pixels
+        // (the first exchange follows a __syncwarp)
+        char* stage = reinterpret_cast<char*>(
+            (reinterpret_cast<uintptr_t>(sm + (w * W::G) * W::STRIDE) + 15) & ~static_cast<uintptr_t>(15));
+        if ((threadIdx.x & 31) == 0) {
+            const uint32_t bytes = (uint32_t)(2 * W::G * H * bpp);
+            const size_t y0w = 2 * ((size_t)blockIdx.x * P + w * W::G);
+            mbar_init(&bar[w]);
+            mbar_expect_tx(&bar[w], bytes);
+            bulk_g2s(stage, static_cast<const char*>(holos) + ((size_t)a * H * H + y0w * H) * bpp, bytes, &bar[w]);
+        }
+        __syncwarp();
+        if (!mbar_wait(&bar[w], 0)) {
+            if ((threadIdx.x & 31) == 0) atomicOr(err, 2);
+            mbar_wait(&bar[w], 0);
+        }
+        row = stage + (size_t)(tr - w * W::G) * 2 * H * bpp;
+    }
     float2 x[E];
     if (bits == 16) {
-        const uint16_t* ra = static_cast<const uint16_t*>(holos) + base + (size_t)ya * H;
+        const uint16_t* ra = reinterpret_cast<const uint16_t*>(row);
 #pragma unroll
         for (int n1 = 0; n1 < E; ++n1) {
             const int xx = j + n1 * T;
@@ -54,7 +85,7 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
             x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
         }
     } else {
-        const uint8_t* ra = static_cast<const uint8_t*>(holos) + base + (size_t)ya * H;
+        const uint8_t* ra = reinterpret_cast<const uint8_t*>(row);
 #pragma unroll
         for (int n1 = 0; n1 < E; ++n1) {
             const int xx = j + n1 * T;
@@ -92,7 +123,7 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, C = Cf::C, TC = C + 1;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2* tile = sm + C * W::STRIDE;  // F x TC: [crop row][column in CTA]
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, c0 = blockIdx.x * C, c = c0 + tr;
@@ -111,24 +142,25 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     __syncwarp();
     const float inv = 1.0f / ((float)H * (float)H);
     const int kx = x0 + c;
+    float best = -1.0f;
+    int bi = 0x7fffffff;
     for (int r = j; r < F; r += T) {
         const int ky = y0 + r;
         const float sg = ((kx + ky) & 1) ? -inv : inv;
-        tile[r * TC + tr] = c_scale(s[W::pad(ky)], sg);
+        const float2 z = c_scale(s[W::pad(ky)], sg);
+        tile[r * TC + tr] = z;
+        if (argpart) argmax_take(best, bi, z, r * F + c);
+    }
+    if (argpart) {  // this warp's partial winner of the specular search (8 records per CTA)
+        argmax_warp(best, bi);
+        if ((threadIdx.x & 31) == 0)
+            argpart[((size_t)a * gridDim.x + blockIdx.x) * 8 + (threadIdx.x >> 5)] = make_float2(best, __int_as_float(bi));
     }
     __syncthreads();
     float2* dst = spectra + (size_t)a * F * F + c0;
-    float best = -1.0f;
-    int bi = 0x7fffffff;
     for (int i = threadIdx.x; i < F * C; i += Cf::NT) {
         const int r = i / C, t = i % C;
-        const float2 z = tile[r * TC + t];
-        dst[(size_t)r * F + t] = z;
-        if (argpart) argmax_take(best, bi, z, r * F + c0 + t);
-    }
-    if (argpart) {  // this CTA's partial winner of the specular search (gridDim.x records per angle)
-        argmax_block(best, bi);
-        if (threadIdx.x == 0) argpart[(size_t)a * gridDim.x + blockIdx.x] = make_float2(best, __int_as_float(bi));
+        dst[(size_t)r * F + t] = tile[r * TC + t];
     }
 }
 

@@ -27,16 +27,20 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
     using C = ExtractCfg<H>;
     const Params& p = c->p;
     const size_t sm_rows = C::smem_rows(p.F), sm_cols = C::smem_cols(p.F);
-    if (allow_smem(k_extract_rows<H>, sm_rows) != cudaSuccess) return TDM_ECUDA;
+    if (allow_smem(k_extract_rows<H, true>, sm_rows) != cudaSuccess) return TDM_ECUDA;
+    if (allow_smem(k_extract_rows<H, false>, sm_rows) != cudaSuccess) return TDM_ECUDA;
     if (allow_smem(k_extract_cols<H>, sm_cols) != cudaSuccess) return TDM_ECUDA;
+    // bulk staging of the rows needs a 16-byte aligned stack (rows are multiples of 16 bytes)
+    const bool bulk = (reinterpret_cast<uintptr_t>(holos) & 15) == 0;
+    auto rows = bulk ? k_extract_rows<H, true> : k_extract_rows<H, false>;
     const size_t bytes_per = (size_t)H * H * (bits == 16 ? 2 : 1);
     for (int h0 = 0; h0 < n; h0 += c->holo_chunk) {
         const int m = n - h0 < c->holo_chunk ? n - h0 : c->holo_chunk;
         const char* src = static_cast<const char*>(holos) + (size_t)h0 * bytes_per;
         {
             Launch l(c, K_EXTRACT_ROWS);
-            k_extract_rows<H><<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->b.tw,
-                                                                             c->b.inter, p.F, p.x0);
+            rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->b.tw, c->b.inter, p.F,
+                                                                p.x0, c->b.err);
         }
         {
             Launch l(c, K_EXTRACT_COLS);
@@ -46,7 +50,7 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
         }
     }
     if (cudaGetLastError() != cudaSuccess) return TDM_ECUDA;
-    return argmax ? (int)C::grid_cols(p.F, 1).x : TDM_OK;
+    return argmax ? (int)C::grid_cols(p.F, 1).x * (C::NT / 32) : TDM_OK;
 }
 
 }  // namespace

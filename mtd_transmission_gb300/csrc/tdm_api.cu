@@ -415,6 +415,7 @@ int tdm_synchronize(tdm_ctx* c) {
     TDM_CU(cudaMemcpy(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
         cudaMemset(c->b.err, 0, sizeof(int));
+        if (err & 2) return fail(c, TDM_ECUDA, "a bulk copy of hologram rows did not complete");
         return fail(c, TDM_EDATA, "an Ewald-cap voxel fell outside the DIM_FINAL volume");
     }
     return TDM_OK;

@@ -87,7 +87,7 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
     using C = ExtractCfg<H>;
     const size_t sm_rows = C::smem_rows(F), sm_cols = C::smem_cols(F);
     if (sm_rows > 48 * 1024 &&
-        cudaFuncSetAttribute(k_extract_rows<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
+        cudaFuncSetAttribute(k_extract_rows<H, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
         return TDM_ECUDA;
     if (sm_cols > 48 * 1024 &&
         cudaFuncSetAttribute(k_extract_cols<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_cols))
@@ -97,9 +97,9 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
     const size_t in_bytes = (size_t)H * H * (bits == 16 ? 2 : 1);
     for (int h0 = 0; h0 < n; h0 += chunk) {
         const int m = n - h0 < chunk ? n - h0 : chunk;
-        k_extract_rows<H><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
+        k_extract_rows<H, false><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
             static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), s.twiddle, s.scratch, F,
-            x0);
+            x0, nullptr);
         k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
             s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0, nullptr);
     }
