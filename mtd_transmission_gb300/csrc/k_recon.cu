@@ -164,11 +164,11 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 // ---------------------------------------------------------------- cap accumulation
 // One warp per voxel column (X, Y); the lanes take 32 consecutive angles at a
 // time.  An angle hits a column at most once, at one plane; lanes whose hits
-// share a plane are grouped and the group's lowest lane adds the members'
-// contributions in ascending angle order to the column's FP32 accumulator in
-// shared memory.  The sums are therefore deterministic, and hit counts exact.
-// (FP32: a column sums at most a few hundred terms, a relative error of order
-// 1e-6; FP64 adds run at a small fraction of the FP32 rate on this part.)
+// share a plane are grouped and the group's lowest lane sums the members'
+// contributions in ascending angle order (FP32, at most 32 terms, usually
+// one) and adds the sum to the plane's FP64 accumulator in shared memory, so
+// the running sum over the angles is FP64.  The sums are deterministic and
+// the hit counts exact.
 constexpr int kGW = 8;  // warps per CTA; a CTA covers 32 consecutive x at one y
 
 template <int D>
@@ -177,12 +177,12 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
              float2* __restrict__ vol, uint32_t* __restrict__ cnt_out) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int band = p.band;
-    float2* acc_all = reinterpret_cast<float2*>(smraw);                  // kGW x band
+    double2* acc_all = reinterpret_cast<double2*>(smraw);                // kGW x band
     float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);   // kGW x 32
     uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32); // kGW x band
     int2* sp = reinterpret_cast<int2*>(cnt_all + ((kGW * band + 3) & ~3));  // M
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2* acc = acc_all + w * band;
+    double2* acc = acc_all + w * band;
     uint16_t* cnt = cnt_all + w * band;
     float2* stg = stg_all + w * 32;
     for (int i = threadIdx.x; i < M; i += kGW * 32) sp[i] = posspec[i];
@@ -196,7 +196,7 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
         const int bx = X - h;  // fd + N = X - D/2 + posSpec
         const size_t koff = (size_t)(by & (F - 1)) * F + (bx & (F - 1));
         for (int e = lane; e < band; e += 32) {
-            acc[e] = make_float2(0.0f, 0.0f);
+            acc[e] = make_double2(0.0, 0.0);
             cnt[e] = 0;
         }
         __syncwarp();
@@ -225,9 +225,9 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
                     sx += u.x;
                     sy += u.y;
                 }
-                float2 t = acc[e];
-                t.x += sx;
-                t.y += sy;
+                double2 t = acc[e];
+                t.x += (double)sx;
+                t.y += (double)sy;
                 acc[e] = t;
                 cnt[e] += (uint16_t)__popc(grp);
             }
@@ -236,10 +236,10 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
         // normalise (main.cpp:243-249); (-1)^(X+Y+Z) stands for the first fftshift3D
         float2* col = vol + ((size_t)Y * D + X) * D + zmin;
         for (int e = lane; e < band; e += 32) {
-            const float2 t = acc[e];
+            const double2 t = acc[e];
             const unsigned n = cnt[e];
-            const float dn = n ? (float)n : 1.0f;
-            float2 val = make_float2(t.x / dn, t.y / dn);
+            const float dn = n ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
+            float2 val = make_float2((float)t.x / dn, (float)t.y / dn);
             if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
             col[e] = val;
             if (cnt_out) cnt_out[((size_t)(zmin + e) * D + Y) * D + X] = n;
@@ -403,7 +403,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    const size_t sm_a = (size_t)kGW * p.band * sizeof(float2) + (size_t)kGW * 32 * sizeof(float2) +
+    const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
                         (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
