@@ -39,8 +39,8 @@ METRIC = "512³ volumes/s (600 holos): plain vs batched/TV-adjoint; rel-L2≤1e-
 UNIT = "volumes/s"
 
 # Algorithmic bytes per launch unit: the compulsory input and output bytes of
-# each kernel (what it must read and write at least once).
-def algorithmic_bytes(name, acq, hits_per_angle):
+# each kernel (what it must read and write at least once, wherever it lives).
+def algorithmic_bytes(name, acq, hits_per_angle, band):
     H, F, D = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final
     L = 2 * F
     per_angle = {
@@ -59,11 +59,28 @@ def algorithmic_bytes(name, acq, hits_per_angle):
         "cap_cols": F * F * 8 + F * F * 10,
     }
     per_volume = {
-        "gather": hits_per_angle * acq.nb_holo * 10 + D ** 3 * 8 + D ** 3,
+        "gather": hits_per_angle * acq.nb_holo * 10 + band * D * D * 8,
         "ypass": 2 * D ** 3 * 8,
         "xpass": D ** 3 * 8 + 2 * D ** 3 * 4,
     }
     return per_angle, per_volume
+
+
+# DRAM bytes (read + write) per launch from one ncu capture of the kernel on
+# the 64-hologram rytov_1024 case (profiles/<kernel>_rytov_1024_64holos.md).
+# A launch of the row pass and of the Volkov passes processes 16 angles in
+# both cases; the gather's read traffic grows with the angles (scaled by
+# angles/64), its write traffic (the band planes) does not.
+def ncu_traffic_per_launch(name, acq):
+    if acq.ccd_roix != 1024 or acq.nxmax != 128 or acq.dim_final != 512:
+        return None
+    if name == "volkov_cols":
+        return 16.835072e6
+    if name == "extract_rows":
+        return 33.61408e6 + 0.312576e6
+    if name == "gather":
+        return 82.249984e6 * acq.nb_holo / 64 + 416.795648e6
+    return None
 
 
 def measured_peaks():
@@ -340,7 +357,7 @@ def main():
         # roofline of the dominant kernel
         hits = float((np.arange(-acq.nxmax, acq.nxmax)[:, None] ** 2 +
                       np.arange(-acq.nxmax, acq.nxmax)[None, :] ** 2 < acq.nxmax ** 2).sum())
-        per_angle, per_volume = algorithmic_bytes(None, acq, hits)
+        per_angle, per_volume = algorithmic_bytes(None, acq, hits, ctx.cap_planes[1])
         peak, peak_kind = measured_peaks()
         kern = {k: (t / args.steps, n / args.steps) for k, (t, n) in prof.items()}
         dom = max(kern, key=lambda k: kern[k][0]) if kern else None
@@ -352,8 +369,12 @@ def main():
             else:
                 bytes_step = per_volume.get(dom, 0)
             achieved = bytes_step / (t_step_ms / 1e3) / 1e9
+            traffic = ncu_traffic_per_launch(dom, acq)
             roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": None,
+                    "frac": round(achieved / peak, 4),
+                    "traffic": round(traffic / 1e6, 3) if traffic else None,
+                    "traffic_unit": "MB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                    "algorithmic_bytes_per_launch_mb": round(bytes_step / max(n_launch, 1) / 1e6, 3),
                     "peak_source": f"{peak_kind} hbm_gbs",
                     "launches_per_step": n_launch, "ms_per_step": round(t_step_ms, 4),
                     "algorithmic_bytes_per_step": int(bytes_step)}

@@ -160,6 +160,11 @@ int tdm_pipeline_async(tdm_ctx* ctx, const void* holos, int bits, int n, float* 
  * overlap on the GPU (other streams or threads) race. */
 int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n, float* spectra_out, void* stream);
 
+/* Planes of the D^3 spectrum that the Ewald caps can reach, [zmin, zmin +
+ * band): the gather writes only these and the z pass reads only these.
+ * Diagnostic; no counterpart in the reference. */
+int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
+
 /* Stream-ordered execution helpers. */
 int tdm_synchronize(tdm_ctx* ctx);
 void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */

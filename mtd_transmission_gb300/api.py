@@ -27,7 +27,7 @@ EXPORTS = (
     "tdm_fields", "tdm_fields_debug", "tdm_reconstruct", "tdm_pipeline", "tdm_synchronize", "tdm_stream",
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
-    "tdm_extract_noalloc", "tdm_pipeline_async",
+    "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes",
 )
 
 
@@ -87,6 +87,7 @@ def lib():
     L.tdm_reconstruct.argtypes = [P, P, P, I, P, P, P, P]
     L.tdm_pipeline.argtypes = [P, P, I, I, P, P, P, P, P]
     L.tdm_pipeline_async.argtypes = [P, P, I, I, P, P, P, P]
+    L.tdm_cap_planes.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
     L.tdm_synchronize.argtypes = [P]
     L.tdm_stream.argtypes = [P]
     L.tdm_stream.restype = P
@@ -235,6 +236,13 @@ class Context:
         n = holos.shape[0] if n is None else n
         self._check(lib().tdm_pipeline(self._h, ptr(holos), self._bits(holos), n, ptr(indice), ptr(absorption),
                                        ptr(otf), ptr(counts), ptr(posspec)), "tdm_pipeline")
+
+    @property
+    def cap_planes(self):
+        """(zmin, band): the spectrum planes the Ewald caps can reach (tdm_cap_planes)."""
+        z, b = ctypes.c_int(), ctypes.c_int()
+        self._check(lib().tdm_cap_planes(self._h, ctypes.byref(z), ctypes.byref(b)), "tdm_cap_planes")
+        return z.value, b.value
 
     def pipeline_async(self, holos, indice=None, absorption=None, otf=None, counts=None, n=None):
         """tdm_pipeline_async: queues one volume and returns; outputs are complete after synchronize().

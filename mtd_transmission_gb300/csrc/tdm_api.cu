@@ -452,6 +452,13 @@ int tdm_profile_read(tdm_ctx* c, int index, const char** name, double* total_ms,
 }
 uint64_t tdm_launch_count(const tdm_ctx* c) { return c ? c->launches : 0; }
 
+int tdm_cap_planes(const tdm_ctx* c, int* zmin, int* band) {
+    if (!c) return TDM_EINVAL;
+    if (zmin) *zmin = c->p.zmin;
+    if (band) *band = c->p.band;
+    return TDM_OK;
+}
+
 double tdm_stage_ms(const tdm_ctx* c, const char* stage) {
     if (!c || !stage) return -1;
     int a, b;
