@@ -93,7 +93,7 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -108,7 +108,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -118,7 +118,11 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self) -> dict:
+    def mark(self) -> int:
+        """Index of the next sample: samples from a mark on fall in the timed region."""
+        return len(self.lines)
+
+    def stop(self, first: int = 0, last: int = None) -> dict:
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -129,7 +133,7 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        for ln in self.lines[first:last]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
@@ -222,7 +226,7 @@ def workload_config(acq, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rytov_1024")
@@ -291,15 +295,17 @@ def main():
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     barrier()
+    s_first = sampler.mark()
     ev0.record(stream)
     for _ in range(args.steps):
         ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
     ev1.record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()
+    s_last = sampler.mark()
     ms = ev0.elapsed_time(ev1)
     launches = ctx.launch_count - launches0
-    clocks = sampler.stop()
+    clocks = sampler.stop(s_first, s_last)
     # per-kernel device times: the same K steps again with CUDA events around every launch
     prof, prof_ms = {}, 0.0
     if not args.no_profile_pass:
