@@ -145,6 +145,60 @@ int tdm_pipeline(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice
 int tdm_pipeline_async(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
                        uint8_t* otf_out, uint32_t* counts_out);
 
+/* ---- Forward operator, adjoint and regularised reconstruction ----
+ * No counterpart in the reference's built code: they are the operators of
+ * the iterative constrained reconstruction its configuration keys describe
+ * (recon.txt GERCHBERG, NB_ITER_GPS, DELTA_NMIN/MAX, KAPPA_MIN/MAX; the
+ * tomo_GPS program itself is absent).  Volumes are D^3 float32 arrays in the
+ * layout of tdm_reconstruct's outputs ([z][y][x], x fastest); x = index +
+ * i absorption.  G(x) = M_in FFT3(M_out x) / (s D^3) is the exact inverse of
+ * the reconstruction's volume stage (s its index scale, M the fftshift sign
+ * patterns); S samples each angle's Ewald-cap cells (the cells
+ * tdm_reconstruct accumulates, same geometry).  posspec: 2n ints (x values
+ * then y values, host or device) or NULL for the context's specular
+ * positions (from the last tdm_fields, tdm_pipeline or tdm_reconstruct call).
+ * Pointers may be host or device memory. */
+
+/* caps_out (n x F x F complex, FFT-bin order [angle][ky][kx], 0 outside the
+ * caps) = S G(index + i absorption); absorption may be NULL (0). */
+int tdm_forward(tdm_ctx* ctx, const float* index, const float* absorption, int n, const int32_t* posspec,
+                float* caps_out);
+
+/* Adjoint of tdm_forward: index_out + i absorption_out = G^H S^H caps (the
+ * unnormalised scatter of the cap values into their cells, then G^H);
+ * absorption_out may be NULL. */
+int tdm_adjoint(tdm_ctx* ctx, const float* caps, int n, const int32_t* posspec, float* index_out,
+                float* absorption_out);
+
+typedef struct {
+    int iterations;            /* projected-gradient iterations */
+    int init;                  /* 0: start from index_io / absorption_io; 1: from the single-pass reconstruction */
+    float step;                /* data step (1: each iteration makes the measured cells data-consistent) */
+    float tv_weight;           /* TV gradient step (0: no regularisation) */
+    float tv_eps;              /* TV smoothing: sum sqrt(|grad x|^2 + eps^2) */
+    float index_min, index_max;            /* box constraints (DELTA_NMIN, DELTA_NMAX) */
+    float absorption_min, absorption_max;  /* (KAPPA_MIN, KAPPA_MAX) */
+} tdm_tv_opts;
+
+typedef struct {
+    int iterations;            /* iterations run */
+    double misfit_first;       /* sum |S G x - caps|^2 at the first and the last iteration */
+    double misfit_last;
+    double seconds;            /* device time of the iterations */
+} tdm_tv_report;
+
+/* Regularised reconstruction: x <- clamp(x - step T(S^H (S G x - caps) / count)
+ * - tv_weight dTV(x)), T = G^-1, count the cells' hit counts (the
+ * single-pass reconstruction's normalisation as the preconditioner), the
+ * clamp the box constraints.  caps: n x F x F complex cap values, or NULL
+ * for the context's cap records (from the last tdm_pipeline or
+ * tdm_reconstruct call: the measured fields' cap contributions).  index_io
+ * (and absorption_io, or NULL to reconstruct the index alone) hold the
+ * starting volume when opts->init = 0 and receive the result, so a run can
+ * be continued from a saved iterate. */
+int tdm_tv_reconstruct(tdm_ctx* ctx, const float* caps, int n, const int32_t* posspec, const tdm_tv_opts* opts,
+                       float* index_io, float* absorption_io, tdm_tv_report* report);
+
 /* Off-axis extraction that allocates nothing.  No counterpart in the
  * reference: it is for callers that cannot allocate GPU memory, such as a
  * camera acquisition loop that must not stall on cudaMalloc between bursts of

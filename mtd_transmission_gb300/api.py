@@ -27,7 +27,8 @@ EXPORTS = (
     "tdm_fields", "tdm_fields_debug", "tdm_reconstruct", "tdm_pipeline", "tdm_synchronize", "tdm_stream",
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
-    "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes",
+    "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
+    "tdm_tv_reconstruct",
 )
 
 
@@ -65,6 +66,20 @@ class Derived(ctypes.Structure):
 _lib = None
 
 
+class TvOpts(ctypes.Structure):
+    """tdm_tv_opts."""
+    _fields_ = [("iterations", ctypes.c_int), ("init", ctypes.c_int), ("step", ctypes.c_float),
+                ("tv_weight", ctypes.c_float), ("tv_eps", ctypes.c_float), ("index_min", ctypes.c_float),
+                ("index_max", ctypes.c_float), ("absorption_min", ctypes.c_float),
+                ("absorption_max", ctypes.c_float)]
+
+
+class TvReport(ctypes.Structure):
+    """tdm_tv_report."""
+    _fields_ = [("iterations", ctypes.c_int), ("misfit_first", ctypes.c_double), ("misfit_last", ctypes.c_double),
+                ("seconds", ctypes.c_double)]
+
+
 def lib():
     """Loads libtdm.so; raises when it has not been built."""
     global _lib
@@ -87,6 +102,9 @@ def lib():
     L.tdm_reconstruct.argtypes = [P, P, P, I, P, P, P, P]
     L.tdm_pipeline.argtypes = [P, P, I, I, P, P, P, P, P]
     L.tdm_pipeline_async.argtypes = [P, P, I, I, P, P, P, P]
+    L.tdm_forward.argtypes = [P, P, P, I, P, P]
+    L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
+    L.tdm_tv_reconstruct.argtypes = [P, P, I, P, ctypes.POINTER(TvOpts), P, P, ctypes.POINTER(TvReport)]
     L.tdm_cap_planes.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
     L.tdm_synchronize.argtypes = [P]
     L.tdm_stream.argtypes = [P]
@@ -236,6 +254,39 @@ class Context:
         n = holos.shape[0] if n is None else n
         self._check(lib().tdm_pipeline(self._h, ptr(holos), self._bits(holos), n, ptr(indice), ptr(absorption),
                                        ptr(otf), ptr(counts), ptr(posspec)), "tdm_pipeline")
+
+    def forward(self, index, absorption=None, n=None, posspec=None, caps_out=None):
+        """tdm_forward: cap values S G(index + i absorption) (n x F x F complex, FFT-bin order)."""
+        F = 2 * self.geom.nxmax
+        if caps_out is None:
+            caps_out = np.zeros((n, F, F), np.complex64)
+        n = caps_out.shape[0] if n is None else n
+        self._check(lib().tdm_forward(self._h, ptr(index), ptr(absorption), n, ptr(posspec), ptr(caps_out)),
+                    "tdm_forward")
+        return caps_out
+
+    def adjoint(self, caps, n=None, posspec=None, index_out=None, absorption_out=None):
+        """tdm_adjoint: index_out + i absorption_out = G^H S^H caps."""
+        n = caps.shape[0] if n is None else n
+        D = self.geom.dim_final
+        if index_out is None:
+            index_out = np.zeros((D, D, D), np.float32)
+        self._check(lib().tdm_adjoint(self._h, ptr(caps), n, ptr(posspec), ptr(index_out), ptr(absorption_out)),
+                    "tdm_adjoint")
+        return index_out, absorption_out
+
+    def tv_reconstruct(self, index_io, absorption_io=None, caps=None, n=None, posspec=None, iterations=50,
+                       init=1, step=1.0, tv_weight=1e-3, tv_eps=1e-4, index_min=0.0, index_max=float("inf"),
+                       absorption_min=0.0, absorption_max=float("inf")):
+        """tdm_tv_reconstruct: projected-gradient TV reconstruction; returns the report as a dict."""
+        n = (caps.shape[0] if caps is not None else self.max_angles) if n is None else n
+        o = TvOpts(iterations=iterations, init=init, step=step, tv_weight=tv_weight, tv_eps=tv_eps,
+                   index_min=index_min, index_max=index_max, absorption_min=absorption_min,
+                   absorption_max=absorption_max)
+        r = TvReport()
+        self._check(lib().tdm_tv_reconstruct(self._h, ptr(caps), n, ptr(posspec), ctypes.byref(o), ptr(index_io),
+                                             ptr(absorption_io), ctypes.byref(r)), "tdm_tv_reconstruct")
+        return {f: getattr(r, f) for f, _ in TvReport._fields_}
 
     @property
     def cap_planes(self):

@@ -38,6 +38,52 @@ struct CapCfg {
     static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
+// ---------------------------------------------------------------- cap geometry
+// fzm0 of an angle (fonctions.cpp:893-899); negative when the angle is skipped.
+__device__ __forceinline__ double cap_fzm0(const Params& p, int2 ps) {
+    const int fxm0 = ps.x - p.N, fym0 = ps.y - p.N;
+    const double c = p.rayon * p.rayon - fxm0 * fxm0 - fym0 * fym0;
+    return (round(c) >= 0) ? sqrt(c) : -1.0;
+}
+
+// Plane z of the cap cell of FFT bin (kx, ky) of an angle with specular
+// position ps and height fz (fonctions.cpp:903-921), or -1 outside the NA
+// disc or for a skipped angle; *sf is sqrt(r^2 - fd^2) in float for the
+// cell's weight.  A plane outside the cap band sets *err and gives -1.
+__device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, int kx, int ky,
+                                         const double* __restrict__ s_tab, const float* __restrict__ s_tabf,
+                                         float* sf, int* __restrict__ err) {
+    const int F = p.F, N = p.N;
+    const int fdx = ((kx + ps.x) & (F - 1)) - N, fdy = ((ky + ps.y) & (F - 1)) - N;
+    if (!(fz >= 0.0) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;
+    const int ti = (fdy + N) * F + fdx + N;
+    *sf = s_tabf[ti];
+    const float d = *sf - (float)fz;
+    const float fr = d - floorf(d);
+    // round(sqrt(fdz^2) - fzm0) in FP64 (fonctions.cpp:921); the FP32 value
+    // decides unless it lies within 1e-3 of a rounding boundary.
+    const float koz = (fabsf(fr - 0.5f) > 1e-3f) ? floorf(d + 0.5f) : (float)round(s_tab[ti] - fz);
+    const int z = (int)koz + p.D / 2;
+    if (z < p.zmin || z >= p.zmin + p.band) {
+        if (err) atomicOr(err, 1);
+        return -1;
+    }
+    return z;
+}
+
+// Cap-cell weight (k0/pi)(-2pi) sdz dx^2 (-1)^(kx+ky) of retroPropag_Born
+// (fonctions.cpp:902,927) with the recentring sign of the per-field spectrum.
+__device__ __forceinline__ float cap_weight(const Params& p, float sf, int kx, int ky) {
+    const float sg = ((kx + ky) & 1) ? -p.dx2 : p.dx2;
+    return p.cap_scale * (sf * (float)p.inv_rayon) * sg;
+}
+
+// Voxel column of FFT bin kx of an angle with specular coordinate q (x or y):
+// D/2 + fd + N - q, the inverse of the gather's bin (X - D/2) mod F.
+__device__ __forceinline__ int cap_col(const Params& p, int k, int q) {
+    return p.D / 2 + ((k + q) & (p.F - 1)) - q;
+}
+
 template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, const float2* __restrict__ tw,
@@ -115,11 +161,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, kx0 = blockIdx.x * B;
     const int2 ps = posspec[a];
-    if (threadIdx.x == 0) {  // fzm0 (fonctions.cpp:893-899); negative when the angle is skipped
-        const int fxm0 = ps.x - p.N, fym0 = ps.y - p.N;
-        const double c = p.rayon * p.rayon - fxm0 * fxm0 - fym0 * fym0;
-        s_fz = (round(c) >= 0) ? sqrt(c) : -1.0;
-    }
+    if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
 #pragma unroll 8
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
@@ -129,33 +171,17 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
     fft_warp<F, -1>(sm + tr * W::STRIDE, j, tw);
     __syncthreads();
     const double fz = s_fz;
-    const float fzf = (float)fz;
-    const int N = p.N;
 #pragma unroll 2
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B, kx = kx0 + t;
         const size_t o = ((size_t)a * F + ky) * F + kx;
-        const int fdx = ((kx + ps.x) & (F - 1)) - N, fdy = ((ky + ps.y) & (F - 1)) - N;
-        int z = -1;
+        float sf = 0.f;
+        const int z = cap_plane(p, ps, fz, kx, ky, s_tab, s_tabf, &sf, err);
         float2 val = make_float2(0.f, 0.f);
-        if (fz >= 0.0 && fdx * fdx + fdy * fdy < p.disc_thr) {
-            const int ti = (fdy + N) * F + fdx + N;
-            const float sf = s_tabf[ti];
-            const float d = sf - fzf;
-            const float fr = d - floorf(d);
-            // round(sqrt(fdz^2) - fzm0) in FP64 (fonctions.cpp:921); the FP32
-            // value decides unless it lies within 1e-3 of a rounding boundary.
-            const float koz = (fabsf(fr - 0.5f) > 1e-3f) ? floorf(d + 0.5f) : (float)round(s_tab[ti] - fz);
-            z = (int)koz + p.D / 2;
-            if (z < p.zmin || z >= p.zmin + p.band) {
-                atomicOr(err, 1);
-                z = -1;
-            } else {
-                float2 v = sm[t * W::STRIDE + W::pad(ky)];
-                const float sg = ((kx + ky) & 1) ? -p.dx2 : p.dx2;
-                const float Bc = p.cap_scale * (sf * (float)p.inv_rayon) * sg;  // (k0/pi)(-2pi) sdz dx^2 (+-1)
-                val = make_float2(-Bc * v.y, Bc * v.x);
-            }
+        if (z >= 0) {
+            const float2 v = sm[t * W::STRIDE + W::pad(ky)];
+            const float Bc = cap_weight(p, sf, kx, ky);
+            val = make_float2(-Bc * v.y, Bc * v.x);
         }
         rec[o] = make_float4(val.x, val.y, __int_as_float(z), 0.f);
     }
@@ -174,7 +200,7 @@ constexpr int kGW = 8;  // warps per CTA; a CTA covers 32 consecutive x at one y
 template <int D>
 __global__ void __launch_bounds__(kGW * 32)
 k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, int M, Params p,
-             float2* __restrict__ vol, uint32_t* __restrict__ cnt_out) {
+             float2* __restrict__ vol, uint32_t* __restrict__ cnt_out, int normalize) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int band = p.band;
     double2* acc_all = reinterpret_cast<double2*>(smraw);                // kGW x band
@@ -233,12 +259,13 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
             }
             __syncwarp();
         }
-        // normalise (main.cpp:243-249); (-1)^(X+Y+Z) stands for the first fftshift3D
+        // normalise (main.cpp:243-249; not for the adjoint scatter); (-1)^(X+Y+Z)
+        // stands for the first fftshift3D
         float2* col = vol + ((size_t)Y * D + X) * D + zmin;
         for (int e = lane; e < band; e += 32) {
             const double2 t = acc[e];
             const unsigned n = cnt[e];
-            const float dn = n ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
+            const float dn = (n && normalize) ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
             float2 val = make_float2((float)t.x / dn, (float)t.y / dn);
             if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
             col[e] = val;
@@ -301,7 +328,7 @@ k_zpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int b
 }
 
 // Inverse FFT along y, in place, for B consecutive z at fixed x.
-template <int D>
+template <int D, int DIR>
 __global__ void __launch_bounds__(PassCfg<D>::NT)
 k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
     using C = PassCfg<D>;
@@ -316,7 +343,7 @@ k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
         sm[t * W::STRIDE + W::pad(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
     }
     __syncthreads();
-    fft_warp<D, +1>(sm + tr * W::STRIDE, j, tw);
+    fft_warp<D, DIR>(sm + tr * W::STRIDE, j, tw);
     __syncthreads();
 #pragma unroll 8
     for (int r = 0; r < B * D / NT; ++r) {
@@ -354,6 +381,189 @@ k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float sca
         const size_t o = ((size_t)Z * D + Y) * D + X;
         if (re) re[o] = v.x * sg;
         if (im) im[o] = v.y * sg;
+    }
+}
+
+// ---------------------------------------------------------------- forward operator and adjoint
+// With the unknown volume x = index + i absorption ([z][y][x], x fastest) and
+// s = out_scale, the volume stage above is x = T(V) = s M_out IFFT3(M_in V)
+// (unnormalised IFFT, M the fftshift sign patterns).  The forward operator
+// is A = S G with G = T^-1 = M_in FFT3(M_out x) / (s D^3) and S the sampling
+// of each angle's cap cells (the cells the gather fills, same geometry); its
+// adjoint is A^H = G^H S^H, G^H = M_out IFFT3(M_in .) / (s D^3) and S^H the
+// unnormalised scatter, i.e. k_accumulate without the division by the hit
+// count followed by the z, y and x passes with scale 1 / (s D^3).
+
+// Forward x pass: FFT along x of B consecutive z rows at fixed y of the
+// index/absorption volumes (x M_out x scale), into the [y][x][z] spectrum.
+template <int D>
+__global__ void __launch_bounds__(PassCfg<D>::NT)
+k_fxpass(const float* __restrict__ re, const float* __restrict__ im, const float2* __restrict__ tw, float scale,
+         float2* __restrict__ vol) {
+    using C = PassCfg<D>;
+    using W = typename C::W;
+    constexpr int B = C::B, NT = C::NT;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
+    const int z0 = blockIdx.x * B, Y = blockIdx.y;
+    const int par = (3 * (D / 2)) & 1;
+#pragma unroll 8
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i / D, X = i % D, Z = z0 + t;
+        const size_t o = ((size_t)Z * D + Y) * D + X;
+        const float sg = ((X + Y + Z + par) & 1) ? -scale : scale;
+        sm[t * W::STRIDE + W::pad(X)] = make_float2(re[o] * sg, im ? im[o] * sg : 0.0f);
+    }
+    __syncthreads();
+    fft_warp<D, -1>(sm + tr * W::STRIDE, j, tw);
+    __syncthreads();
+#pragma unroll 8
+    for (int r = 0; r < B * D / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % B, X = i / B;
+        vol[((size_t)Y * D + X) * D + z0 + t] = sm[t * W::STRIDE + W::pad(X)];
+    }
+}
+
+// Forward z pass: FFT along z of B columns (all planes in), x M_in, only the
+// cap band written (the sampling reads nothing else).
+template <int D>
+__global__ void __launch_bounds__(PassCfg<D>::NT)
+k_fzpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int band) {
+    using C = PassCfg<D>;
+    using W = typename C::W;
+    constexpr int B = C::B, T = W::T, E = W::E;
+    extern __shared__ float2 sm[];
+    const int t = threadIdx.x / T, j = threadIdx.x % T;
+    const size_t c = (size_t)blockIdx.x * B + t;  // y * D + x
+    const int XY = (int)(c % D) + (int)(c / D);
+    float2* col = vol + c * D;
+    float2 x[E];
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) x[n1] = col[j + n1 * T];
+    fft_warp_regs<D, -1>(x, sm + t * W::STRIDE, j, tw);
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) {
+            const int Z = j + q * T + E * k2;
+            if (Z >= zmin && Z < zmin + band) {
+                const float2 v = x[q * T + k2];
+                col[Z] = ((XY + Z) & 1) ? make_float2(-v.x, -v.y) : v;
+            }
+        }
+    }
+}
+
+// Cap values of the spectrum: for each angle and FFT bin, the spectrum at its
+// cap cell (0 outside the cap).  With data (cap records of measured values),
+// the residual spectrum - data on the data's cells, as cap records, and the
+// misfit sum |residual|^2 added to *misfit.
+__global__ void __launch_bounds__(256)
+k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, Params p,
+             const double* __restrict__ s_tab, const float* __restrict__ s_tabf, const float4* __restrict__ data,
+             float2* __restrict__ caps, float4* __restrict__ res, double* __restrict__ misfit, int* __restrict__ err) {
+    const int a = blockIdx.y, F = p.F, D = p.D;
+    const int2 ps = posspec[a];
+    __shared__ double s_fz;
+    __shared__ double red[8];
+    if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
+    __syncthreads();
+    double m2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F * F; i += gridDim.x * blockDim.x) {
+        const int kx = i % F, ky = i / F;
+        const size_t o = (size_t)a * F * F + i;
+        int z;
+        float2 d = make_float2(0.f, 0.f);
+        if (data) {
+            const float4 r = data[o];
+            z = __float_as_int(r.z);
+            d = make_float2(r.x, r.y);
+        } else {
+            float sf;
+            z = cap_plane(p, ps, s_fz, kx, ky, s_tab, s_tabf, &sf, err);
+        }
+        float2 v = make_float2(0.f, 0.f);
+        if (z >= 0) {
+            const int X = cap_col(p, kx, ps.x), Y = cap_col(p, ky, ps.y);
+            v = vol[((size_t)Y * D + X) * D + z];
+            v = make_float2(v.x - d.x, v.y - d.y);
+            m2 += (double)v.x * v.x + (double)v.y * v.y;
+        }
+        if (caps) caps[o] = v;
+        if (res) res[o] = make_float4(v.x, v.y, __int_as_float(z), 0.f);
+    }
+    if (misfit) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) m2 += __shfl_down_sync(0xffffffffu, m2, off);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+            atomicAdd(misfit, t);
+        }
+    }
+}
+
+// Cap records (value, cell plane) of given cap values, for the scatter.
+__global__ void __launch_bounds__(256)
+k_cap_pack(const float2* __restrict__ caps, const int2* __restrict__ posspec, Params p,
+           const double* __restrict__ s_tab, const float* __restrict__ s_tabf, float4* __restrict__ rec,
+           int* __restrict__ err) {
+    const int a = blockIdx.y, F = p.F;
+    const int2 ps = posspec[a];
+    __shared__ double s_fz;
+    if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F * F; i += gridDim.x * blockDim.x) {
+        const size_t o = (size_t)a * F * F + i;
+        float sf;
+        const int z = cap_plane(p, ps, s_fz, i % F, i / F, s_tab, s_tabf, &sf, err);
+        const float2 v = z >= 0 ? caps[o] : make_float2(0.f, 0.f);
+        rec[o] = make_float4(v.x, v.y, __int_as_float(z), 0.f);
+    }
+}
+
+// One projected-gradient step of the regularised reconstruction, per voxel of
+// the [z][y][x] volumes: x <- clamp(x - step g - step_tv tv_weight dTV(x)),
+// for the index (real part) and, when present, the absorption.  TV is the
+// isotropic total variation with forward differences (zero across the far
+// faces) smoothed by eps: sum sqrt(|grad x|^2 + eps^2).
+__device__ __forceinline__ float tv_grad(const float* __restrict__ x, int D, int X, int Y, int Z, float eps2) {
+    const size_t sy = D, sz = (size_t)D * D;
+    auto at = [&](int x_, int y_, int z_) { return x[(size_t)z_ * sz + (size_t)y_ * sy + x_]; };
+    // gradient of the cell anchored at (x_, y_, z_) and its norm
+    auto cell = [&](int x_, int y_, int z_, float& gx, float& gy, float& gz) {
+        const float c = at(x_, y_, z_);
+        gx = x_ + 1 < D ? at(x_ + 1, y_, z_) - c : 0.0f;
+        gy = y_ + 1 < D ? at(x_, y_ + 1, z_) - c : 0.0f;
+        gz = z_ + 1 < D ? at(x_, y_, z_ + 1) - c : 0.0f;
+        return rsqrtf(gx * gx + gy * gy + gz * gz + eps2);
+    };
+    float gx, gy, gz;
+    float inv = cell(X, Y, Z, gx, gy, gz);
+    float g = -(gx + gy + gz) * inv;
+    if (X > 0) { inv = cell(X - 1, Y, Z, gx, gy, gz); g += gx * inv; }
+    if (Y > 0) { inv = cell(X, Y - 1, Z, gx, gy, gz); g += gy * inv; }
+    if (Z > 0) { inv = cell(X, Y, Z - 1, gx, gy, gz); g += gz * inv; }
+    return g;
+}
+
+__global__ void __launch_bounds__(256)
+k_tv_step(const float* __restrict__ xn, const float* __restrict__ xk, const float* __restrict__ gn,
+          const float* __restrict__ gk, int D, float step, float tv_step, float eps2, float nlo, float nhi, float klo,
+          float khi, float* __restrict__ xn_out, float* __restrict__ xk_out) {
+    const size_t total = (size_t)D * D * D;
+    for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < total; v += (size_t)gridDim.x * blockDim.x) {
+        const int X = (int)(v % D), Y = (int)((v / D) % D), Z = (int)(v / ((size_t)D * D));
+        float a = xn[v] - step * gn[v];
+        if (tv_step != 0.0f) a -= tv_step * tv_grad(xn, D, X, Y, Z, eps2);
+        xn_out[v] = fminf(fmaxf(a, nlo), nhi);
+        if (xk) {
+            float b = xk[v] - step * gk[v];
+            if (tv_step != 0.0f) b -= tv_step * tv_grad(xk, D, X, Y, Z, eps2);
+            xk_out[v] = fminf(fmaxf(b, klo), khi);
+        }
     }
 }
 
@@ -407,7 +617,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
                         (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
-    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D>, sm_p) ||
+    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
     const bool host_out = out.host_re || out.host_im || out.host_otf || out.host_cnt;
@@ -421,7 +631,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     cudaEventRecord(c->ev_stage[4], c->stream);
     {
         Launch l(c, K_GATHER);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(b.rec, b.posspec, n, p, b.vol, cnt);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(b.rec, b.posspec, n, p, b.vol, cnt, 1);
     }
     cudaEventRecord(c->ev_stage[5], c->stream);
     const size_t NT = (size_t)D * D * D;
@@ -440,7 +650,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     }
     {
         Launch l(c, K_YPASS);
-        k_ypass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
+        k_ypass<D, 1><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
     }
     // x pass by slabs of z blocks; a slab's planes are final once it has run
     const bool host_vol = out.host_re || out.host_im;
@@ -469,6 +679,70 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
+template <int D>
+int forward_impl(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float4* data, float4* res,
+                 double* misfit) {
+    using P = PassCfg<D>;
+    Buffers& b = c->b;
+    const Params& p = c->p;
+    const size_t sm_p = P::SMEM;
+    if (allow_smem(k_fxpass<D>, sm_p) || allow_smem(k_ypass<D, -1>, sm_p) || allow_smem(k_fzpass<D>, sm_p))
+        return TDM_ECUDA;
+    const float scale = (float)(1.0 / ((double)p.out_scale * (double)D * D * D));
+    {
+        Launch l(c, K_XPASS);
+        k_fxpass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(xn, xk, b.tw, scale, b.vol);
+    }
+    {
+        Launch l(c, K_YPASS);
+        k_ypass<D, -1><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
+    }
+    {
+        Launch l(c, K_ZPASS);
+        k_fzpass<D><<<dim3(D * D / P::B), P::NT, sm_p, c->stream>>>(b.vol, b.tw, p.zmin, p.band);
+    }
+    {
+        Launch l(c, K_CAP_COLS);
+        const int per = (p.F * p.F + 255) / 256;
+        k_cap_sample<<<dim3(per < 16 ? per : 16, n), 256, 0, c->stream>>>(b.vol, b.posspec, p, b.s_tab, b.s_tabf, data,
+                                                                          caps, res, misfit, b.err);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+template <int D>
+int adjoint_impl(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bool normalize) {
+    using P = PassCfg<D>;
+    Buffers& b = c->b;
+    const Params& p = c->p;
+    const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
+                        (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
+    const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
+    if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
+    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
+        allow_smem(k_xpass<D>, sm_p))
+        return TDM_ECUDA;
+    {
+        Launch l(c, K_GATHER);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(recs, b.posspec, n, p, b.vol, nullptr,
+                                                                         normalize ? 1 : 0);
+    }
+    {
+        Launch l(c, K_ZPASS);
+        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, c->stream>>>(b.vol, b.tw, p.zmin, p.band, nullptr);
+    }
+    {
+        Launch l(c, K_YPASS);
+        k_ypass<D, 1><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
+    }
+    const float scale = normalize ? p.out_scale : (float)(1.0 / ((double)p.out_scale * (double)D * D * D));
+    {
+        Launch l(c, K_XPASS);
+        k_xpass<D><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw, scale, 0, xn, xk);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
 }  // namespace
 
 int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
@@ -489,6 +763,48 @@ int launch_volume(tdm_ctx* c, int n, const VolumeOut& out) {
         case 1024: return volume_impl<1024>(c, n, out);
         default: return TDM_EUNSUPPORTED;
     }
+}
+
+int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float4* data,
+                   float4* res, double* misfit) {
+    switch (c->p.D) {
+        case 128: return forward_impl<128>(c, xn, xk, n, caps, data, res, misfit);
+        case 256: return forward_impl<256>(c, xn, xk, n, caps, data, res, misfit);
+        case 512: return forward_impl<512>(c, xn, xk, n, caps, data, res, misfit);
+        case 1024: return forward_impl<1024>(c, xn, xk, n, caps, data, res, misfit);
+        default: return TDM_EUNSUPPORTED;
+    }
+}
+
+int launch_adjoint(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bool normalize) {
+    switch (c->p.D) {
+        case 128: return adjoint_impl<128>(c, recs, n, xn, xk, normalize);
+        case 256: return adjoint_impl<256>(c, recs, n, xn, xk, normalize);
+        case 512: return adjoint_impl<512>(c, recs, n, xn, xk, normalize);
+        case 1024: return adjoint_impl<1024>(c, recs, n, xn, xk, normalize);
+        default: return TDM_EUNSUPPORTED;
+    }
+}
+
+int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float4* recs) {
+    const int per = (c->p.F * c->p.F + 255) / 256;
+    {
+        Launch l(c, K_CAP_COLS);
+        k_cap_pack<<<dim3(per < 16 ? per : 16, n), 256, 0, c->stream>>>(caps, c->b.posspec, c->p, c->b.s_tab,
+                                                                        c->b.s_tabf, recs, c->b.err);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
+                   float tv_step, float eps, float nlo, float nhi, float klo, float khi, float* xn_out, float* xk_out) {
+    const int D = c->p.D;
+    {
+        Launch l(c, K_FORM);
+        k_tv_step<<<152 * 8, 256, 0, c->stream>>>(xn, xk, gn, gk, D, step, tv_step, eps * eps, nlo, nhi, klo, khi,
+                                                   xn_out, xk_out);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
 }  // namespace tdm

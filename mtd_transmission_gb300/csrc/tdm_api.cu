@@ -80,7 +80,8 @@ void free_all(tdm_ctx* c) {
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec, b.vol, b.out_re, b.out_im, b.out_otf,
-                    b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err};
+                    b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
+                    b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = Buffers{};
@@ -594,6 +595,24 @@ static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t
     return host && wait ? tdm_synchronize(c) : TDM_OK;
 }
 
+// Specular positions (x values then y values) into b.posspec.
+static int set_posspec(tdm_ctx* c, const int32_t* posspec_in, int n, const char* who) {
+    if (is_device_ptr(posspec_in)) {
+        Launch l(c, K_POSSPEC);
+        k_pack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(posspec_in, n, c->b.posspec);
+        return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+    }
+    std::vector<int2> tmp(n);
+    for (int a = 0; a < n; ++a) {
+        if (posspec_in[a] < 0 || posspec_in[a] >= c->p.F || posspec_in[n + a] < 0 || posspec_in[n + a] >= c->p.F)
+            return fail(c, TDM_EINVAL, std::string(who) + ": specular position outside the field");
+        tmp[a] = make_int2(posspec_in[a], posspec_in[n + a]);
+    }
+    TDM_CU(cudaMemcpyAsync(c->b.posspec, tmp.data(), n * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+    TDM_CU(cudaStreamSynchronize(c->stream));
+    return TDM_OK;
+}
+
 int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_in, int n, float* indice_out,
                     float* absorption_out, uint8_t* otf_out, uint32_t* counts_out) {
     if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, "tdm_reconstruct: invalid argument");
@@ -604,23 +623,13 @@ int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_i
     if (fields_in && fields_in != reinterpret_cast<const float*>(c->b.fields))
         TDM_CU(cudaMemcpyAsync(c->b.fields, fields_in, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
     if (posspec_in) {
-        if (is_device_ptr(posspec_in)) {
-            Launch l(c, K_POSSPEC);
-            k_pack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(posspec_in, n, c->b.posspec);
-        } else {
-            std::vector<int2> tmp(n);
-            for (int a = 0; a < n; ++a) {
-                if (posspec_in[a] < 0 || posspec_in[a] >= c->p.F || posspec_in[n + a] < 0 || posspec_in[n + a] >= c->p.F)
-                    return fail(c, TDM_EINVAL, "tdm_reconstruct: specular position outside the field");
-                tmp[a] = make_int2(posspec_in[a], posspec_in[n + a]);
-            }
-            TDM_CU(cudaMemcpyAsync(c->b.posspec, tmp.data(), n * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
-            TDM_CU(cudaStreamSynchronize(c->stream));
-        }
+        if (int rc = set_posspec(c, posspec_in, n, "tdm_reconstruct")) return rc;
+        c->n_fields = std::max(c->n_fields, n);
     }
     TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
     int rc = run_volume(c, n, true, indice_out, absorption_out, otf_out, counts_out);
     if (rc) return rc;
+    c->n_caps = n;
     if (fields_in && !is_device_ptr(fields_in)) return tdm_synchronize(c);
     return TDM_OK;
 }
@@ -670,6 +679,7 @@ static int pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indic
     TDM_CU(cudaEventRecord(c->ev_stage[2], c->stream));
     c->n_spectra = n;
     c->n_fields = n;
+    c->n_caps = n;
     if (posspec_out && is_device_ptr(posspec_out)) {
         Launch l(c, K_POSSPEC);
         k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
@@ -697,6 +707,149 @@ int tdm_pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indice_o
 int tdm_pipeline_async(tdm_ctx* c, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
                        uint8_t* otf_out, uint32_t* counts_out) {
     return pipeline(c, holos, bits, n, indice_out, absorption_out, otf_out, counts_out, nullptr, false);
+}
+
+// ---------------------------------------------------------------- forward operator, adjoint, regularised reconstruction
+static int ensure_operator_buffers(tdm_ctx* c) {
+    const size_t NT = (size_t)c->p.D * c->p.D * c->p.D, MF = (size_t)c->max_angles * c->p.F * c->p.F;
+    for (auto& v : c->b.xv)
+        if (!v && dev_alloc(c, &v, NT)) return TDM_ENOMEM;
+    if (!c->b.caps && dev_alloc(c, &c->b.caps, MF)) return TDM_ENOMEM;
+    if (!c->b.rec2 && dev_alloc(c, &c->b.rec2, MF)) return TDM_ENOMEM;
+    if (!c->b.misfit && dev_alloc(c, &c->b.misfit, 1)) return TDM_ENOMEM;
+    return TDM_OK;
+}
+
+static int operator_setup(tdm_ctx* c, int n, const int32_t* posspec, const char* who) {
+    if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, std::string(who) + ": invalid argument");
+    cudaSetDevice(c->device);
+    if (posspec) {
+        if (int rc = set_posspec(c, posspec, n, who)) return rc;
+        c->n_fields = std::max(c->n_fields, n);
+    } else if (n > c->n_fields) {
+        return fail(c, TDM_EINVAL, std::string(who) + ": no specular positions for that many angles in the context");
+    }
+    if (ensure_operator_buffers(c)) return fail(c, TDM_ENOMEM, std::string(who) + ": buffer allocation failed");
+    return TDM_OK;
+}
+
+int tdm_forward(tdm_ctx* c, const float* index, const float* absorption, int n, const int32_t* posspec,
+                float* caps_out) {
+    if (!index || !caps_out) return fail(c, TDM_EINVAL, "tdm_forward: invalid argument");
+    if (int rc = operator_setup(c, n, posspec, "tdm_forward")) return rc;
+    const size_t NT = (size_t)c->p.D * c->p.D * c->p.D, FF = (size_t)c->p.F * c->p.F;
+    const float* xn = index;
+    const float* xk = absorption;
+    if (!is_device_ptr(xn)) {
+        TDM_CU(cudaMemcpyAsync(c->b.xv[0], xn, NT * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        xn = c->b.xv[0];
+    }
+    if (xk && !is_device_ptr(xk)) {
+        TDM_CU(cudaMemcpyAsync(c->b.xv[1], xk, NT * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        xk = c->b.xv[1];
+    }
+    const bool host_out = !is_device_ptr(caps_out);
+    float2* caps = host_out ? c->b.caps : reinterpret_cast<float2*>(caps_out);
+    if (int rc = launch_forward(c, xn, xk, n, caps, nullptr, nullptr, nullptr))
+        return fail(c, rc, "tdm_forward: launch failed");
+    if (host_out)
+        TDM_CU(cudaMemcpyAsync(caps_out, caps, n * FF * sizeof(float2), cudaMemcpyDeviceToHost, c->stream));
+    const bool host = host_out || !is_device_ptr(index) || (absorption && !is_device_ptr(absorption));
+    return host ? tdm_synchronize(c) : TDM_OK;
+}
+
+int tdm_adjoint(tdm_ctx* c, const float* caps, int n, const int32_t* posspec, float* index_out,
+                float* absorption_out) {
+    if (!caps || !index_out) return fail(c, TDM_EINVAL, "tdm_adjoint: invalid argument");
+    if (int rc = operator_setup(c, n, posspec, "tdm_adjoint")) return rc;
+    const size_t NT = (size_t)c->p.D * c->p.D * c->p.D, FF = (size_t)c->p.F * c->p.F;
+    const float2* cv = reinterpret_cast<const float2*>(caps);
+    if (!is_device_ptr(caps)) {
+        TDM_CU(cudaMemcpyAsync(c->b.caps, caps, n * FF * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+        cv = c->b.caps;
+    }
+    float* xn = is_device_ptr(index_out) ? index_out : c->b.xv[4];
+    float* xk = absorption_out ? (is_device_ptr(absorption_out) ? absorption_out : c->b.xv[5]) : nullptr;
+    if (int rc = launch_cap_pack(c, cv, n, c->b.rec2)) return fail(c, rc, "tdm_adjoint: launch failed");
+    if (int rc = launch_adjoint(c, c->b.rec2, n, xn, xk, false)) return fail(c, rc, "tdm_adjoint: launch failed");
+    bool host = !is_device_ptr(caps);
+    if (xn != index_out) {
+        TDM_CU(cudaMemcpyAsync(index_out, xn, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        host = true;
+    }
+    if (xk && xk != absorption_out) {
+        TDM_CU(cudaMemcpyAsync(absorption_out, xk, NT * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        host = true;
+    }
+    return host ? tdm_synchronize(c) : TDM_OK;
+}
+
+int tdm_tv_reconstruct(tdm_ctx* c, const float* caps, int n, const int32_t* posspec, const tdm_tv_opts* o,
+                       float* index_io, float* absorption_io, tdm_tv_report* report) {
+    if (!o || !index_io || o->iterations < 0) return fail(c, TDM_EINVAL, "tdm_tv_reconstruct: invalid argument");
+    if (int rc = operator_setup(c, n, posspec, "tdm_tv_reconstruct")) return rc;
+    Buffers& b = c->b;
+    const size_t NT = (size_t)c->p.D * c->p.D * c->p.D, FF = (size_t)c->p.F * c->p.F;
+    if (caps) {  // the data: cap records of the given cap values
+        const float2* cv = reinterpret_cast<const float2*>(caps);
+        if (!is_device_ptr(caps)) {
+            TDM_CU(cudaMemcpyAsync(b.caps, caps, n * FF * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+            cv = b.caps;
+        }
+        if (int rc = launch_cap_pack(c, cv, n, b.rec)) return fail(c, rc, "tdm_tv_reconstruct: launch failed");
+        c->n_caps = n;
+    } else if (n > c->n_caps) {
+        return fail(c, TDM_EINVAL, "tdm_tv_reconstruct: no cap records for that many angles in the context");
+    }
+    const bool absn = absorption_io != nullptr;
+    float* xn = b.xv[0];
+    float* xk = absn ? b.xv[1] : nullptr;
+    float* xn2 = b.xv[2];
+    float* xk2 = absn ? b.xv[3] : nullptr;
+    float* gn = b.xv[4];
+    float* gk = absn ? b.xv[5] : nullptr;
+    if (o->init == 1) {
+        if (int rc = launch_adjoint(c, b.rec, n, xn, xk, true)) return fail(c, rc, "tdm_tv_reconstruct: launch failed");
+    } else {
+        TDM_CU(cudaMemcpyAsync(xn, index_io, NT * sizeof(float), cudaMemcpyDefault, c->stream));
+        if (absn) TDM_CU(cudaMemcpyAsync(xk, absorption_io, NT * sizeof(float), cudaMemcpyDefault, c->stream));
+    }
+    cudaEvent_t t0 = prof_event(c), t1 = prof_event(c);
+    TDM_CU(cudaEventRecord(t0, c->stream));
+    double first = -1, last = -1;
+    for (int it = 0; it < o->iterations; ++it) {
+        TDM_CU(cudaMemsetAsync(b.misfit, 0, sizeof(double), c->stream));
+        if (int rc = launch_forward(c, xn, xk, n, nullptr, b.rec, b.rec2, b.misfit))
+            return fail(c, rc, "tdm_tv_reconstruct: launch failed");
+        if (it == 0 || it == o->iterations - 1) {
+            double m = 0;
+            TDM_CU(cudaMemcpyAsync(&m, b.misfit, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+            TDM_CU(cudaStreamSynchronize(c->stream));
+            (it == 0 ? first : last) = m;
+            if (o->iterations == 1) last = m;
+        }
+        if (int rc = launch_adjoint(c, b.rec2, n, gn, gk, true)) return fail(c, rc, "tdm_tv_reconstruct: launch failed");
+        if (int rc = launch_tv_step(c, xn, xk, gn, gk, o->step, o->tv_weight, o->tv_eps, o->index_min, o->index_max,
+                                    o->absorption_min, o->absorption_max, xn2, xk2))
+            return fail(c, rc, "tdm_tv_reconstruct: launch failed");
+        std::swap(xn, xn2);
+        std::swap(xk, xk2);
+    }
+    TDM_CU(cudaEventRecord(t1, c->stream));
+    TDM_CU(cudaMemcpyAsync(index_io, xn, NT * sizeof(float), cudaMemcpyDefault, c->stream));
+    if (absn) TDM_CU(cudaMemcpyAsync(absorption_io, xk, NT * sizeof(float), cudaMemcpyDefault, c->stream));
+    if (int rc = tdm_synchronize(c)) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    c->ev_pool.push_back(t0);
+    c->ev_pool.push_back(t1);
+    if (report) {
+        report->iterations = o->iterations;
+        report->misfit_first = first;
+        report->misfit_last = last;
+        report->seconds = ms / 1e3;
+    }
+    return TDM_OK;
 }
 
 }  // extern "C"

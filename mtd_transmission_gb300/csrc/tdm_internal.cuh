@@ -65,6 +65,11 @@ struct Buffers {
     float* samp_q = nullptr;       // nsamp x kNC orthonormal basis values
     double* rinv = nullptr;        // kNC x kNC: monomial coefficients from basis coefficients
     int* err = nullptr;            // device error flags
+    // forward operator / adjoint / regularised reconstruction (allocated on first use)
+    float* xv[6] = {};             // D^3 each: iterate index/absorption (x2, double buffered), gradient index/absorption
+    float2* caps = nullptr;        // max_angles x F*F cap values staged for host callers
+    float4* rec2 = nullptr;        // max_angles x F*F residual / adjoint-input cap records
+    double* misfit = nullptr;      // data misfit accumulator
 };
 
 // Kernel names for the opt-in per-launch profiler (tdm_profile).
@@ -94,6 +99,7 @@ struct tdm_ctx {
     int device = 0;
     int n_fields = 0;            // angles held in b.fields / b.posspec
     int n_spectra = 0;           // angles held in b.spectra
+    int n_caps = 0;              // angles held in b.rec (cap records)
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // hologram uploads
     cudaStream_t dl_stream = nullptr;    // output downloads (a second copy engine)
@@ -160,6 +166,21 @@ struct VolumeOut {
     uint8_t* host_otf = nullptr;
     uint32_t* host_cnt = nullptr;
 };
+// Forward operator of the cap mapping on the D^3 volumes xn + i xk ([z][y][x];
+// xk may be null): caps (n x F^2, may be null) = the spectrum at each angle's
+// cap cells; with data (cap records), res = spectrum - data on the data's
+// cells and *misfit += sum |res|^2.  Uses b.vol.
+int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float4* data,
+                   float4* res, double* misfit);
+// Adjoint of the forward operator applied to cap records (unnormalised
+// scatter, z/y/x passes); with normalize, the hit-count-normalised scatter and
+// the reconstruction's own scale (the single-pass reconstruction of recs).
+int launch_adjoint(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bool normalize);
+// Cap records (value, cell plane) of cap values in FFT-bin order.
+int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float4* recs);
+// One projected-gradient step with the TV gradient and box constraints.
+int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
+                   float tv_step, float eps, float nlo, float nhi, float klo, float khi, float* xn_out, float* xk_out);
 // gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs.
 // Downloads run on c->dl_stream and end with c->ev_dl_done; the staging
 // buffers are not written before the previous volume's downloads are done.

@@ -213,3 +213,83 @@ def reconstruction(fields_: np.ndarray, posspec: np.ndarray, cfg: Config, want_c
 
 def set_threads(n: int) -> int:
     return int(lib().orc_set_threads(n))
+
+
+# ---------------------------------------------------------------- forward operator and adjoint
+# The volume stage of the reconstruction is x = T(V) = s shift3(IFFT3(shift3(V)))
+# with s = delta_f^3 * (-1 / (2 n0 k_v^2)) (Reconstruction/main.cpp:282-352) and
+# IFFT3 unnormalised.  The forward operator samples G(x) = T^-1(x) at every
+# angle's cap cells, the cells retroPropag_Born accumulates
+# (Reconstruction/src/fonctions.cpp:903-925); cap values are indexed by the
+# per-field FFT bin (kx, ky), the bin of cell fd being ((fd + N) - posSpec) mod F.
+
+def _round_half_away(v):
+    return np.sign(v) * np.floor(np.abs(v) + 0.5)
+
+
+def volume_scale(cfg: Config) -> float:
+    dv = derive(cfg)
+    k_v = 2 * np.pi / float(np.float32(cfg.lambda0))
+    return dv["delta_f"] ** 3 * (-1.0 / (2 * float(np.float32(cfg.n0)) * k_v * k_v))
+
+
+def cap_cells(posspec: np.ndarray, cfg: Config):
+    """Per angle: (mask over the F x F bins [ky][kx], Z, Y, X cell indices) or None when skipped."""
+    N, D = cfg.nxmax, cfg.dim_final
+    F, dec = 2 * N, D // 2
+    rayon = derive(cfg)["rayon"]
+    M = len(posspec) // 2
+    ky, kx = np.meshgrid(np.arange(F), np.arange(F), indexing="ij")
+    coef = float(np.float32(cfg.coef_na_obj_limit))
+    out = []
+    for a in range(M):
+        px, py = int(posspec[a]), int(posspec[M + a])
+        fxm0, fym0 = px - N, py - N
+        c = rayon * rayon - fxm0 * fxm0 - fym0 * fym0
+        if _round_half_away(c) < 0:
+            out.append(None)
+            continue
+        fzm0 = np.sqrt(c)
+        fdx = ((kx + px) % F) - N
+        fdy = ((ky + py) % F) - N
+        inside = fdx * fdx + fdy * fdy < coef * N * N
+        s2 = np.where(inside, rayon * rayon - fdx * fdx - fdy * fdy, 0.0)
+        koz = _round_half_away(np.sqrt(s2) - fzm0)
+        X = -fxm0 + fdx + dec
+        Y = -fym0 + fdy + dec
+        Z = (koz + dec).astype(np.int64)
+        out.append((inside, Z[inside], Y[inside], X[inside]))
+    return out
+
+
+def _shift3(v):
+    return np.fft.fftshift(v)
+
+
+def forward_caps(index: np.ndarray, absorption: np.ndarray | None, posspec: np.ndarray, cfg: Config) -> np.ndarray:
+    """Cap values S G(index + i absorption), n x F x F complex in FFT-bin order."""
+    D, F = cfg.dim_final, 2 * cfg.nxmax
+    x = index.astype(np.complex128)
+    if absorption is not None:
+        x = x + 1j * absorption
+    G = _shift3(np.fft.fftn(_shift3(x))) / (volume_scale(cfg) * D ** 3)
+    cells = cap_cells(posspec, cfg)
+    caps = np.zeros((len(cells), F, F), np.complex128)
+    for a, cell in enumerate(cells):
+        if cell is None:
+            continue
+        inside, Z, Y, X = cell
+        caps[a][inside] = G[Z, Y, X]
+    return caps
+
+
+def adjoint_caps(caps: np.ndarray, posspec: np.ndarray, cfg: Config) -> np.ndarray:
+    """G^H S^H caps as a complex volume (index = real part, absorption = imaginary part)."""
+    D = cfg.dim_final
+    V = np.zeros((D, D, D), np.complex128)
+    for a, cell in enumerate(cap_cells(posspec, cfg)):
+        if cell is None:
+            continue
+        inside, Z, Y, X = cell
+        np.add.at(V, (Z, Y, X), caps[a][inside])
+    return _shift3(np.fft.ifftn(_shift3(V)) * D ** 3) / (volume_scale(cfg) * D ** 3)

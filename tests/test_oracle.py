@@ -144,3 +144,25 @@ def test_extraction_of_a_plane_wave():
     spec = oracle.extract(holo, oracle_cfg(acq))
     k = oracle.coord_spec(spec)
     assert (k % (2 * N), k // (2 * N)) == (N + tx, N + ty)
+
+
+def test_oracle_forward_adjoint_pair():
+    """The oracle's cap forward operator and adjoint are adjoint (dot-product
+    test in FP64) and sample exactly the cells the reconstruction counts."""
+    cfg = oracle.Config()
+    cfg.ccd_roix, cfg.nxmax, cfg.circle_cx, cfg.circle_cy, cfg.dim_final = 256, 16, 64, 64, 64
+    rng = np.random.default_rng(0)
+    M, F, D = 5, 32, 64
+    pos = np.concatenate([rng.integers(6, F - 6, M), rng.integers(6, F - 6, M)]).astype(np.float64)
+    xn, xk = rng.standard_normal((D, D, D)), rng.standard_normal((D, D, D))
+    y = rng.standard_normal((M, F, F)) + 1j * rng.standard_normal((M, F, F))
+    ax = oracle.forward_caps(xn, xk, pos, cfg)
+    ahy = oracle.adjoint_caps(y, pos, cfg)
+    lhs, rhs = np.vdot(y, ax), np.vdot(ahy, xn + 1j * xk)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    # the cells are the reconstruction's: scattering ones gives its hit counts
+    counts = np.zeros((D, D, D))
+    for a, cell in enumerate(oracle.cap_cells(pos, cfg)):
+        np.add.at(counts, cell[1:], 1.0)
+    ref = oracle.reconstruction(np.zeros((M, F, F), np.complex128), pos, cfg, want_otf=False, want_indice=False)
+    np.testing.assert_array_equal(counts, ref["counts"])
