@@ -214,6 +214,138 @@ def run_reference(args, acq, ph, seed):
     print(json.dumps(line))
 
 
+def tv_form(iterations: int = 50, segment: int = 5):
+    """Regularised reconstruction form: forward-operator data of a missing-cone
+    phantom (two touching cells, dn 0.03) on 256^3 from 400 caps of 128^2,
+    single-pass reconstruction against projected gradient with positivity and
+    TV 1e-3.  The iterations run in segments of `segment`, each resuming from
+    the previous segment's saved iterate, with the error to the phantom read
+    between segments."""
+    from dataclasses import replace
+
+    import numpy as np
+    import torch
+
+    from mtd_transmission_gb300 import Context, Geometry, simul
+    acq, _, _ = simul.workload("plain_512_born")
+    M = 400
+    acq = replace(acq, nb_holo=M)
+    N, D = acq.nxmax, acq.dim_final
+    t = simul.spiral_tilts(M, N)
+    pos = torch.from_numpy(np.concatenate([N + t[:, 0], N + t[:, 1]]).astype(np.int32)).cuda()
+    z, y, x = torch.meshgrid(*(torch.arange(D, device="cuda", dtype=torch.float32) - D / 2,) * 3, indexing="ij")
+    truth = torch.zeros((D, D, D), device="cuda")
+    for cx in (-0.12 * D, 0.12 * D):
+        truth[(x - cx) ** 2 + y ** 2 + (z / 0.8) ** 2 < (0.12 * D) ** 2] = 0.03
+    del x, y, z
+
+    def err(v):
+        return float(torch.linalg.vector_norm(v - truth) / torch.linalg.vector_norm(truth))
+
+    opts = dict(step=1.0, tv_weight=1e-3, tv_eps=1e-3, index_min=0.0, index_max=0.1)
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        caps = torch.empty((M, 2 * N, 2 * N, 2), device="cuda")
+        ctx.forward(truth, None, n=M, posspec=pos, caps_out=caps)
+        born = torch.empty_like(truth)
+        ctx.tv_reconstruct(born, caps=caps, n=M, posspec=pos, iterations=0, init=1)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.tv_reconstruct(born, caps=caps, n=M, posspec=pos, iterations=0, init=1)
+        torch.cuda.synchronize()
+        born_s = time.perf_counter() - t0
+        e_born = err(born)
+        xv = torch.empty_like(truth)
+        tol = 0.5 * e_born
+        dev_s, done, trace, t_tol = 0.0, 0, [], None
+        while done < iterations:
+            k = min(segment, iterations - done)
+            rep = ctx.tv_reconstruct(xv, caps=caps, n=M, posspec=pos, iterations=k, init=1 if done == 0 else 0,
+                                     **opts)
+            dev_s += rep["seconds"]
+            done += k
+            e = err(xv)
+            trace.append([done, round(e, 4)])
+            if t_tol is None and e <= tol:
+                t_tol = dev_s
+    return {"workload": f"two touching cells dn 0.03 in {D}^3, {M} Ewald caps of {2 * N}^2 (forward-operator data)",
+            "single_pass_rel_l2": round(e_born, 4), "single_pass_s": round(born_s, 5),
+            "regularised_rel_l2": trace[-1][1], "iterations": iterations,
+            "ms_per_iteration": round(1e3 * dev_s / iterations, 3),
+            "tolerance": f"rel-L2 <= {tol:.4f} (half the single-pass error)",
+            "time_to_tolerance_s": round(t_tol, 5) if t_tol is not None else None,
+            "rel_l2_trace": trace, "options": opts}
+
+
+def batched_form(count: int = 8, seed: int = 2, rounds: int = 3):
+    """Batched form: `count` acquisitions of uneven size (holograms of 256^2 to
+    2048^2, 50-800 angles, volumes 128^3-512^3 matched to the crop, random
+    bead/ellipsoid phantoms with dn 0.005-0.05), reconstructed one by one
+    (one tdm_pipeline call each) and as one CUDA-graph launch (tdm_batch)."""
+    import numpy as np
+    import torch
+
+    from mtd_transmission_gb300 import Batch, Context, Geometry, simul
+    rng = np.random.default_rng(seed)
+    specs, stacks, ctxs = [], [], []
+    for i in range(count):
+        H = int(rng.choice([256, 512, 1024, 2048]))
+        N = int(rng.choice([n for n in (32, 64, 128) if n <= H // 4]))
+        M = int(rng.integers(50, 801))
+        M = min(M, int(1.5e9 // (H * H)))  # bounds the synthesis time of the largest stacks
+        acq = simul.Acquisition(ccd_roix=H, nxmax=N, circle_cx=H // 4, circle_cy=H // 4, dim_final=4 * N,
+                                nb_holo=M, born=int(rng.integers(0, 2)))
+        objs = [simul.Ellipsoid(tuple(rng.uniform(-0.2, 0.2, 3)), tuple(rng.uniform(0.04, 0.15, 3)),
+                                float(rng.uniform(0.005, 0.05)), smooth=bool(rng.integers(0, 2)))
+                for _ in range(int(rng.integers(1, 5)))]
+        ph = simul.Phantom(objs, phase_max=None if acq.born else 20.0)
+        d = simul.holograms(acq, ph, seed=seed * 100 + i, device="cuda")
+        ctx = Context(Geometry.from_acquisition(acq), M)
+        ctxs.append(ctx)
+        ctx.set_mask(np.ascontiguousarray(d["mask"].cpu().numpy()))
+        D = acq.dim_final
+        holos = d["holos"].contiguous()
+        re = torch.empty((D, D, D), device="cuda")
+        im = torch.empty_like(re)
+        otf = torch.empty((D, D, D), dtype=torch.uint8, device="cuda")
+        stacks.append((ctx, holos, re, im, otf))
+        specs.append([H, M, D])
+        del d
+    holos_total = sum(m for _, m, _ in specs)
+
+    def one_by_one():
+        for ctx, holos, re, im, otf in stacks:
+            ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+        for ctx in ctxs:
+            ctx.synchronize()
+
+    one_by_one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(rounds):
+        one_by_one()
+    seq_s = (time.perf_counter() - t0) / rounds
+    with Batch(stacks) as b:
+        st = torch.cuda.current_stream()
+        b.launch(st.cuda_stream)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(st)
+        for _ in range(rounds):
+            b.launch(st.cuda_stream)
+        ev1.record(st)
+        torch.cuda.synchronize()
+        graph_s = ev0.elapsed_time(ev1) / 1e3 / rounds
+    for ctx in ctxs:
+        ctx.close()
+    return {"stacks": [{"hologram_px": h, "holograms": m, "volume": d} for h, m, d in specs],
+            "holograms": holos_total,
+            "one_by_one": {"holograms_per_s": round(holos_total / seq_s, 1), "volumes_per_s": round(count / seq_s, 3),
+                           "s": round(seq_s, 5)},
+            "graph": {"holograms_per_s": round(holos_total / graph_s, 1), "volumes_per_s": round(count / graph_s, 3),
+                      "s": round(graph_s, 5)},
+            "note": "holograms resident in HBM; one CUDA graph with the stacks as independent branches"}
+
+
 def workload_config(acq, args):
     return {"workload": f"{args.workload}: {acq.nb_holo} x {acq.ccd_roix}^2 uint16 12-bit holograms, "
                         f"NXMAX {acq.nxmax} ({2 * acq.nxmax}^2 fields), {'Born' if acq.born else 'Rytov'}, "
@@ -237,6 +369,7 @@ def main():
     ap.add_argument("--profile-out", default=None)
     ap.add_argument("--no-profile-pass", action="store_true", help="skip the per-kernel event pass")
     ap.add_argument("--holograms", type=int, default=None, help="override the workload's hologram count")
+    ap.add_argument("--no-forms", action="store_true", help="skip the regularised-reconstruction form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -410,6 +543,9 @@ def main():
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][0])},
             "profiled_ms_per_step": round(prof_ms / args.steps, 3),
         }
+        if not args.no_forms:
+            ctx.close()
+            line["forms"] = {"tv_adjoint": tv_form(), "batched": batched_form()}
         if args.profile_out:
             with open(args.profile_out, "w") as f:
                 json.dump(line, f, indent=1)

@@ -174,7 +174,8 @@ typedef struct {
     int iterations;            /* projected-gradient iterations */
     int init;                  /* 0: start from index_io / absorption_io; 1: from the single-pass reconstruction */
     float step;                /* data step (1: each iteration makes the measured cells data-consistent) */
-    float tv_weight;           /* TV gradient step (0: no regularisation) */
+    float tv_weight;           /* TV gradient step per iteration, relative to each channel's box range
+                                  (max - min; absolute when the box is unbounded); 0: no regularisation */
     float tv_eps;              /* TV smoothing: sum sqrt(|grad x|^2 + eps^2) */
     float index_min, index_max;            /* box constraints (DELTA_NMIN, DELTA_NMAX) */
     float absorption_min, absorption_max;  /* (KAPPA_MIN, KAPPA_MAX) */
@@ -188,7 +189,7 @@ typedef struct {
 } tdm_tv_report;
 
 /* Regularised reconstruction: x <- clamp(x - step T(S^H (S G x - caps) / count)
- * - tv_weight dTV(x)), T = G^-1, count the cells' hit counts (the
+ * - tv dTV(x)), tv = tv_weight x the box range, T = G^-1, count the cells' hit counts (the
  * single-pass reconstruction's normalisation as the preconditioner), the
  * clamp the box constraints.  caps: n x F x F complex cap values, or NULL
  * for the context's cap records (from the last tdm_pipeline or
@@ -198,6 +199,22 @@ typedef struct {
  * be continued from a saved iterate. */
 int tdm_tv_reconstruct(tdm_ctx* ctx, const float* caps, int n, const int32_t* posspec, const tdm_tv_opts* opts,
                        float* index_io, float* absorption_io, tdm_tv_report* report);
+
+/* ---- Batched acquisitions ----
+ * Several stacks of uneven size (one context each, any geometries) processed
+ * by one CUDA-graph launch.  No counterpart in the reference.
+ * tdm_batch_create captures, for stack i, tdm_pipeline(ctxs[i], holos[i],
+ * bits[i], n[i], indice[i], absorption[i], otf[i], NULL, NULL) into one
+ * graph in which the stacks are independent branches; all buffers must be
+ * device memory and are bound at creation (refill holos[i] between
+ * launches).  tdm_batch_launch runs the graph on `stream` (a cudaStream_t,
+ * 0 for the default stream) and returns without waiting.  A context must
+ * not be used by other calls while a launch of a batch that holds it runs. */
+typedef struct tdm_batch tdm_batch;
+int tdm_batch_create(int count, tdm_ctx* const* ctxs, const void* const* holos, const int* bits, const int* n,
+                     float* const* indice, float* const* absorption, uint8_t* const* otf, tdm_batch** out);
+int tdm_batch_launch(tdm_batch* batch, void* stream);
+int tdm_batch_destroy(tdm_batch* batch);
 
 /* Off-axis extraction that allocates nothing.  No counterpart in the
  * reference: it is for callers that cannot allocate GPU memory, such as a

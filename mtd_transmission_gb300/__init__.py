@@ -5,5 +5,6 @@ Born/Rytov fields and Ewald-cap mapping with the 3D inverse FFT, as sm_103a
 CUDA kernels behind the C ABI declared in include/tdm.h.
 """
 from .api import (  # noqa: F401
-    Context, Derived, Geometry, TdmError, derive, extract_string, extract_val, lib, read_geom, read_pgm, write_tiff,
+    Batch, Context, Derived, Geometry, TdmError, derive, extract_string, extract_val, lib, read_geom, read_pgm,
+    write_tiff,
 )

@@ -28,7 +28,7 @@ EXPORTS = (
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
-    "tdm_tv_reconstruct",
+    "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy",
 )
 
 
@@ -103,6 +103,9 @@ def lib():
     L.tdm_pipeline.argtypes = [P, P, I, I, P, P, P, P, P]
     L.tdm_pipeline_async.argtypes = [P, P, I, I, P, P, P, P]
     L.tdm_forward.argtypes = [P, P, P, I, P, P]
+    L.tdm_batch_create.argtypes = [I, P, P, P, P, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
+    L.tdm_batch_launch.argtypes = [P, P]
+    L.tdm_batch_destroy.argtypes = [P]
     L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
     L.tdm_tv_reconstruct.argtypes = [P, P, I, P, ctypes.POINTER(TvOpts), P, P, ctypes.POINTER(TvReport)]
     L.tdm_cap_planes.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
@@ -361,3 +364,45 @@ def write_tiff(path: str, vol: np.ndarray, pixel_size: float, orientation: int =
     rc = lib().tdm_write_tiff_f32(path.encode(), ptr(v), wdt, hgt, pages, pixel_size, orientation)
     if rc != TDM_OK:
         raise TdmError(rc, f"cannot write {path}")
+
+
+class Batch:
+    """tdm_batch: several stacks (one Context each) in one CUDA-graph launch.
+
+    stacks: list of (context, holos, indice, absorption, otf) with device
+    buffers (otf / absorption may be None); the buffers are bound at creation."""
+
+    def __init__(self, stacks):
+        k = len(stacks)
+        arr = lambda vals: (ctypes.c_void_p * k)(*[None if v is None else ptr(v).value for v in vals])
+        ctxs = (ctypes.c_void_p * k)(*[st[0]._h.value for st in stacks])
+        holos = arr([st[1] for st in stacks])
+        bits = (ctypes.c_int * k)(*[st[0]._bits(st[1]) for st in stacks])
+        n = (ctypes.c_int * k)(*[int(st[1].shape[0]) for st in stacks])
+        h = ctypes.c_void_p()
+        rc = lib().tdm_batch_create(k, ctxs, holos, bits, n, arr([st[2] for st in stacks]),
+                                    arr([st[3] for st in stacks]), arr([st[4] for st in stacks]), ctypes.byref(h))
+        if rc != TDM_OK:
+            raise TdmError(rc, "tdm_batch_create: " + lib().tdm_last_error(stacks[0][0]._h).decode())
+        self._h = h
+        self._stacks = stacks  # keep the buffers alive
+
+    def launch(self, stream: int = 0):
+        rc = lib().tdm_batch_launch(self._h, ctypes.c_void_p(stream))
+        if rc != TDM_OK:
+            raise TdmError(rc, "tdm_batch_launch failed")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tdm_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+

@@ -525,7 +525,7 @@ k_cap_pack(const float2* __restrict__ caps, const int2* __restrict__ posspec, Pa
 }
 
 // One projected-gradient step of the regularised reconstruction, per voxel of
-// the [z][y][x] volumes: x <- clamp(x - step g - step_tv tv_weight dTV(x)),
+// the [z][y][x] volumes: x <- clamp(x - step g - tv dTV(x)) (tv per channel),
 // for the index (real part) and, when present, the absorption.  TV is the
 // isotropic total variation with forward differences (zero across the far
 // faces) smoothed by eps: sum sqrt(|grad x|^2 + eps^2).
@@ -551,17 +551,17 @@ __device__ __forceinline__ float tv_grad(const float* __restrict__ x, int D, int
 
 __global__ void __launch_bounds__(256)
 k_tv_step(const float* __restrict__ xn, const float* __restrict__ xk, const float* __restrict__ gn,
-          const float* __restrict__ gk, int D, float step, float tv_step, float eps2, float nlo, float nhi, float klo,
-          float khi, float* __restrict__ xn_out, float* __restrict__ xk_out) {
+          const float* __restrict__ gk, int D, float step, float tv_n, float tv_k, float eps2, float nlo, float nhi,
+          float klo, float khi, float* __restrict__ xn_out, float* __restrict__ xk_out) {
     const size_t total = (size_t)D * D * D;
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < total; v += (size_t)gridDim.x * blockDim.x) {
         const int X = (int)(v % D), Y = (int)((v / D) % D), Z = (int)(v / ((size_t)D * D));
         float a = xn[v] - step * gn[v];
-        if (tv_step != 0.0f) a -= tv_step * tv_grad(xn, D, X, Y, Z, eps2);
+        if (tv_n != 0.0f) a -= tv_n * tv_grad(xn, D, X, Y, Z, eps2);
         xn_out[v] = fminf(fmaxf(a, nlo), nhi);
         if (xk) {
             float b = xk[v] - step * gk[v];
-            if (tv_step != 0.0f) b -= tv_step * tv_grad(xk, D, X, Y, Z, eps2);
+            if (tv_k != 0.0f) b -= tv_k * tv_grad(xk, D, X, Y, Z, eps2);
             xk_out[v] = fminf(fmaxf(b, klo), khi);
         }
     }
@@ -797,11 +797,12 @@ int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float4* recs) {
 }
 
 int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
-                   float tv_step, float eps, float nlo, float nhi, float klo, float khi, float* xn_out, float* xk_out) {
+                   float tv_n, float tv_k, float eps, float nlo, float nhi, float klo, float khi, float* xn_out,
+                   float* xk_out) {
     const int D = c->p.D;
     {
         Launch l(c, K_FORM);
-        k_tv_step<<<152 * 8, 256, 0, c->stream>>>(xn, xk, gn, gk, D, step, tv_step, eps * eps, nlo, nhi, klo, khi,
+        k_tv_step<<<152 * 8, 256, 0, c->stream>>>(xn, xk, gn, gk, D, step, tv_n, tv_k, eps * eps, nlo, nhi, klo, khi,
                                                    xn_out, xk_out);
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;

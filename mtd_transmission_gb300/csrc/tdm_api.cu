@@ -814,6 +814,10 @@ int tdm_tv_reconstruct(tdm_ctx* c, const float* caps, int n, const int32_t* poss
         TDM_CU(cudaMemcpyAsync(xn, index_io, NT * sizeof(float), cudaMemcpyDefault, c->stream));
         if (absn) TDM_CU(cudaMemcpyAsync(xk, absorption_io, NT * sizeof(float), cudaMemcpyDefault, c->stream));
     }
+    // TV steps relative to each channel's box range (absolute when unbounded)
+    auto range = [](float lo, float hi) { return std::isfinite(hi - lo) && hi > lo ? hi - lo : 1.0f; };
+    const float tv_n = o->tv_weight * range(o->index_min, o->index_max);
+    const float tv_k = o->tv_weight * range(o->absorption_min, o->absorption_max);
     cudaEvent_t t0 = prof_event(c), t1 = prof_event(c);
     TDM_CU(cudaEventRecord(t0, c->stream));
     double first = -1, last = -1;
@@ -829,7 +833,7 @@ int tdm_tv_reconstruct(tdm_ctx* c, const float* caps, int n, const int32_t* poss
             if (o->iterations == 1) last = m;
         }
         if (int rc = launch_adjoint(c, b.rec2, n, gn, gk, true)) return fail(c, rc, "tdm_tv_reconstruct: launch failed");
-        if (int rc = launch_tv_step(c, xn, xk, gn, gk, o->step, o->tv_weight, o->tv_eps, o->index_min, o->index_max,
+        if (int rc = launch_tv_step(c, xn, xk, gn, gk, o->step, tv_n, tv_k, o->tv_eps, o->index_min, o->index_max,
                                     o->absorption_min, o->absorption_max, xn2, xk2))
             return fail(c, rc, "tdm_tv_reconstruct: launch failed");
         std::swap(xn, xn2);
@@ -849,6 +853,69 @@ int tdm_tv_reconstruct(tdm_ctx* c, const float* caps, int n, const int32_t* poss
         report->misfit_last = last;
         report->seconds = ms / 1e3;
     }
+    return TDM_OK;
+}
+
+// ---------------------------------------------------------------- batched acquisitions
+struct tdm_batch {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+int tdm_batch_create(int count, tdm_ctx* const* ctxs, const void* const* holos, const int* bits, const int* n,
+                     float* const* indice, float* const* absorption, uint8_t* const* otf, tdm_batch** out) {
+    if (!out || count <= 0 || !ctxs || !holos || !bits || !n) return TDM_EINVAL;
+    *out = nullptr;
+    for (int i = 0; i < count; ++i) {
+        if (!ctxs[i] || !holos[i] || !is_device_ptr(holos[i])) return TDM_EINVAL;
+        const void* outs[3] = {indice ? indice[i] : nullptr, absorption ? absorption[i] : nullptr,
+                               otf ? otf[i] : nullptr};
+        for (const void* o : outs)
+            if (o && !is_device_ptr(o)) return fail(ctxs[i], TDM_EINVAL, "tdm_batch_create: outputs must be device memory");
+    }
+    auto* b = new tdm_batch;
+    if (cudaGraphCreate(&b->graph, 0) != cudaSuccess) {
+        delete b;
+        return TDM_ECUDA;
+    }
+    for (int i = 0; i < count; ++i) {
+        tdm_ctx* c = ctxs[i];
+        cudaSetDevice(c->device);
+        // relaxed: the pipeline sets kernel attributes while it is captured
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            tdm_batch_destroy(b);
+            return cuda_fail(c, cudaGetLastError(), "tdm_batch_create: capture");
+        }
+        const int rc = pipeline(c, holos[i], bits[i], n[i], indice ? indice[i] : nullptr,
+                                absorption ? absorption[i] : nullptr, otf ? otf[i] : nullptr, nullptr, nullptr, false);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        cudaGraphNode_t node;
+        if (rc || e != cudaSuccess || cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, g) != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            tdm_batch_destroy(b);
+            return rc ? rc : cuda_fail(c, e ? e : cudaGetLastError(), "tdm_batch_create: graph");
+        }
+        cudaGraphDestroy(g);  // the child node holds a copy
+    }
+    if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+        tdm_batch_destroy(b);
+        return cuda_fail(ctxs[0], cudaGetLastError(), "tdm_batch_create: instantiate");
+    }
+    *out = b;
+    return TDM_OK;
+}
+
+int tdm_batch_launch(tdm_batch* b, void* stream) {
+    if (!b || !b->exec) return TDM_EINVAL;
+    return cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)) == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+int tdm_batch_destroy(tdm_batch* b) {
+    if (!b) return TDM_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    delete b;
     return TDM_OK;
 }
 

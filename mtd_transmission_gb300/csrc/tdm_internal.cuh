@@ -178,9 +178,10 @@ int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* 
 int launch_adjoint(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bool normalize);
 // Cap records (value, cell plane) of cap values in FFT-bin order.
 int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float4* recs);
-// One projected-gradient step with the TV gradient and box constraints.
+// One projected-gradient step with the TV gradient (steps tv_n, tv_k) and box constraints.
 int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
-                   float tv_step, float eps, float nlo, float nhi, float klo, float khi, float* xn_out, float* xk_out);
+                   float tv_n, float tv_k, float eps, float nlo, float nhi, float klo, float khi, float* xn_out,
+                   float* xk_out);
 // gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs.
 // Downloads run on c->dl_stream and end with c->ev_dl_done; the staging
 // buffers are not written before the previous volume's downloads are done.

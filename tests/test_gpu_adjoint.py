@@ -147,7 +147,7 @@ def test_tv_reconstruction_beats_single_pass_and_resumes():
     acq, pos = geometry(M=24, seed=9)
     D, M = acq.dim_final, acq.nb_holo
     truth = phantom(D)
-    opts = dict(step=1.0, tv_weight=2e-4, tv_eps=1e-3, index_min=0.0, index_max=0.05)
+    opts = dict(step=1.0, tv_weight=2e-3, tv_eps=1e-3, index_min=0.0, index_max=0.05)
     with Context(Geometry.from_acquisition(acq), M) as ctx:
         caps = ctx.forward(truth, None, n=M, posspec=pos)
         born = np.zeros((D, D, D), np.float32)

@@ -226,3 +226,40 @@ def test_mask_without_background():
     with Context(Geometry.from_acquisition(acq), 1) as ctx:
         with pytest.raises(TdmError):
             ctx.set_mask(np.zeros((F, F), np.uint8))
+
+
+def test_batch_graph_matches_one_by_one():
+    """Three stacks of different geometries in one CUDA-graph launch
+    (tdm_batch) give, bit for bit, the volumes of one tdm_pipeline call each."""
+    import torch
+    from mtd_transmission_gb300 import Batch
+    cases = [small_case("plain_512_born", M=5),
+             small_case("rytov_1024", M=4, ccd_roix=512, nxmax=64, circle_cx=128, circle_cy=128, dim_final=256),
+             small_case("plain_512_born", M=3, ccd_roix=256, nxmax=32, circle_cx=64, circle_cy=64, dim_final=128)]
+    ctxs, stacks, refs = [], [], []
+    try:
+        for acq, _, d in cases:
+            D, M = acq.dim_final, acq.nb_holo
+            ctx = Context(Geometry.from_acquisition(acq), M)
+            ctxs.append(ctx)
+            ctx.set_mask(np.ascontiguousarray(d["mask"]))
+            holos = torch.from_numpy(np.ascontiguousarray(d["holos"])).cuda()
+            re = torch.zeros((D, D, D), device="cuda")
+            im = torch.zeros_like(re)
+            otf = torch.zeros((D, D, D), dtype=torch.uint8, device="cuda")
+            ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+            ctx.synchronize()
+            refs.append((re.clone(), im.clone(), otf.clone()))
+            re.zero_()
+            im.zero_()
+            otf.zero_()
+            stacks.append((ctx, holos, re, im, otf))
+        with Batch(stacks) as b:
+            for _ in range(2):  # replays reuse the bound buffers
+                b.launch(torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+        for (ctx, holos, re, im, otf), (r0, i0, o0) in zip(stacks, refs):
+            assert torch.equal(re, r0) and torch.equal(im, i0) and torch.equal(otf, o0)
+    finally:
+        for ctx in ctxs:
+            ctx.close()
