@@ -236,6 +236,12 @@ int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n
  * Diagnostic; no counterpart in the reference. */
 int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
 
+/* Project autotuner (no counterpart in the reference): times tdm_pipeline on
+ * the given stack (device holograms) with 8, 16 and 32 angles per chunk of
+ * the per-angle stages (the schedule the stages are streamed in) and keeps
+ * the fastest for the context; *chunk_out receives it. */
+int tdm_autotune(tdm_ctx* ctx, const void* holos, int bits, int n, int* chunk_out);
+
 /* Stream-ordered execution helpers. */
 int tdm_synchronize(tdm_ctx* ctx);
 void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */

@@ -28,7 +28,7 @@ EXPORTS = (
     "tdm_launch_count", "tdm_stage_ms", "tdm_extract_val", "tdm_extract_string", "tdm_read_geom", "tdm_read_pgm",
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
-    "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy",
+    "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
 )
 
 
@@ -105,6 +105,7 @@ def lib():
     L.tdm_forward.argtypes = [P, P, P, I, P, P]
     L.tdm_batch_create.argtypes = [I, P, P, P, P, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
     L.tdm_batch_launch.argtypes = [P, P]
+    L.tdm_autotune.argtypes = [P, P, I, I, ctypes.POINTER(I)]
     L.tdm_batch_destroy.argtypes = [P]
     L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
     L.tdm_tv_reconstruct.argtypes = [P, P, I, P, ctypes.POINTER(TvOpts), P, P, ctypes.POINTER(TvReport)]
@@ -290,6 +291,13 @@ class Context:
         self._check(lib().tdm_tv_reconstruct(self._h, ptr(caps), n, ptr(posspec), ctypes.byref(o), ptr(index_io),
                                              ptr(absorption_io), ctypes.byref(r)), "tdm_tv_reconstruct")
         return {f: getattr(r, f) for f, _ in TvReport._fields_}
+
+    def autotune(self, holos, n=None) -> int:
+        """tdm_autotune: picks the angles per chunk (8, 16 or 32) fastest on this stack; returns it."""
+        n = holos.shape[0] if n is None else n
+        out = ctypes.c_int()
+        self._check(lib().tdm_autotune(self._h, ptr(holos), self._bits(holos), n, ctypes.byref(out)), "tdm_autotune")
+        return out.value
 
     @property
     def cap_planes(self):

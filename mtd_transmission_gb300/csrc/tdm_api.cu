@@ -311,15 +311,14 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     for (auto& e : c->ev_stage) cudaEventCreate(&e);
     for (auto& e : c->ev_out) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     Buffers& b = c->b;
-    const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk, L = p.L;
-    c->holo_chunk = 16;
+    const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk_cap, L = p.L;
     TRY(dev_alloc(c, &b.tw, kTwTotal));
     TRY(dev_alloc(c, &b.tuk_h, p.H));
     TRY(dev_alloc(c, &b.tuk_f, F));
     TRY(dev_alloc(c, &b.s_tab, FF));
     TRY(dev_alloc(c, &b.s_tabf, FF));
-    TRY(dev_alloc(c, &b.holo_stage, 2 * (size_t)c->holo_chunk * p.H * p.H * 2));
-    TRY(dev_alloc(c, &b.inter, (size_t)c->holo_chunk * p.H * F));
+    TRY(dev_alloc(c, &b.holo_stage, 2 * CH * p.H * p.H * 2));
+    TRY(dev_alloc(c, &b.inter, CH * p.H * F));
     TRY(dev_alloc(c, &b.spectra, M * FF));
     TRY(dev_alloc(c, &b.posspec, M));
     TRY(dev_alloc(c, &b.specval, M));
@@ -484,7 +483,7 @@ static int stage_extract(tdm_ctx* c, const void* holos, int bits, int n) {
     const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
     if (is_device_ptr(holos)) return launch_extract(c, holos, bits, n, 0);
     // host holograms: chunked copies on the copy stream, double buffered
-    const size_t stage_bytes = (size_t)c->holo_chunk * p.H * p.H * 2;
+    const size_t stage_bytes = (size_t)c->chunk_cap * p.H * p.H * 2;  // one staging half
     for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
         const int m = std::min(c->holo_chunk, n - h0);
         const int buf = k & 1;
@@ -642,7 +641,7 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
     const Params& p = c->p;
     const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
     const bool dev = is_device_ptr(holos);
-    const size_t stage_bytes = (size_t)c->holo_chunk * p.H * p.H * 2;
+    const size_t stage_bytes = (size_t)c->chunk_cap * p.H * p.H * 2;  // one staging half
     for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
         const int m = std::min(c->holo_chunk, n - h0);
         const void* src = static_cast<const char*>(holos) + h0 * per;
@@ -916,6 +915,40 @@ int tdm_batch_destroy(tdm_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     delete b;
+    return TDM_OK;
+}
+
+// ---------------------------------------------------------------- autotuning
+int tdm_autotune(tdm_ctx* c, const void* holos, int bits, int n, int* chunk_out) {
+    if (!c || !holos || !is_device_ptr(holos) || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
+        return fail(c, TDM_EINVAL, "tdm_autotune: invalid argument (device holograms required)");
+    cudaSetDevice(c->device);
+    const int cands[] = {8, 16, 32};
+    int best = c->chunk;
+    float best_ms = 0;
+    cudaEvent_t t0 = prof_event(c), t1 = prof_event(c);
+    int rc = TDM_OK;
+    for (int cand : cands) {
+        if (cand > c->chunk_cap) continue;
+        c->chunk = c->holo_chunk = cand;
+        rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);  // warm-up
+        if (!rc && cudaEventRecord(t0, c->stream) != cudaSuccess) rc = TDM_ECUDA;
+        for (int r = 0; r < 2 && !rc; ++r) rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);
+        if (!rc && cudaEventRecord(t1, c->stream) != cudaSuccess) rc = TDM_ECUDA;
+        if (!rc) rc = tdm_synchronize(c);
+        float ms = 0;
+        if (!rc && cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) rc = TDM_ECUDA;
+        if (rc) break;
+        if (best_ms == 0 || ms < best_ms) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    c->ev_pool.push_back(t0);
+    c->ev_pool.push_back(t1);
+    c->chunk = c->holo_chunk = best;
+    if (rc) return rc;
+    if (chunk_out) *chunk_out = best;
     return TDM_OK;
 }
 

@@ -93,8 +93,9 @@ struct tdm_ctx {
     tdm::Params p{};
     tdm::Buffers b{};
     int max_angles = 0;
-    int chunk = 16;              // angles per chunk of the per-angle stages
-    int holo_chunk = 16;         // holograms per extraction chunk
+    int chunk = 16;              // angles per chunk of the per-angle stages (tdm_autotune may change it)
+    int holo_chunk = 16;         // holograms per extraction chunk (equal to chunk)
+    int chunk_cap = 32;          // chunk capacity of the per-chunk buffers
     int nsamp = 0;
     int device = 0;
     int n_fields = 0;            // angles held in b.fields / b.posspec

@@ -263,3 +263,24 @@ def test_batch_graph_matches_one_by_one():
     finally:
         for ctx in ctxs:
             ctx.close()
+
+
+def test_autotune_keeps_results():
+    """tdm_autotune picks 8, 16 or 32 angles per chunk; the volume does not
+    depend on the chunking (every per-angle kernel sees only its own angle)."""
+    import torch
+    acq, _, d = small_case("plain_512_born", M=40)
+    D = acq.dim_final
+    holos = torch.from_numpy(np.ascontiguousarray(d["holos"])).cuda()
+    with Context(Geometry.from_acquisition(acq), 40) as ctx:
+        ctx.set_mask(np.ascontiguousarray(d["mask"]))
+        re0 = torch.zeros((D, D, D), device="cuda")
+        im0 = torch.zeros_like(re0)
+        ctx.pipeline(holos, indice=re0, absorption=im0)
+        chunk = ctx.autotune(holos)
+        assert chunk in (8, 16, 32)
+        re = torch.zeros_like(re0)
+        im = torch.zeros_like(re0)
+        ctx.pipeline(holos, indice=re, absorption=im)
+        ctx.synchronize()
+        assert torch.equal(re, re0) and torch.equal(im, im0), chunk
