@@ -242,8 +242,13 @@ int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
  * the fastest for the context; *chunk_out receives it. */
 int tdm_autotune(tdm_ctx* ctx, const void* holos, int bits, int n, int* chunk_out);
 
-/* Stream-ordered execution helpers. */
+/* Stream-ordered execution helpers.  tdm_pipeline queues each volume's stage
+ * (gather, 3D inverse FFT, outputs) on a second stream of the context, so that
+ * it overlaps the next call's per-angle stages; tdm_join orders the context
+ * stream after those volume stages (the other entry points do this
+ * themselves; tdm_synchronize waits for everything). */
 int tdm_synchronize(tdm_ctx* ctx);
+int tdm_join(tdm_ctx* ctx);
 void* tdm_stream(tdm_ctx* ctx);               /* cudaStream_t of the context */
 uint64_t tdm_launch_count(const tdm_ctx* ctx); /* kernels launched so far */
 /* Device-side elapsed time of the last tdm_* call's dominant kernel group

@@ -29,6 +29,7 @@ EXPORTS = (
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
     "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
+    "tdm_join",
 )
 
 
@@ -106,6 +107,7 @@ def lib():
     L.tdm_batch_create.argtypes = [I, P, P, P, P, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
     L.tdm_batch_launch.argtypes = [P, P]
     L.tdm_autotune.argtypes = [P, P, I, I, ctypes.POINTER(I)]
+    L.tdm_join.argtypes = [P]
     L.tdm_batch_destroy.argtypes = [P]
     L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
     L.tdm_tv_reconstruct.argtypes = [P, P, I, P, ctypes.POINTER(TvOpts), P, P, ctypes.POINTER(TvReport)]
@@ -220,6 +222,10 @@ class Context:
 
     def synchronize(self):
         self._check(lib().tdm_synchronize(self._h), "tdm_synchronize")
+
+    def join(self):
+        """tdm_join: orders the context stream after the queued volume stages."""
+        self._check(lib().tdm_join(self._h), "tdm_join")
 
     def set_mask(self, mask=None):
         self._check(lib().tdm_set_mask(self._h, ptr(mask)), "tdm_set_mask")

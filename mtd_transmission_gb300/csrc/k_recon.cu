@@ -596,16 +596,18 @@ int cap_impl(tdm_ctx* c, int a0, int n, bool form) {
 }
 
 // Download of bytes from a device buffer to host memory on the download
-// stream, after the work queued so far on c->stream.
-static cudaError_t download_after(tdm_ctx* c, cudaEvent_t ev, void* host, const void* dev, size_t bytes) {
-    cudaError_t e = cudaEventRecord(ev, c->stream);
+// stream, after the work queued so far on st.
+static cudaError_t download_after(tdm_ctx* c, cudaStream_t st, cudaEvent_t ev, void* host, const void* dev,
+                                  size_t bytes) {
+    cudaError_t e = cudaEventRecord(ev, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->dl_stream, ev, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->dl_stream);
     return e;
 }
 
 template <int D>
-int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
+int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float4* rec, const int2* posspec,
+                cudaEvent_t ev_gathered) {
     float* re = out.re;
     float* im = out.im;
     uint8_t* otf = out.otf;
@@ -622,35 +624,36 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
         return TDM_ECUDA;
     const bool host_out = out.host_re || out.host_im || out.host_otf || out.host_cnt;
     // the staging buffers may still be downloading the previous volume
-    if (host_out && cudaStreamWaitEvent(c->stream, c->ev_dl_done, 0)) return TDM_ECUDA;
+    if (host_out && cudaStreamWaitEvent(st, c->ev_dl_done, 0)) return TDM_ECUDA;
     if (cnt) {  // planes outside the cap band carry no hits
         const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
-        cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), c->stream);
-        cudaMemsetAsync(cnt + hi, 0, ((size_t)D * plane - hi) * sizeof(uint32_t), c->stream);
+        cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), st);
+        cudaMemsetAsync(cnt + hi, 0, ((size_t)D * plane - hi) * sizeof(uint32_t), st);
     }
-    cudaEventRecord(c->ev_stage[4], c->stream);
+    cudaEventRecord(c->ev_stage[4], st);
     {
-        Launch l(c, K_GATHER);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(b.rec, b.posspec, n, p, b.vol, cnt, 1);
+        Launch l(c, K_GATHER, st);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, st>>>(rec, posspec, n, p, b.vol, cnt, 1);
     }
-    cudaEventRecord(c->ev_stage[5], c->stream);
+    cudaEventRecord(c->ev_stage[5], st);
+    if (ev_gathered && cudaEventRecord(ev_gathered, st)) return TDM_ECUDA;
     const size_t NT = (size_t)D * D * D;
     bool downloads = false;
     if (out.host_cnt) {
-        if (download_after(c, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t))) return TDM_ECUDA;
+        if (download_after(c, st, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t))) return TDM_ECUDA;
         downloads = true;
     }
     {
-        Launch l(c, K_ZPASS);
-        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, c->stream>>>(b.vol, b.tw, p.zmin, p.band, otf);
+        Launch l(c, K_ZPASS, st);
+        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, st>>>(b.vol, b.tw, p.zmin, p.band, otf);
     }
     if (out.host_otf) {
-        if (download_after(c, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT)) return TDM_ECUDA;
+        if (download_after(c, st, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT)) return TDM_ECUDA;
         downloads = true;
     }
     {
-        Launch l(c, K_YPASS);
-        k_ypass<D, 1><<<dim3(D / P::B, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw);
+        Launch l(c, K_YPASS, st);
+        k_ypass<D, 1><<<dim3(D / P::B, D), P::NT, sm_p, st>>>(b.vol, b.tw);
     }
     // x pass by slabs of z blocks; a slab's planes are final once it has run
     const bool host_vol = out.host_re || out.host_im;
@@ -658,12 +661,12 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
     for (int sl = 0; sl < nslab; ++sl) {
         const int zb0 = sl * zblocks / nslab, zb1 = (sl + 1) * zblocks / nslab;
         {
-            Launch l(c, K_XPASS);
-            k_xpass<D><<<dim3(zb1 - zb0, D), P::NT, sm_p, c->stream>>>(b.vol, b.tw, p.out_scale, zb0, re, im);
+            Launch l(c, K_XPASS, st);
+            k_xpass<D><<<dim3(zb1 - zb0, D), P::NT, sm_p, st>>>(b.vol, b.tw, p.out_scale, zb0, re, im);
         }
         if (host_vol) {
             const size_t off = (size_t)zb0 * P::B * D * D, len = (size_t)(zb1 - zb0) * P::B * D * D;
-            if (cudaEventRecord(c->ev_out[sl], c->stream) || cudaStreamWaitEvent(c->dl_stream, c->ev_out[sl], 0))
+            if (cudaEventRecord(c->ev_out[sl], st) || cudaStreamWaitEvent(c->dl_stream, c->ev_out[sl], 0))
                 return TDM_ECUDA;
             if (out.host_re && cudaMemcpyAsync(out.host_re + off, re + off, len * sizeof(float),
                                                cudaMemcpyDeviceToHost, c->dl_stream))
@@ -674,7 +677,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out) {
             downloads = true;
         }
     }
-    cudaEventRecord(c->ev_stage[6], c->stream);
+    cudaEventRecord(c->ev_stage[6], st);
     if (downloads && cudaEventRecord(c->ev_dl_done, c->dl_stream)) return TDM_ECUDA;
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
@@ -755,12 +758,13 @@ int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
     }
 }
 
-int launch_volume(tdm_ctx* c, int n, const VolumeOut& out) {
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float4* rec, const int2* posspec,
+                  cudaEvent_t ev_gathered) {
     switch (c->p.D) {
-        case 128: return volume_impl<128>(c, n, out);
-        case 256: return volume_impl<256>(c, n, out);
-        case 512: return volume_impl<512>(c, n, out);
-        case 1024: return volume_impl<1024>(c, n, out);
+        case 128: return volume_impl<128>(c, n, out, st, rec, posspec, ev_gathered);
+        case 256: return volume_impl<256>(c, n, out, st, rec, posspec, ev_gathered);
+        case 512: return volume_impl<512>(c, n, out, st, rec, posspec, ev_gathered);
+        case 1024: return volume_impl<1024>(c, n, out, st, rec, posspec, ev_gathered);
         default: return TDM_EUNSUPPORTED;
     }
 }

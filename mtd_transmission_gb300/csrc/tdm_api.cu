@@ -79,7 +79,8 @@ void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
-                    b.fit_part, b.fit_done, b.fields, b.r1, b.rec, b.vol, b.out_re, b.out_im, b.out_otf,
+                    b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0], b.rec_buf[1], b.posspec_vol[0],
+                    b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
                     b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit};
     for (void* p : ptrs)
@@ -300,7 +301,12 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_dl_done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&c->vol_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_dl_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_angles, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_vol_last, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_rec_free[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_rec_free[1], cudaEventDisableTiming) != cudaSuccess) {
         delete c;
         return TDM_ECUDA;
     }
@@ -336,7 +342,11 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.fit_done, CH * 2));
     TRY(dev_alloc(c, &b.fields, M * FF));
     TRY(dev_alloc(c, &b.r1, CH * FF));
-    TRY(dev_alloc(c, &b.rec, M * FF));
+    TRY(dev_alloc(c, &b.rec_buf[0], M * FF));
+    TRY(dev_alloc(c, &b.rec_buf[1], M * FF));
+    TRY(dev_alloc(c, &b.posspec_vol[0], M));
+    TRY(dev_alloc(c, &b.posspec_vol[1], M));
+    b.rec = b.rec_buf[0];
     TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
     TRY(dev_alloc(c, &b.err, 4));
@@ -365,6 +375,7 @@ int tdm_destroy(tdm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
+    if (c->vol_stream) cudaStreamSynchronize(c->vol_stream);
     free_all(c);
     for (int i = 0; i < 2; ++i) {
         if (c->ev_copy[i]) cudaEventDestroy(c->ev_copy[i]);
@@ -379,7 +390,9 @@ int tdm_destroy(tdm_ctx* c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
-    if (c->ev_dl_done) cudaEventDestroy(c->ev_dl_done);
+    if (c->vol_stream) cudaStreamDestroy(c->vol_stream);
+    for (cudaEvent_t e : {c->ev_dl_done, c->ev_angles, c->ev_vol_last, c->ev_rec_free[0], c->ev_rec_free[1]})
+        if (e) cudaEventDestroy(e);
     delete c;
     return TDM_OK;
 }
@@ -392,9 +405,22 @@ int tdm_get_derived(const tdm_ctx* c, tdm_derived* out) {
     return TDM_OK;
 }
 
+// Orders the context stream after the volume stages that tdm_pipeline queued
+// on vol_stream (every entry point but tdm_pipeline starts with it).
+static cudaError_t join_volume(tdm_ctx* c) { return cudaStreamWaitEvent(c->stream, c->ev_vol_last, 0); }
+
+int tdm_join(tdm_ctx* c) {
+    if (!c) return TDM_EINVAL;
+    cudaSetDevice(c->device);
+    TDM_CU(join_volume(c));
+    return TDM_OK;
+}
+
 int tdm_set_mask(tdm_ctx* c, const uint8_t* mask) {
     if (!c) return TDM_EINVAL;
     cudaSetDevice(c->device);
+    // the background-sample tables are replaced with blocking copies: no work may still use them
+    if (int rc = tdm_synchronize(c)) return rc;
     if (!c->p.c_aber) return TDM_OK;
     std::vector<uint8_t> hm;
     if (mask && is_device_ptr(mask)) {
@@ -409,6 +435,7 @@ int tdm_set_mask(tdm_ctx* c, const uint8_t* mask) {
 int tdm_synchronize(tdm_ctx* c) {
     if (!c) return TDM_EINVAL;
     TDM_CU(cudaStreamSynchronize(c->copy_stream));
+    TDM_CU(cudaStreamSynchronize(c->vol_stream));
     TDM_CU(cudaStreamSynchronize(c->dl_stream));
     TDM_CU(cudaStreamSynchronize(c->stream));
     int err = 0;
@@ -436,6 +463,7 @@ int tdm_profile(tdm_ctx* c, int enable) {
 int tdm_profile_read(tdm_ctx* c, int index, const char** name, double* total_ms, int* launches) {
     if (!c || index < 0 || index >= K_COUNT) return TDM_EINVAL;
     TDM_CU(cudaStreamSynchronize(c->stream));
+    TDM_CU(cudaStreamSynchronize(c->vol_stream));
     double t = 0;
     int n = 0;
     for (const ProfRec& r : c->prof_recs) {
@@ -503,6 +531,7 @@ int tdm_extract(tdm_ctx* c, const void* holos, int bits, int n, float* spectra_o
     if (!c || !holos || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
         return fail(c, TDM_EINVAL, "tdm_extract: invalid argument");
     cudaSetDevice(c->device);
+    TDM_CU(join_volume(c));
     TDM_CU(cudaEventRecord(c->ev_stage[0], c->stream));
     if (int rc = stage_extract(c, holos, bits, n)) return rc;
     TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));
@@ -518,6 +547,7 @@ static int run_fields(tdm_ctx* c, const float* spectra_in, int n, float* fields_
                       float* dph, float* dun, float* dam) {
     if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, "tdm_fields: invalid argument");
     cudaSetDevice(c->device);
+    TDM_CU(join_volume(c));
     const size_t FF = (size_t)c->p.F * c->p.F;
     if (spectra_in && spectra_in != reinterpret_cast<float*>(c->b.spectra)) {
         TDM_CU(cudaMemcpyAsync(c->b.spectra, spectra_in, n * FF * sizeof(float2), cudaMemcpyDefault, c->stream));
@@ -564,7 +594,8 @@ int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_o
 // first); outputs may be host or device memory.  Host outputs are written to
 // device staging buffers and downloaded while the later passes run.
 static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt,
-                      bool wait = true) {
+                      bool wait = true, cudaStream_t st = nullptr, const float4* rec = nullptr,
+                      const int2* posspec = nullptr, cudaEvent_t ev_gathered = nullptr) {
     const Params& p = c->p;
     const size_t NT = (size_t)p.D * p.D * p.D;
     if (cap && launch_cap(c, 0, n)) return fail(c, TDM_ECUDA, "cap mapping launch failed");
@@ -589,7 +620,9 @@ static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t
     if (im && out.im != im) out.host_im = im;
     if (otf && out.otf != otf) out.host_otf = otf;
     if (cnt && out.cnt != cnt) out.host_cnt = cnt;
-    if (int rc = launch_volume(c, n, out)) return fail(c, rc, "volume launch failed");
+    if (int rc = launch_volume(c, n, out, st ? st : c->stream, rec ? rec : b.rec, posspec ? posspec : b.posspec,
+                               ev_gathered))
+        return fail(c, rc, "volume launch failed");
     const bool host = out.host_re || out.host_im || out.host_otf || out.host_cnt;
     return host && wait ? tdm_synchronize(c) : TDM_OK;
 }
@@ -616,6 +649,7 @@ int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_i
                     float* absorption_out, uint8_t* otf_out, uint32_t* counts_out) {
     if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, "tdm_reconstruct: invalid argument");
     cudaSetDevice(c->device);
+    TDM_CU(join_volume(c));
     const size_t FF = (size_t)c->p.F * c->p.F;
     if ((!fields_in || !posspec_in) && n > c->n_fields)
         return fail(c, TDM_EINVAL, "tdm_reconstruct: fewer fields in the context than requested");
@@ -672,6 +706,16 @@ static int pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indic
     if (!c || !holos || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
         return fail(c, TDM_EINVAL, "tdm_pipeline: invalid argument");
     cudaSetDevice(c->device);
+    // The per-angle stages run on c->stream, the volume stage on vol_stream, so
+    // that this call's volume stage overlaps the next call's per-angle stages.
+    // This call's cap records go to rec_buf[par], after the gather of two calls
+    // ago has read it; the specular positions its gather reads are copied aside.
+    const int par = c->rec_parity;
+    c->b.rec = c->b.rec_buf[par];
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TDM_CU(cudaStreamIsCapturing(c->stream, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (!capturing) TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_rec_free[par], 0));  // a graph is ordered by its launches
     TDM_CU(cudaEventRecord(c->ev_stage[0], c->stream));
     if (int rc = stage_angles(c, holos, bits, n)) return rc;
     TDM_CU(cudaEventRecord(c->ev_stage[1], c->stream));  // extract, fields and map are interleaved
@@ -683,8 +727,16 @@ static int pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indic
         Launch l(c, K_POSSPEC);
         k_unpack_posspec<<<(n + 255) / 256, 256, 0, c->stream>>>(c->b.posspec, n, posspec_out);
     }
-    int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out, wait);
+    TDM_CU(cudaMemcpyAsync(c->b.posspec_vol[par], c->b.posspec, n * sizeof(int2), cudaMemcpyDeviceToDevice,
+                           c->stream));
+    TDM_CU(cudaEventRecord(c->ev_angles, c->stream));
+    TDM_CU(cudaStreamWaitEvent(c->vol_stream, c->ev_angles, 0));
+    int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out, wait, c->vol_stream,
+                        c->b.rec_buf[par], c->b.posspec_vol[par], c->ev_rec_free[par]);
     if (rc) return rc;
+    TDM_CU(cudaEventRecord(c->ev_vol_last, c->vol_stream));
+    c->rec_parity ^= 1;
+    if (capturing) TDM_CU(join_volume(c));  // a capture must end joined
     if (posspec_out && !is_device_ptr(posspec_out)) {
         std::vector<int2> tmp(n);
         TDM_CU(cudaMemcpyAsync(tmp.data(), c->b.posspec, n * sizeof(int2), cudaMemcpyDeviceToHost, c->stream));
@@ -722,6 +774,7 @@ static int ensure_operator_buffers(tdm_ctx* c) {
 static int operator_setup(tdm_ctx* c, int n, const int32_t* posspec, const char* who) {
     if (!c || n <= 0 || n > c->max_angles) return fail(c, TDM_EINVAL, std::string(who) + ": invalid argument");
     cudaSetDevice(c->device);
+    TDM_CU(join_volume(c));
     if (posspec) {
         if (int rc = set_posspec(c, posspec, n, who)) return rc;
         c->n_fields = std::max(c->n_fields, n);
@@ -934,7 +987,7 @@ int tdm_autotune(tdm_ctx* c, const void* holos, int bits, int n, int* chunk_out)
         rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);  // warm-up
         if (!rc && cudaEventRecord(t0, c->stream) != cudaSuccess) rc = TDM_ECUDA;
         for (int r = 0; r < 2 && !rc; ++r) rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);
-        if (!rc && cudaEventRecord(t1, c->stream) != cudaSuccess) rc = TDM_ECUDA;
+        if (!rc && (join_volume(c) != cudaSuccess || cudaEventRecord(t1, c->stream) != cudaSuccess)) rc = TDM_ECUDA;
         if (!rc) rc = tdm_synchronize(c);
         float ms = 0;
         if (!rc && cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) rc = TDM_ECUDA;

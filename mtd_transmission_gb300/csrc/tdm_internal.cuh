@@ -55,7 +55,9 @@ struct Buffers {
     unsigned* fit_done = nullptr;  // chunk x 2 finished-slice counters (zero between launches)
     float2* fields = nullptr;      // max_angles x F*F
     float2* r1 = nullptr;          // chunk x F*F
-    float4* rec = nullptr;         // max_angles x F*F cap records (contribution re, im; plane; unused)
+    float4* rec = nullptr;         // max_angles x F*F cap records (contribution re, im; plane; unused): rec_buf[i]
+    float4* rec_buf[2] = {};       // the two cap-record buffers of consecutive pipeline calls
+    int2* posspec_vol[2] = {};     // max_angles: specular positions read by the volume stage of those calls
     float2* vol = nullptr;         // D^3 complex, [y][x][z] layout
     float* out_re = nullptr;       // D^3 staging when the caller's output is in host memory
     float* out_im = nullptr;
@@ -105,6 +107,14 @@ struct tdm_ctx {
     cudaStream_t copy_stream = nullptr;  // hologram uploads
     cudaStream_t dl_stream = nullptr;    // output downloads (a second copy engine)
     cudaEvent_t ev_dl_done = nullptr;    // last download of the previous volume
+    // tdm_pipeline runs each volume's stage (gather, z/y/x passes) on vol_stream, so that it
+    // overlaps the next call's per-angle stages; the cap records and the specular positions the
+    // volume stage reads are double buffered
+    cudaStream_t vol_stream = nullptr;
+    cudaEvent_t ev_angles = nullptr;     // per-angle stages of the current call done (stream)
+    cudaEvent_t ev_vol_last = nullptr;   // last volume stage queued on vol_stream
+    cudaEvent_t ev_rec_free[2] = {};     // gather that read rec_buf[i] done
+    int rec_parity = 0;
     cudaEvent_t ev_copy[2] = {nullptr, nullptr};
     cudaEvent_t ev_free[2] = {nullptr, nullptr};
     cudaEvent_t ev_stage[8] = {};
@@ -124,17 +134,18 @@ cudaEvent_t prof_event(tdm_ctx* c);
 struct Launch {
     tdm_ctx* c;
     int id;
+    cudaStream_t st;
     cudaEvent_t b = nullptr;
-    Launch(tdm_ctx* ctx, int kid) : c(ctx), id(kid) {
+    Launch(tdm_ctx* ctx, int kid, cudaStream_t stream = nullptr) : c(ctx), id(kid), st(stream ? stream : ctx->stream) {
         if (c->prof) {
             cudaEvent_t a = prof_event(c);
             b = prof_event(c);
-            cudaEventRecord(a, c->stream);
+            cudaEventRecord(a, st);
             c->prof_recs.push_back(ProfRec{id, a, b});
         }
     }
     ~Launch() {
-        if (b) cudaEventRecord(b, c->stream);
+        if (b) cudaEventRecord(b, st);
         c->launches++;
     }
 };
@@ -183,8 +194,11 @@ int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float4* recs);
 int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
                    float tv_n, float tv_k, float eps, float nlo, float nhi, float klo, float khi, float* xn_out,
                    float* xk_out);
-// gather, normalisation and 3D inverse FFT of fields [0, n) into the outputs.
-// Downloads run on c->dl_stream and end with c->ev_dl_done; the staging
-// buffers are not written before the previous volume's downloads are done.
-int launch_volume(tdm_ctx* c, int n, const VolumeOut& out);
+// gather of the cap records rec (angles [0, n), specular positions posspec),
+// normalisation and 3D inverse FFT into the outputs, on stream st.  Downloads
+// run on c->dl_stream and end with c->ev_dl_done; the staging buffers are not
+// written before the previous volume's downloads are done.  ev_gathered (may
+// be null) is recorded on st once the gather has read rec.
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float4* rec, const int2* posspec,
+                  cudaEvent_t ev_gathered);
 }  // namespace tdm
