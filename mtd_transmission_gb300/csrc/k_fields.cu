@@ -167,6 +167,11 @@ struct VCfg {
     static constexpr int B = 3 * P;             // transforms per CTA
     static constexpr int NT = B * W::T;
     static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
+    static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;  // pass-2 transform stride, 2 mod 16
+    static constexpr int LSZ = L + 2;                                  // pass-2 phasor stride, 2 mod 16
+    static constexpr int LSG = L + 4;                                  // pass-2 gradient stride, 4 mod 32
+    static constexpr size_t SMEM_COLS =
+        ((size_t)B * VS + (size_t)2 * P * LSZ) * sizeof(float2) + (size_t)2 * P * LSG * sizeof(float);
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
@@ -228,10 +233,14 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
               const float2* __restrict__ tw, float2* __restrict__ qc) {
     using C = VCfg<L>;
     using W = typename C::W;
-    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P, NC = 2 * P, NT = C::NT, LS = L + 1;
+    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P, NC = 2 * P, NT = C::NT;
+    // Strides chosen for the staging pattern (a warp writes NC = 8 columns x 4
+    // rows): transform arrays and phasors 2 mod 16 float2 apart, gradients
+    // 4 mod 32 floats apart, so the 32 lanes of each store hit distinct banks.
+    constexpr int VS = C::VS, LS = C::LSZ, LG = C::LSG;
     extern __shared__ float2 sm[];
-    float2* szp = sm + C::B * W::STRIDE;                        // NC x LS exp(i phase) along the mirror column
-    float* sgx = reinterpret_cast<float*>(szp + NC * LS);       // NC x LS gx along the mirror column
+    float2* szp = sm + C::B * VS;                               // NC x LS exp(i phase) along the mirror column
+    float* sgx = reinterpret_cast<float*>(szp + NC * LS);       // NC x LG gx along the mirror column
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const bool zk = tr < NC;
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
@@ -241,17 +250,17 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
         const size_t src = ((size_t)a * F + mirror(Y, F)) * F + x0 + c;
         const float2 z = zph[src];
         szp[c * LS + Y] = z;
-        sgx[c * LS + Y] = gxh[src];
-        sm[c * W::STRIDE + W::pad(Y)] = z;
-        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * W::STRIDE + W::pad(Y)])[c & 1] = phase[src];
+        sgx[c * LG + Y] = gxh[src];
+        sm[c * VS + W::pad(Y)] = z;
+        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * VS + W::pad(Y)])[c & 1] = phase[src];
     }
     __syncthreads();
-    float2* s = sm + tr * W::STRIDE;
+    float2* s = sm + tr * VS;
     fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
     __syncthreads();
     if (zk) {  // warp-uniform
         const int c = tr;
-        const float2* sp = sm + (NC + (c >> 1)) * W::STRIDE;
+        const float2* sp = sm + (NC + (c >> 1)) * VS;
 #pragma unroll 8
         for (int n1 = 0; n1 < E; ++n1) {
             const int Y = j + n1 * T;
@@ -259,7 +268,7 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
             const float2 g = s[j + n1 * (T + 1)];
             const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
             const float2 q = sp[j + n1 * (T + 1)];
-            s[j + n1 * (T + 1)] = make_float2(sgx[c * LS + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
+            s[j + n1 * (T + 1)] = make_float2(sgx[c * LG + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
         }
         __syncwarp();
         fft_warp_call<L, -1>(s, j, tw);
@@ -268,7 +277,7 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, ky = i / NC;
-        qc[((size_t)a * L + ky) * F + x0 + c] = sm[c * W::STRIDE + W::pad(ky)];
+        qc[((size_t)a * L + ky) * F + x0 + c] = sm[c * VS + W::pad(ky)];
     }
 }
 
@@ -473,7 +482,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
     const size_t sm_vrows = (size_t)VC::B * VC::W::STRIDE * sizeof(float2);
-    const size_t sm_vcols = sm_vrows + (size_t)2 * VC::P * (L + 1) * (sizeof(float2) + sizeof(float));
+    const size_t sm_vcols = VC::SMEM_COLS;
     if (allow_smem(k_field_rows<F>, FC::SMEM) || allow_smem(k_field_cols<F>, FC::SMEM) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
         allow_smem(k_volkov_integ_rows<L>, IC::SMEM) || allow_smem(k_volkov_integ_cols<L>, IC::SMEM))
