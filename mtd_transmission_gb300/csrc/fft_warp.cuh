@@ -172,27 +172,17 @@ struct WarpFFT {
     __host__ __device__ static constexpr int pad(int i) { return i + (i >> LOG_T); }
 };
 
-// x[k1] *= W_N^(DIR j k1), k1 = 1 .. E-1, from the [k1][j] table.  The loads
-// are issued in groups of 8 behind a compiler barrier so that they do not all
-// become live at once (E - 1 twiddles would otherwise double the registers).
+// x[k1] *= W_N^(DIR j k1), k1 = 1 .. E-1, from the [k1][j] table (L1-cached
+// loads, all independent).
 template <int N, int DIR>
 __device__ __forceinline__ void twiddle_lane(float2 (&x)[WarpFFT<N>::E], const float2* __restrict__ twr, int j) {
     using W = WarpFFT<N>;
     constexpr int E = W::E, T = W::T;
 #pragma unroll
-    for (int g = 0; g < E; g += 8) {
-        float2 w[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if (g + i > 0) w[i] = __ldg(&twr[(g + i) * T + j]);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (g + i > 0) {
-                if constexpr (DIR > 0) w[i].y = -w[i].y;
-                x[g + i] = c_mul(x[g + i], w[i]);
-            }
-        }
-        asm volatile("" ::: "memory");
+    for (int k1 = 1; k1 < E; ++k1) {
+        float2 w = __ldg(&twr[k1 * T + j]);
+        if constexpr (DIR > 0) w.y = -w.y;
+        x[k1] = c_mul(x[k1], w);
     }
 }
 
