@@ -189,12 +189,14 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 
 // ---------------------------------------------------------------- cap accumulation
 // One warp per voxel column (X, Y); the lanes take 32 consecutive angles at a
-// time.  An angle hits a column at most once, at one plane; lanes whose hits
-// share a plane are grouped and the group's lowest lane sums the members'
-// contributions in ascending angle order (FP32, at most 32 terms, usually
-// one) and adds the sum to the plane's FP64 accumulator in shared memory, so
-// the running sum over the angles is FP64.  The sums are deterministic and
-// the hit counts exact.
+// time, the next group's records loaded while the current one is added.  An
+// angle hits a column at most once, at one plane, and the column's running
+// sums live in FP64 in shared memory.  When the group's planes are distinct
+// (the usual case, seen through a plane -> lane ownership table) every lane
+// adds its own hit; otherwise lanes sharing a plane are grouped and the
+// group's lowest lane sums the members in ascending angle order (FP32, at most
+// 32 terms) before adding the sum.  The sums are deterministic, the hit
+// counts exact.
 constexpr int kGW = 8;  // warps per CTA; a CTA covers 32 consecutive x at one y
 
 template <int D>
@@ -203,13 +205,15 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
              float2* __restrict__ vol, uint32_t* __restrict__ cnt_out, int normalize) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int band = p.band;
-    double2* acc_all = reinterpret_cast<double2*>(smraw);                // kGW x band
-    float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);   // kGW x 32
-    uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32); // kGW x band
-    int2* sp = reinterpret_cast<int2*>(cnt_all + ((kGW * band + 3) & ~3));  // M
+    double2* acc_all = reinterpret_cast<double2*>(smraw);                   // kGW x band
+    float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);      // kGW x 32
+    uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32);    // kGW x band
+    uint8_t* own_all = reinterpret_cast<uint8_t*>(cnt_all + kGW * band);    // kGW x band
+    int2* sp = reinterpret_cast<int2*>(own_all + ((kGW * band + 7) & ~7));  // M
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double2* acc = acc_all + w * band;
     uint16_t* cnt = cnt_all + w * band;
+    uint8_t* own = own_all + w * band;
     float2* stg = stg_all + w * 32;
     for (int i = threadIdx.x; i < M; i += kGW * 32) sp[i] = posspec[i];
     __syncthreads();
@@ -225,37 +229,51 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
             acc[e] = make_double2(0.0, 0.0);
             cnt[e] = 0;
         }
-        __syncwarp();
-        for (int a0 = 0; a0 < M; a0 += 32) {
-            const int a = a0 + lane;
-            int e = -1;
-            float2 v = make_float2(0.f, 0.f);
+        // record of angle a for this column, or plane -1 when its window misses the column
+        auto fetch = [&](int a) {
+            float4 r = make_float4(0.f, 0.f, __int_as_float(-1), 0.f);
             if (a < M) {
                 const int2 q = sp[a];
-                if ((unsigned)(bx + q.x) < (unsigned)F && (unsigned)(by + q.y) < (unsigned)F) {
-                    const float4 r = __ldg(&rec[(size_t)a * FF + koff]);
-                    const int z = __float_as_int(r.z);
-                    if (z >= 0) {
-                        e = z - zmin;
-                        v = make_float2(r.x, r.y);
-                    }
-                }
+                if ((unsigned)(bx + q.x) < (unsigned)F && (unsigned)(by + q.y) < (unsigned)F)
+                    r = __ldg(&rec[(size_t)a * FF + koff]);
             }
-            const unsigned grp = __match_any_sync(0xffffffffu, e >= 0 ? e : -1 - lane);
-            stg[lane] = v;
+            return r;
+        };
+        float4 nxt = fetch(lane);
+        __syncwarp();
+        for (int a0 = 0; a0 < M; a0 += 32) {
+            const float4 r = nxt;
+            nxt = fetch(a0 + 32 + lane);
+            const int z = __float_as_int(r.z);
+            const int e = z >= 0 ? z - zmin : -1;
+            if (e >= 0) own[e] = (uint8_t)lane;
             __syncwarp();
-            if (e >= 0 && (grp & ((1u << lane) - 1)) == 0) {  // lowest lane of its plane group
-                float sx = 0.0f, sy = 0.0f;
-                for (unsigned g = grp; g; g &= g - 1) {
-                    const float2 u = stg[__ffs(g) - 1];
-                    sx += u.x;
-                    sy += u.y;
+            const bool shared_plane = e >= 0 && own[e] != lane;
+            if (!__any_sync(0xffffffffu, shared_plane)) {
+                if (e >= 0) {
+                    double2 t = acc[e];
+                    t.x += (double)r.x;
+                    t.y += (double)r.y;
+                    acc[e] = t;
+                    cnt[e]++;
                 }
-                double2 t = acc[e];
-                t.x += (double)sx;
-                t.y += (double)sy;
-                acc[e] = t;
-                cnt[e] += (uint16_t)__popc(grp);
+            } else {
+                const unsigned grp = __match_any_sync(0xffffffffu, e >= 0 ? e : -1 - lane);
+                stg[lane] = make_float2(r.x, r.y);
+                __syncwarp();
+                if (e >= 0 && (grp & ((1u << lane) - 1)) == 0) {  // lowest lane of its plane group
+                    float sx = 0.0f, sy = 0.0f;
+                    for (unsigned g = grp; g; g &= g - 1) {
+                        const float2 u = stg[__ffs(g) - 1];
+                        sx += u.x;
+                        sy += u.y;
+                    }
+                    double2 t = acc[e];
+                    t.x += (double)sx;
+                    t.y += (double)sy;
+                    acc[e] = t;
+                    cnt[e] += (uint16_t)__popc(grp);
+                }
             }
             __syncwarp();
         }
@@ -275,7 +293,6 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
     }
 }
 
-// Volume passes: B transforms of D points per CTA on the warp-resident FFT.
 template <int D>
 struct PassCfg {
     using W = WarpFFT<D>;
@@ -616,7 +633,8 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     Buffers& b = c->b;
     const Params& p = c->p;
     const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-                        (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
+                        (size_t)kGW * p.band * sizeof(uint16_t) + (size_t)((kGW * p.band + 7) & ~7) +
+                        (size_t)n * sizeof(int2);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
@@ -719,7 +737,8 @@ int adjoint_impl(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bo
     Buffers& b = c->b;
     const Params& p = c->p;
     const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-                        (size_t)((kGW * p.band + 3) & ~3) * sizeof(uint16_t) + (size_t)n * sizeof(int2);
+                        (size_t)kGW * p.band * sizeof(uint16_t) + (size_t)((kGW * p.band + 7) & ~7) +
+                        (size_t)n * sizeof(int2);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
