@@ -407,7 +407,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rytov_1024")
-    ap.add_argument("--e2e-steps", type=int, default=16)
+    ap.add_argument("--e2e-steps", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=12)
     ap.add_argument("--ref-sample", type=int, default=8)
@@ -524,6 +524,10 @@ def main():
         for _ in range(args.e2e_steps):
             ctx.pipeline(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
         e2e_sync_s = time.perf_counter() - t0
+        for k in range(2):  # warm-up of the pipelined path (both output sets), untimed
+            h_re, h_im, h_otf = h_outs[k % 2]
+            ctx.pipeline_async(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
+        ctx.synchronize()
         barrier()
         t0 = time.perf_counter()
         for k in range(args.e2e_steps):

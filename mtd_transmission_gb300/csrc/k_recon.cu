@@ -20,6 +20,7 @@
 #include "tdm_internal.cuh"
 #include "fft_warp.cuh"
 #include "form.cuh"
+#include "fp_bits.cuh"
 
 namespace tdm {
 namespace {
@@ -188,39 +189,78 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 }
 
 // ---------------------------------------------------------------- cap accumulation
-// One warp per voxel column (X, Y); the lanes take 32 consecutive angles at a
-// time, the next group's records loaded while the current one is added.  An
-// angle hits a column at most once, at one plane, and the column's running
-// sums live in FP64 in shared memory.  When the group's planes are distinct
-// (the usual case, seen through a plane -> lane ownership table) every lane
-// adds its own hit; otherwise lanes sharing a plane are grouped and the
-// group's lowest lane sums the members in ascending angle order (FP32, at most
-// 32 terms) before adding the sum.  The sums are deterministic, the hit
-// counts exact.
-constexpr int kGW = 8;  // warps per CTA; a CTA covers 32 consecutive x at one y
+// One warp per voxel column (X, Y); a CTA covers 32 consecutive X at one Y.
+// An angle's cap window is the F x F bins around its specular position, so a
+// column is covered by a fraction of the angles: the CTA first lists, in
+// ascending order, the angles whose window covers row Y and any of its 32
+// columns.  The lanes then take 32 consecutive listed angles at a time, the
+// next group's records loaded while the current one is added; groups without
+// a hit are skipped.  An angle hits a column at most once, at one plane, and
+// the column's running sums live in FP64 in shared memory.  When the group's
+// planes are distinct (seen through a plane -> lane ownership table) every
+// lane adds its own hit; otherwise lanes sharing a plane are grouped and the
+// group's lowest lane sums the members in ascending angle order (FP32, at
+// most 32 terms) before adding the sum.  The sums are deterministic, the hit
+// counts exact.  Widening the FP32 hits and narrowing the sums are done on
+// the integer pipe (fp_bits.cuh), so the FP64 pipe only adds.
+constexpr int kGW = 8;  // warps per CTA
+
+// Dynamic shared memory of k_accumulate: per warp the band's sums, counts and
+// owners plus a 32-lane staging row, and the CTA's list of n angles at most.
+size_t gather_smem(int band, int n) {
+    return (size_t)kGW * band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
+           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 7) & ~7) + (size_t)n * sizeof(int2);
+}
 
 template <int D>
 __global__ void __launch_bounds__(kGW * 32)
 k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, int M, Params p,
              float2* __restrict__ vol, uint32_t* __restrict__ cnt_out, int normalize) {
     extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ int s_wc[kGW];
+    __shared__ int s_listed;
     const int band = p.band;
     double2* acc_all = reinterpret_cast<double2*>(smraw);                   // kGW x band
     float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);      // kGW x 32
     uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32);    // kGW x band
     uint8_t* own_all = reinterpret_cast<uint8_t*>(cnt_all + kGW * band);    // kGW x band
-    int2* sp = reinterpret_cast<int2*>(own_all + ((kGW * band + 7) & ~7));  // M
+    int2* list = reinterpret_cast<int2*>(own_all + ((kGW * band + 7) & ~7));  // (q.x, angle), <= M
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double2* acc = acc_all + w * band;
     uint16_t* cnt = cnt_all + w * band;
     uint8_t* own = own_all + w * band;
     float2* stg = stg_all + w * 32;
-    for (int i = threadIdx.x; i < M; i += kGW * 32) sp[i] = posspec[i];
-    __syncthreads();
     const int F = p.F, h = D / 2, zmin = p.zmin;
     const size_t FF = (size_t)F * F;
     const int Y = blockIdx.y;
     const int by = Y - h;
+    const int bx0 = blockIdx.x * 32 - h;
+    // the angles whose window covers row Y and one of the columns bx0 .. bx0 + 31
+    if (threadIdx.x == 0) s_listed = 0;
+    __syncthreads();
+    for (int a0 = 0; a0 < M; a0 += kGW * 32) {
+        const int a = a0 + threadIdx.x;
+        int2 q = make_int2(0, 0);
+        bool keep = false;
+        if (a < M) {
+            q = posspec[a];
+            keep = (unsigned)(by + q.y) < (unsigned)F && bx0 + 31 + q.x >= 0 && bx0 + q.x < F;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) s_wc[w] = __popc(bal);
+        __syncthreads();
+        int off = s_listed;
+        for (int k = 0; k < w; ++k) off += s_wc[k];
+        if (keep) list[off + __popc(bal & ((1u << lane) - 1u))] = make_int2(q.x, a);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = s_listed;
+            for (int k = 0; k < kGW; ++k) t += s_wc[k];
+            s_listed = t;
+        }
+        __syncthreads();
+    }
+    const int listed = s_listed;
     for (int cx = 0; cx < 32; cx += kGW) {
         const int X = blockIdx.x * 32 + cx + w;
         const int bx = X - h;  // fd + N = X - D/2 + posSpec
@@ -229,31 +269,31 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
             acc[e] = make_double2(0.0, 0.0);
             cnt[e] = 0;
         }
-        // record of angle a for this column, or plane -1 when its window misses the column
-        auto fetch = [&](int a) {
+        // record of listed angle i for this column, or plane -1 when its window misses the column
+        auto fetch = [&](int i) {
             float4 r = make_float4(0.f, 0.f, __int_as_float(-1), 0.f);
-            if (a < M) {
-                const int2 q = sp[a];
-                if ((unsigned)(bx + q.x) < (unsigned)F && (unsigned)(by + q.y) < (unsigned)F)
-                    r = __ldg(&rec[(size_t)a * FF + koff]);
+            if (i < listed) {
+                const int2 q = list[i];
+                if ((unsigned)(bx + q.x) < (unsigned)F) r = __ldg(&rec[(size_t)q.y * FF + koff]);
             }
             return r;
         };
         float4 nxt = fetch(lane);
         __syncwarp();
-        for (int a0 = 0; a0 < M; a0 += 32) {
+        for (int g0 = 0; g0 < listed; g0 += 32) {
             const float4 r = nxt;
-            nxt = fetch(a0 + 32 + lane);
+            nxt = fetch(g0 + 32 + lane);
             const int z = __float_as_int(r.z);
             const int e = z >= 0 ? z - zmin : -1;
+            if (!__any_sync(0xffffffffu, e >= 0)) continue;
             if (e >= 0) own[e] = (uint8_t)lane;
             __syncwarp();
             const bool shared_plane = e >= 0 && own[e] != lane;
             if (!__any_sync(0xffffffffu, shared_plane)) {
                 if (e >= 0) {
                     double2 t = acc[e];
-                    t.x += (double)r.x;
-                    t.y += (double)r.y;
+                    t.x += widen(r.x);
+                    t.y += widen(r.y);
                     acc[e] = t;
                     cnt[e]++;
                 }
@@ -269,8 +309,8 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
                         sy += u.y;
                     }
                     double2 t = acc[e];
-                    t.x += (double)sx;
-                    t.y += (double)sy;
+                    t.x += widen(sx);
+                    t.y += widen(sy);
                     acc[e] = t;
                     cnt[e] += (uint16_t)__popc(grp);
                 }
@@ -281,10 +321,13 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
         // stands for the first fftshift3D
         float2* col = vol + ((size_t)Y * D + X) * D + zmin;
         for (int e = lane; e < band; e += 32) {
-            const double2 t = acc[e];
             const unsigned n = cnt[e];
-            const float dn = (n && normalize) ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
-            float2 val = make_float2((float)t.x / dn, (float)t.y / dn);
+            float2 val = make_float2(0.0f, 0.0f);
+            if (n) {
+                const double2 t = acc[e];
+                const float dn = normalize ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
+                val = make_float2(narrow(t.x) / dn, narrow(t.y) / dn);
+            }
             if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
             col[e] = val;
             if (cnt_out) cnt_out[((size_t)(zmin + e) * D + Y) * D + X] = n;
@@ -632,9 +675,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-                        (size_t)kGW * p.band * sizeof(uint16_t) + (size_t)((kGW * p.band + 7) & ~7) +
-                        (size_t)n * sizeof(int2);
+    const size_t sm_a = gather_smem(p.band, n);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
@@ -736,9 +777,7 @@ int adjoint_impl(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bo
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    const size_t sm_a = (size_t)kGW * p.band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-                        (size_t)kGW * p.band * sizeof(uint16_t) + (size_t)((kGW * p.band + 7) & ~7) +
-                        (size_t)n * sizeof(int2);
+    const size_t sm_a = gather_smem(p.band, n);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
     if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
