@@ -681,9 +681,11 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
-    const bool host_out = out.host_re || out.host_im || out.host_otf || out.host_cnt;
-    // the staging buffers may still be downloading the previous volume
-    if (host_out && cudaStreamWaitEvent(st, c->ev_dl_done, 0)) return TDM_ECUDA;
+    // A staged output part may still be downloading from the previous volume:
+    // each part's writer waits for that part's download (ev_dl) just before it runs.
+    auto staged_free = [&](int part) { return cudaStreamWaitEvent(st, c->ev_dl[part], 0); };
+    auto downloaded = [&](int part) { return cudaEventRecord(c->ev_dl[part], c->dl_stream); };
+    if (out.host_cnt && staged_free(kOutSlabs)) return TDM_ECUDA;
     if (cnt) {  // planes outside the cap band carry no hits
         const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
         cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), st);
@@ -697,18 +699,19 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     cudaEventRecord(c->ev_stage[5], st);
     if (ev_gathered && cudaEventRecord(ev_gathered, st)) return TDM_ECUDA;
     const size_t NT = (size_t)D * D * D;
-    bool downloads = false;
     if (out.host_cnt) {
-        if (download_after(c, st, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t))) return TDM_ECUDA;
-        downloads = true;
+        if (download_after(c, st, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t)) ||
+            downloaded(kOutSlabs))
+            return TDM_ECUDA;
     }
+    if (out.host_otf && staged_free(kOutSlabs + 1)) return TDM_ECUDA;
     {
         Launch l(c, K_ZPASS, st);
         k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, st>>>(b.vol, b.tw, p.zmin, p.band, otf);
     }
     if (out.host_otf) {
-        if (download_after(c, st, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT)) return TDM_ECUDA;
-        downloads = true;
+        if (download_after(c, st, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT) || downloaded(kOutSlabs + 1))
+            return TDM_ECUDA;
     }
     {
         Launch l(c, K_YPASS, st);
@@ -719,6 +722,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     const int zblocks = D / P::B, nslab = host_vol ? (zblocks < kOutSlabs ? zblocks : kOutSlabs) : 1;
     for (int sl = 0; sl < nslab; ++sl) {
         const int zb0 = sl * zblocks / nslab, zb1 = (sl + 1) * zblocks / nslab;
+        if (host_vol && staged_free(sl)) return TDM_ECUDA;
         {
             Launch l(c, K_XPASS, st);
             k_xpass<D><<<dim3(zb1 - zb0, D), P::NT, sm_p, st>>>(b.vol, b.tw, p.out_scale, zb0, re, im);
@@ -733,11 +737,10 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
             if (out.host_im && cudaMemcpyAsync(out.host_im + off, im + off, len * sizeof(float),
                                                cudaMemcpyDeviceToHost, c->dl_stream))
                 return TDM_ECUDA;
-            downloads = true;
+            if (downloaded(sl)) return TDM_ECUDA;
         }
     }
     cudaEventRecord(c->ev_stage[6], st);
-    if (downloads && cudaEventRecord(c->ev_dl_done, c->dl_stream)) return TDM_ECUDA;
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 

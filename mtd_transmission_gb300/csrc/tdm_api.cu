@@ -302,7 +302,9 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->vol_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_dl_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_lane_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_lane_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_angles, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_vol_last, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_rec_free[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -316,6 +318,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     }
     for (auto& e : c->ev_stage) cudaEventCreate(&e);
     for (auto& e : c->ev_out) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    for (auto& e : c->ev_dl) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk_cap, L = p.L;
     TRY(dev_alloc(c, &b.tw, kTwTotal));
@@ -376,6 +379,7 @@ int tdm_destroy(tdm_ctx* c) {
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
     if (c->vol_stream) cudaStreamSynchronize(c->vol_stream);
+    if (c->lane_stream) cudaStreamSynchronize(c->lane_stream);
     free_all(c);
     for (int i = 0; i < 2; ++i) {
         if (c->ev_copy[i]) cudaEventDestroy(c->ev_copy[i]);
@@ -385,13 +389,17 @@ int tdm_destroy(tdm_ctx* c) {
         if (e) cudaEventDestroy(e);
     for (auto& e : c->ev_out)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->ev_dl)
+        if (e) cudaEventDestroy(e);
     prof_release(c);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
     if (c->vol_stream) cudaStreamDestroy(c->vol_stream);
-    for (cudaEvent_t e : {c->ev_dl_done, c->ev_angles, c->ev_vol_last, c->ev_rec_free[0], c->ev_rec_free[1]})
+    if (c->lane_stream) cudaStreamDestroy(c->lane_stream);
+    for (cudaEvent_t e : {c->ev_angles, c->ev_vol_last, c->ev_rec_free[0], c->ev_rec_free[1],
+                          c->ev_lane_fork, c->ev_lane_join})
         if (e) cudaEventDestroy(e);
     delete c;
     return TDM_OK;
@@ -437,6 +445,7 @@ int tdm_synchronize(tdm_ctx* c) {
     TDM_CU(cudaStreamSynchronize(c->copy_stream));
     TDM_CU(cudaStreamSynchronize(c->vol_stream));
     TDM_CU(cudaStreamSynchronize(c->dl_stream));
+    TDM_CU(cudaStreamSynchronize(c->lane_stream));
     TDM_CU(cudaStreamSynchronize(c->stream));
     int err = 0;
     TDM_CU(cudaMemcpy(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -667,17 +676,65 @@ int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_i
     return TDM_OK;
 }
 
+// Scratch of the per-angle stages (the buffers sized chunk_cap angles) seen
+// from chunk slot s on: the slots [s, s + chunk) of each.
+struct ChunkScratch {
+    float2 *inter, *argpart, *I1, *zph, *qc, *tq, *r1;
+    float *phase, *amp, *gx, *unwrapped, *fit_part;
+    double* beta;
+    unsigned* fit_done;
+};
+
+static ChunkScratch scratch_at(const tdm_ctx* c, int s) {
+    const Buffers& b = c->b;
+    const size_t FF = (size_t)c->p.F * c->p.F, LF = (size_t)c->p.L * c->p.F, S = (size_t)s;
+    return ChunkScratch{b.inter + S * c->p.F * c->p.H, b.argpart + S * kArgPartsMax, b.I1 + S * FF, b.zph + S * FF,
+                        b.qc + S * LF, b.tq + S * LF, b.r1 + S * FF, b.phase + S * FF, b.amp + S * FF,
+                        b.gx + S * FF, b.unwrapped + S * FF, b.fit_part + S * 2 * 8 * kNC, b.beta + S * 2 * kNC,
+                        b.fit_done + S * 2};
+}
+
+static void use_scratch(tdm_ctx* c, const ChunkScratch& k) {
+    Buffers& b = c->b;
+    b.inter = k.inter, b.argpart = k.argpart, b.I1 = k.I1, b.zph = k.zph, b.qc = k.qc, b.tq = k.tq, b.r1 = k.r1;
+    b.phase = k.phase, b.amp = k.amp, b.gx = k.gx, b.unwrapped = k.unwrapped, b.fit_part = k.fit_part;
+    b.beta = k.beta, b.fit_done = k.fit_done;
+}
+
 // Per-angle stages of the pipeline, streamed by hologram chunk: for each
 // chunk, extraction, field formation and cap mapping run back to back (the
 // chunk's spectra and fields stay in L2), and with host holograms the upload
-// of the next chunk overlaps them.
+// of the next chunk overlaps them.  When the scratch buffers hold two chunks,
+// consecutive chunks run at once on two streams (the per-chunk grids fill a
+// fraction of the GPU): even chunks on c->stream with the lower slots, odd
+// ones on lane_stream with the upper slots, joined back at the end.  The
+// launchers read c->stream and the scratch pointers, which are switched per
+// chunk here and restored on every return.
 static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
     const Params& p = c->p;
     const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
     const bool dev = is_device_ptr(holos);
     const size_t stage_bytes = (size_t)c->chunk_cap * p.H * p.H * 2;  // one staging half
+    const bool two = 2 * c->chunk <= c->chunk_cap && n > c->holo_chunk;
+    struct Restore {
+        tdm_ctx* c;
+        cudaStream_t main;
+        ChunkScratch base;
+        ~Restore() {
+            c->stream = main;
+            use_scratch(c, base);
+        }
+    } restore{c, c->stream, scratch_at(c, 0)};
+    const ChunkScratch upper = scratch_at(c, c->chunk);
+    if (two) {
+        TDM_CU(cudaEventRecord(c->ev_lane_fork, restore.main));
+        TDM_CU(cudaStreamWaitEvent(c->lane_stream, c->ev_lane_fork, 0));
+    }
     for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
         const int m = std::min(c->holo_chunk, n - h0);
+        const bool odd = two && (k & 1);
+        c->stream = odd ? c->lane_stream : restore.main;
+        use_scratch(c, odd ? upper : restore.base);
         const void* src = static_cast<const char*>(holos) + h0 * per;
         const int buf = k & 1;
         if (!dev) {
@@ -697,6 +754,10 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
         if (int rc = launch_fields(c, h0, m, nullptr, nullptr, nullptr, parts, !form_in_cap))
             return fail(c, rc, "fields launch failed");
         if (int rc = launch_cap(c, h0, m, form_in_cap)) return fail(c, rc, "cap mapping launch failed");
+    }
+    if (two) {
+        TDM_CU(cudaEventRecord(c->ev_lane_join, c->lane_stream));
+        TDM_CU(cudaStreamWaitEvent(restore.main, c->ev_lane_join, 0));
     }
     return TDM_OK;
 }

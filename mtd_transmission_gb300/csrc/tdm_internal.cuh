@@ -106,11 +106,17 @@ struct tdm_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // hologram uploads
     cudaStream_t dl_stream = nullptr;    // output downloads (a second copy engine)
-    cudaEvent_t ev_dl_done = nullptr;    // last download of the previous volume
+    // downloads of the staged outputs done, per part (x-pass slabs, then counts, then OTF): a volume
+    // stage waits for the previous volume's download of a part just before it rewrites that part
+    cudaEvent_t ev_dl[tdm::kOutEvents] = {};
     // tdm_pipeline runs each volume's stage (gather, z/y/x passes) on vol_stream, so that it
     // overlaps the next call's per-angle stages; the cap records and the specular positions the
     // volume stage reads are double buffered
     cudaStream_t vol_stream = nullptr;
+    // with chunk <= chunk_cap / 2 the per-angle stages run two chunks at once:
+    // odd chunks on lane_stream with the upper chunk slots of the scratch buffers
+    cudaStream_t lane_stream = nullptr;
+    cudaEvent_t ev_lane_fork = nullptr, ev_lane_join = nullptr;
     cudaEvent_t ev_angles = nullptr;     // per-angle stages of the current call done (stream)
     cudaEvent_t ev_vol_last = nullptr;   // last volume stage queued on vol_stream
     cudaEvent_t ev_rec_free[2] = {};     // gather that read rec_buf[i] done
@@ -196,9 +202,10 @@ int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn
                    float* xk_out);
 // gather of the cap records rec (angles [0, n), specular positions posspec),
 // normalisation and 3D inverse FFT into the outputs, on stream st.  Downloads
-// run on c->dl_stream and end with c->ev_dl_done; the staging buffers are not
-// written before the previous volume's downloads are done.  ev_gathered (may
-// be null) is recorded on st once the gather has read rec.
+// run on c->dl_stream; each staged part (x-pass slab, counts, OTF) is
+// rewritten only after the previous volume's download of that part is done
+// (c->ev_dl).  ev_gathered (may be null) is recorded on st once the gather
+// has read rec.
 int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float4* rec, const int2* posspec,
                   cudaEvent_t ev_gathered);
 }  // namespace tdm
