@@ -236,10 +236,19 @@ int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n
  * Diagnostic; no counterpart in the reference. */
 int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
 
+/* Schedule of the per-angle stages (no counterpart in the reference): tdm_pipeline
+ * streams the angles in chunks of `chunk` and keeps `lanes` consecutive chunks in
+ * flight at once, each on its own stream with its own scratch (1 <= lanes <= 8,
+ * chunk * lanes <= min(128, max_angles rounded up to a multiple of 16), the
+ * scratch capacity of the context).  Default: chunk 16, 4 lanes (fewer when the
+ * capacity or the stack is smaller).  Waits for the context's queued work first.
+ * Results do not depend on the schedule. */
+int tdm_set_schedule(tdm_ctx* ctx, int chunk, int lanes);
+
 /* Project autotuner (no counterpart in the reference): times tdm_pipeline on
- * the given stack (device holograms) with 8, 16 and 32 angles per chunk of
- * the per-angle stages (the schedule the stages are streamed in) and keeps
- * the fastest for the context; *chunk_out receives it. */
+ * the given stack (device holograms) with the schedules (chunk, lanes) = (16, 4),
+ * (16, 2), (8, 4), (12, 4), (32, 2) and (16, 6) that fit the context's scratch
+ * and keeps the fastest; *chunk_out receives its chunk. */
 int tdm_autotune(tdm_ctx* ctx, const void* holos, int bits, int n, int* chunk_out);
 
 /* Stream-ordered execution helpers.  tdm_pipeline queues each volume's stage

@@ -29,7 +29,7 @@ EXPORTS = (
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
     "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
-    "tdm_join",
+    "tdm_join", "tdm_set_schedule",
 )
 
 
@@ -107,6 +107,7 @@ def lib():
     L.tdm_batch_create.argtypes = [I, P, P, P, P, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
     L.tdm_batch_launch.argtypes = [P, P]
     L.tdm_autotune.argtypes = [P, P, I, I, ctypes.POINTER(I)]
+    L.tdm_set_schedule.argtypes = [P, I, I]
     L.tdm_join.argtypes = [P]
     L.tdm_batch_destroy.argtypes = [P]
     L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
@@ -298,8 +299,12 @@ class Context:
                                              ptr(absorption_io), ctypes.byref(r)), "tdm_tv_reconstruct")
         return {f: getattr(r, f) for f, _ in TvReport._fields_}
 
+    def set_schedule(self, chunk: int, lanes: int):
+        """tdm_set_schedule: angles per chunk and chunks in flight of the per-angle stages."""
+        self._check(lib().tdm_set_schedule(self._h, chunk, lanes), "tdm_set_schedule")
+
     def autotune(self, holos, n=None) -> int:
-        """tdm_autotune: picks the angles per chunk (8, 16 or 32) fastest on this stack; returns it."""
+        """tdm_autotune: picks the fastest schedule (chunk, lanes) on this stack; returns its chunk."""
         n = holos.shape[0] if n is None else n
         out = ctypes.c_int()
         self._check(lib().tdm_autotune(self._h, ptr(holos), self._bits(holos), n, ctypes.byref(out)), "tdm_autotune")

@@ -224,6 +224,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     tdm_ctx* c = new tdm_ctx();
     c->g = *geom;
     c->max_angles = max_angles;
+    c->chunk_cap = std::min(kChunkCapMax, (max_angles + 15) / 16 * 16);
     tdm_derive(geom, &c->dv);
     Params& p = c->p;
     p.H = geom->ccd_roix;
@@ -302,9 +303,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->vol_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_lane_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_lane_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_angles, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_vol_last, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_rec_free[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -312,7 +311,13 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         delete c;
         return TDM_ECUDA;
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kMaxLanes - 1; ++i)
+        if (cudaStreamCreateWithFlags(&c->lane_stream[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_lane_join[i], cudaEventDisableTiming) != cudaSuccess) {
+            tdm_destroy(c);
+            return TDM_ECUDA;
+        }
+    for (int i = 0; i < kStageSlots; ++i) {
         cudaEventCreateWithFlags(&c->ev_copy[i], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&c->ev_free[i], cudaEventDisableTiming);
     }
@@ -379,11 +384,16 @@ int tdm_destroy(tdm_ctx* c) {
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
     if (c->vol_stream) cudaStreamSynchronize(c->vol_stream);
-    if (c->lane_stream) cudaStreamSynchronize(c->lane_stream);
+    for (cudaStream_t l : c->lane_stream)
+        if (l) cudaStreamSynchronize(l);
     free_all(c);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kStageSlots; ++i) {
         if (c->ev_copy[i]) cudaEventDestroy(c->ev_copy[i]);
         if (c->ev_free[i]) cudaEventDestroy(c->ev_free[i]);
+    }
+    for (int i = 0; i < kMaxLanes - 1; ++i) {
+        if (c->lane_stream[i]) cudaStreamDestroy(c->lane_stream[i]);
+        if (c->ev_lane_join[i]) cudaEventDestroy(c->ev_lane_join[i]);
     }
     for (auto& e : c->ev_stage)
         if (e) cudaEventDestroy(e);
@@ -397,9 +407,7 @@ int tdm_destroy(tdm_ctx* c) {
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
     if (c->vol_stream) cudaStreamDestroy(c->vol_stream);
-    if (c->lane_stream) cudaStreamDestroy(c->lane_stream);
-    for (cudaEvent_t e : {c->ev_angles, c->ev_vol_last, c->ev_rec_free[0], c->ev_rec_free[1],
-                          c->ev_lane_fork, c->ev_lane_join})
+    for (cudaEvent_t e : {c->ev_angles, c->ev_vol_last, c->ev_rec_free[0], c->ev_rec_free[1], c->ev_lane_fork})
         if (e) cudaEventDestroy(e);
     delete c;
     return TDM_OK;
@@ -445,7 +453,7 @@ int tdm_synchronize(tdm_ctx* c) {
     TDM_CU(cudaStreamSynchronize(c->copy_stream));
     TDM_CU(cudaStreamSynchronize(c->vol_stream));
     TDM_CU(cudaStreamSynchronize(c->dl_stream));
-    TDM_CU(cudaStreamSynchronize(c->lane_stream));
+    for (cudaStream_t l : c->lane_stream) TDM_CU(cudaStreamSynchronize(l));
     TDM_CU(cudaStreamSynchronize(c->stream));
     int err = 0;
     TDM_CU(cudaMemcpy(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -515,16 +523,25 @@ double tdm_stage_ms(const tdm_ctx* c, const char* stage) {
 }
 
 // ---------------------------------------------------------------- stages
+// Hologram staging for host stacks: a ring of slots of holo_chunk holograms
+// (16-bit size) in the 2 chunk_cap holograms of b.holo_stage.
+static int stage_slots(const tdm_ctx* c) {
+    return std::max(1, std::min(kStageSlots, 2 * c->chunk_cap / c->holo_chunk));
+}
+static uint8_t* stage_slot(tdm_ctx* c, int s) {
+    return c->b.holo_stage + (size_t)s * c->holo_chunk * c->p.H * c->p.H * 2;
+}
+
 static int stage_extract(tdm_ctx* c, const void* holos, int bits, int n) {
     const Params& p = c->p;
     const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
     if (is_device_ptr(holos)) return launch_extract(c, holos, bits, n, 0);
-    // host holograms: chunked copies on the copy stream, double buffered
-    const size_t stage_bytes = (size_t)c->chunk_cap * p.H * p.H * 2;  // one staging half
+    // host holograms: chunked copies on the copy stream into a ring of staging slots
+    const int nslot = stage_slots(c);
     for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
         const int m = std::min(c->holo_chunk, n - h0);
-        const int buf = k & 1;
-        uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
+        const int buf = k % nslot;
+        uint8_t* dst = stage_slot(c, buf);
         TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));  // no-op before its first record
         TDM_CU(cudaMemcpyAsync(dst, static_cast<const char*>(holos) + h0 * per, m * per, cudaMemcpyHostToDevice,
                                c->copy_stream));
@@ -704,18 +721,19 @@ static void use_scratch(tdm_ctx* c, const ChunkScratch& k) {
 // Per-angle stages of the pipeline, streamed by hologram chunk: for each
 // chunk, extraction, field formation and cap mapping run back to back (the
 // chunk's spectra and fields stay in L2), and with host holograms the upload
-// of the next chunk overlaps them.  When the scratch buffers hold two chunks,
-// consecutive chunks run at once on two streams (the per-chunk grids fill a
-// fraction of the GPU): even chunks on c->stream with the lower slots, odd
-// ones on lane_stream with the upper slots, joined back at the end.  The
-// launchers read c->stream and the scratch pointers, which are switched per
-// chunk here and restored on every return.
+// of later chunks overlaps them.  `lanes` consecutive chunks run at once (a
+// per-chunk grid fills a fraction of the GPU): chunk k on lane k mod lanes,
+// each lane a stream with its own chunk slots of the scratch buffers, forked
+// from the context stream and joined back at the end.  The launchers read
+// c->stream and the scratch pointers, which are switched per chunk here and
+// restored on every return.
 static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
     const Params& p = c->p;
     const size_t per = (size_t)p.H * p.H * (bits == 16 ? 2 : 1);
     const bool dev = is_device_ptr(holos);
-    const size_t stage_bytes = (size_t)c->chunk_cap * p.H * p.H * 2;  // one staging half
-    const bool two = 2 * c->chunk <= c->chunk_cap && n > c->holo_chunk;
+    const int nchunks = (n + c->holo_chunk - 1) / c->holo_chunk;
+    const int nl = std::max(1, std::min(std::min(c->lanes, kMaxLanes), std::min(c->chunk_cap / c->chunk, nchunks)));
+    const int nslot = stage_slots(c);
     struct Restore {
         tdm_ctx* c;
         cudaStream_t main;
@@ -725,20 +743,21 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
             use_scratch(c, base);
         }
     } restore{c, c->stream, scratch_at(c, 0)};
-    const ChunkScratch upper = scratch_at(c, c->chunk);
-    if (two) {
+    ChunkScratch lane_scratch[kMaxLanes];
+    for (int l = 0; l < nl; ++l) lane_scratch[l] = scratch_at(c, l * c->chunk);
+    if (nl > 1) {
         TDM_CU(cudaEventRecord(c->ev_lane_fork, restore.main));
-        TDM_CU(cudaStreamWaitEvent(c->lane_stream, c->ev_lane_fork, 0));
+        for (int l = 1; l < nl; ++l) TDM_CU(cudaStreamWaitEvent(c->lane_stream[l - 1], c->ev_lane_fork, 0));
     }
     for (int h0 = 0, k = 0; h0 < n; h0 += c->holo_chunk, ++k) {
         const int m = std::min(c->holo_chunk, n - h0);
-        const bool odd = two && (k & 1);
-        c->stream = odd ? c->lane_stream : restore.main;
-        use_scratch(c, odd ? upper : restore.base);
+        const int lane = k % nl;
+        c->stream = lane ? c->lane_stream[lane - 1] : restore.main;
+        use_scratch(c, lane_scratch[lane]);
         const void* src = static_cast<const char*>(holos) + h0 * per;
-        const int buf = k & 1;
+        const int buf = k % nslot;
         if (!dev) {
-            uint8_t* dst = c->b.holo_stage + buf * stage_bytes;
+            uint8_t* dst = stage_slot(c, buf);
             TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));  // no-op before its first record
             TDM_CU(cudaMemcpyAsync(dst, src, m * per, cudaMemcpyHostToDevice, c->copy_stream));
             TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
@@ -755,9 +774,9 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
             return fail(c, rc, "fields launch failed");
         if (int rc = launch_cap(c, h0, m, form_in_cap)) return fail(c, rc, "cap mapping launch failed");
     }
-    if (two) {
-        TDM_CU(cudaEventRecord(c->ev_lane_join, c->lane_stream));
-        TDM_CU(cudaStreamWaitEvent(restore.main, c->ev_lane_join, 0));
+    for (int l = 1; l < nl; ++l) {
+        TDM_CU(cudaEventRecord(c->ev_lane_join[l - 1], c->lane_stream[l - 1]));
+        TDM_CU(cudaStreamWaitEvent(restore.main, c->ev_lane_join[l - 1], 0));
     }
     return TDM_OK;
 }
@@ -1033,18 +1052,30 @@ int tdm_batch_destroy(tdm_batch* b) {
 }
 
 // ---------------------------------------------------------------- autotuning
+int tdm_set_schedule(tdm_ctx* c, int chunk, int lanes) {
+    if (!c || chunk < 1 || lanes < 1 || lanes > kMaxLanes || chunk * lanes > c->chunk_cap)
+        return fail(c, TDM_EINVAL, "tdm_set_schedule: need 1 <= lanes <= 8 and chunk * lanes <= the chunk capacity");
+    cudaSetDevice(c->device);
+    if (int rc = tdm_synchronize(c)) return rc;  // the staging ring's slots move with the chunk size
+    c->chunk = c->holo_chunk = chunk;
+    c->lanes = lanes;
+    return TDM_OK;
+}
+
 int tdm_autotune(tdm_ctx* c, const void* holos, int bits, int n, int* chunk_out) {
     if (!c || !holos || !is_device_ptr(holos) || (bits != 8 && bits != 16) || n <= 0 || n > c->max_angles)
         return fail(c, TDM_EINVAL, "tdm_autotune: invalid argument (device holograms required)");
     cudaSetDevice(c->device);
-    const int cands[] = {8, 16, 32};
-    int best = c->chunk;
+    if (int rc = tdm_synchronize(c)) return rc;
+    const int cands[][2] = {{16, 4}, {16, 2}, {8, 4}, {12, 4}, {32, 2}, {16, 6}};
+    int best = c->chunk, best_lanes = c->lanes;
     float best_ms = 0;
     cudaEvent_t t0 = prof_event(c), t1 = prof_event(c);
     int rc = TDM_OK;
-    for (int cand : cands) {
-        if (cand > c->chunk_cap) continue;
-        c->chunk = c->holo_chunk = cand;
+    for (const auto& cand : cands) {
+        if (cand[0] * cand[1] > c->chunk_cap) continue;
+        c->chunk = c->holo_chunk = cand[0];
+        c->lanes = cand[1];
         rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);  // warm-up
         if (!rc && cudaEventRecord(t0, c->stream) != cudaSuccess) rc = TDM_ECUDA;
         for (int r = 0; r < 2 && !rc; ++r) rc = pipeline(c, holos, bits, n, nullptr, nullptr, nullptr, nullptr, nullptr, false);
@@ -1055,12 +1086,14 @@ int tdm_autotune(tdm_ctx* c, const void* holos, int bits, int n, int* chunk_out)
         if (rc) break;
         if (best_ms == 0 || ms < best_ms) {
             best_ms = ms;
-            best = cand;
+            best = cand[0];
+            best_lanes = cand[1];
         }
     }
     c->ev_pool.push_back(t0);
     c->ev_pool.push_back(t1);
     c->chunk = c->holo_chunk = best;
+    c->lanes = best_lanes;
     if (rc) return rc;
     if (chunk_out) *chunk_out = best;
     return TDM_OK;

@@ -15,6 +15,9 @@ namespace tdm {
 constexpr int kNC = 15;  // degree-4 2D polynomial: 15 monomials
 constexpr int kOutSlabs = 8;  // x-pass slabs whose outputs are downloaded while the next slab runs
 constexpr int kOutEvents = kOutSlabs + 2;
+constexpr int kMaxLanes = 8;    // chunks of the per-angle stages in flight at once
+constexpr int kStageSlots = 16; // hologram upload slots of one chunk each
+constexpr int kChunkCapMax = 128;  // angles of per-chunk scratch (all lanes together), at most
 
 // Device-side parameters of one volume, fixed at context creation.
 struct Params {
@@ -95,9 +98,10 @@ struct tdm_ctx {
     tdm::Params p{};
     tdm::Buffers b{};
     int max_angles = 0;
-    int chunk = 16;              // angles per chunk of the per-angle stages (tdm_autotune may change it)
+    int chunk = 16;              // angles per chunk of the per-angle stages (tdm_set_schedule, tdm_autotune)
     int holo_chunk = 16;         // holograms per extraction chunk (equal to chunk)
-    int chunk_cap = 32;          // chunk capacity of the per-chunk buffers
+    int lanes = 4;               // chunks in flight at once; lanes * chunk <= chunk_cap
+    int chunk_cap = 64;          // angles of per-chunk scratch: min(128, max_angles rounded up to 16)
     int nsamp = 0;
     int device = 0;
     int n_fields = 0;            // angles held in b.fields / b.posspec
@@ -113,16 +117,18 @@ struct tdm_ctx {
     // overlaps the next call's per-angle stages; the cap records and the specular positions the
     // volume stage reads are double buffered
     cudaStream_t vol_stream = nullptr;
-    // with chunk <= chunk_cap / 2 the per-angle stages run two chunks at once:
-    // odd chunks on lane_stream with the upper chunk slots of the scratch buffers
-    cudaStream_t lane_stream = nullptr;
-    cudaEvent_t ev_lane_fork = nullptr, ev_lane_join = nullptr;
+    // the per-angle stages run `lanes` chunks at once: chunk k on lane k mod lanes (lane 0 is
+    // `stream`, lane l > 0 is lane_stream[l - 1]) with chunk slots [l chunk, (l + 1) chunk) of the
+    // scratch buffers
+    cudaStream_t lane_stream[tdm::kMaxLanes - 1] = {};
+    cudaEvent_t ev_lane_fork = nullptr;
+    cudaEvent_t ev_lane_join[tdm::kMaxLanes - 1] = {};
     cudaEvent_t ev_angles = nullptr;     // per-angle stages of the current call done (stream)
     cudaEvent_t ev_vol_last = nullptr;   // last volume stage queued on vol_stream
     cudaEvent_t ev_rec_free[2] = {};     // gather that read rec_buf[i] done
     int rec_parity = 0;
-    cudaEvent_t ev_copy[2] = {nullptr, nullptr};
-    cudaEvent_t ev_free[2] = {nullptr, nullptr};
+    cudaEvent_t ev_copy[tdm::kStageSlots] = {};  // upload into hologram staging slot s done
+    cudaEvent_t ev_free[tdm::kStageSlots] = {};  // extraction that read slot s done
     cudaEvent_t ev_stage[8] = {};
     cudaEvent_t ev_out[tdm::kOutEvents] = {};  // downloads of the volume outputs (copy stream)
     uint64_t launches = 0;
