@@ -68,11 +68,11 @@ def algorithmic_bytes(name, acq, hits_per_angle, band):
     return per_angle, per_volume
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the kernel on
-# the 64-hologram rytov_1024 case (profiles/<kernel>_rytov_1024_64holos.md).
-# A launch of the row pass and of the Volkov passes processes 16 angles in
-# both cases; the gather's read traffic grows with the angles (scaled by
-# angles/64), its write traffic (the band planes) does not.
+# DRAM bytes (read + write) per launch from one ncu capture of the kernel
+# (profiles/<kernel>_rytov_1024_*.md): the row pass and the Volkov passes on
+# the 64-hologram case (a launch processes 16 angles in every case), the
+# gather on the 600-hologram case; the gather's read traffic grows with the
+# angles (scaled by angles/600), its write traffic (the band planes) does not.
 def ncu_traffic_per_launch(name, acq):
     if acq.ccd_roix != 1024 or acq.nxmax != 128 or acq.dim_final != 512:
         return None
@@ -81,7 +81,7 @@ def ncu_traffic_per_launch(name, acq):
     if name == "extract_rows":
         return 33.61408e6 + 0.312576e6
     if name == "gather":
-        return 82.249984e6 * acq.nb_holo / 64 + 416.795648e6
+        return 648.724224e6 * acq.nb_holo / 600 + 419.033088e6
     return None
 
 
@@ -490,8 +490,8 @@ def main():
     launches = ctx.launch_count - launches0
     clocks = sampler.stop(s_first, s_last)
     # per-kernel device times: the same K steps again with CUDA events around
-    # every launch, one chunk in flight (with several, launches share the GPU
-    # and their event durations overlap)
+    # every launch, one chunk in flight and each volume stage joined before the
+    # next call (launches that share the GPU would have overlapping durations)
     prof, prof_ms = {}, 0.0
     if not args.no_profile_pass:
         ctx.set_schedule(SCHEDULE[0], 1)
@@ -499,7 +499,7 @@ def main():
         ev0.record(stream)
         for _ in range(args.steps):
             ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
-        ctx.join()
+            ctx.join()
         ev1.record(stream)
         ctx.synchronize()
         prof_ms = ev0.elapsed_time(ev1)
