@@ -12,37 +12,42 @@ namespace extract {
 
 // Both passes run on the warp-resident FFT (fft_warp.cuh) in CTAs of 8
 // warps.  The row pass packs two real rows into one complex transform and
-// keeps the crop's kx band, written column-major (inter[a][c][y]) through a
-// shared-memory tile so that each column's 2P rows leave as one contiguous
-// segment; the column pass then reads whole columns contiguously and writes
-// the crop rows through a second tile (and, on request, the crop's partial
-// specular-peak winners, one record per warp).
+// keeps the crop's kx band, written column-major (inter[a][c][y]): each lane
+// stores the two rows' values of one column as one 16-byte word (the CTA's
+// other row pairs fill the rest of each column segment).  The column pass
+// then reads whole columns contiguously and writes the crop rows through a
+// shared-memory tile (and, on request, the crop's partial specular-peak
+// winners, one record per warp).
 template <int H>
 struct ExtractCfg {
     using W = WarpFFT<H>;
     static constexpr int NT = 256;         // threads per CTA
     static constexpr int P = 8 * W::G;     // row pairs per CTA (rows pass)
     static constexpr int C = 8 * W::G;     // columns per CTA (cols pass)
-    static size_t smem_rows(int F) { return ((size_t)P * W::STRIDE + (size_t)F * (2 * P + 1)) * sizeof(float2); }
+    // row-pass CTAs per SM that the registers are capped for (shared memory
+    // would allow 3 up to H = 1024, but capping to 80 registers for them
+    // spills and measured slower than 2)
+    static constexpr int ROWS_CTAS = H >= 2048 ? 1 : 2;
+    static size_t smem_rows(int) { return (size_t)P * W::STRIDE * sizeof(float2); }
     static size_t smem_cols(int F) { return ((size_t)C * W::STRIDE + (size_t)F * (C + 1)) * sizeof(float2); }
     static dim3 grid_rows(int m) { return dim3(H / (2 * P), m); }
     static dim3 grid_cols(int F, int m) { return dim3(F / C, m); }
 };
 
-// Row pass.  BULK: each warp's 2G rows (its G row pairs, consecutive in
+// Row pass.  tuk is the 1D hologram window, exactly 1 on [flat.x, flat.y]
+// (not read there).  BULK: each warp's 2G rows (its G row pairs, consecutive in
 // memory) are staged in shared memory by one bulk copy and read from there;
 // requires a 16-byte aligned stack.  Otherwise the lanes load the pixels
 // directly.  A bulk copy that does not complete within the poll bound sets
 // bit 1 of *err (the call then fails).
 template <int H, bool BULK>
-__global__ void __launch_bounds__(ExtractCfg<H>::NT)
-k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk,
+__global__ void __launch_bounds__(ExtractCfg<H>::NT, ExtractCfg<H>::ROWS_CTAS)
+k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk, int2 flat,
                const float2* __restrict__ tw, float2* __restrict__ inter, int F, int x0, int* __restrict__ err) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
-    constexpr int T = W::T, E = W::E, P = Cf::P, TP = 2 * P + 1;
+    constexpr int T = W::T, E = W::E, P = Cf::P;
     extern __shared__ __align__(16) float2 sm[];
-    float2* tile = sm + P * W::STRIDE;  // F x TP: [c][row in CTA]
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y;
     const int ya = 2 * (blockIdx.x * P + tr), yb = ya + 1;
@@ -50,7 +55,27 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
     const float wa = tuk[ya], wb = tuk[yb];
     const float sx = (j & 1) ? -1.0f : 1.0f;  // (-1)^x for x = j + T n1, T even; ya even, yb odd
     const size_t bpp = bits == 16 ? 2 : 1;
-    const char* row = static_cast<const char*>(holos) + ((size_t)a * H * H + (size_t)ya * H) * bpp;
+    float2 x[E];
+    // windowed pixels of rows ya (real part) and yb (imaginary part, negated)
+    auto load = [&](const char* row) {
+        if (bits == 16) {
+            const uint16_t* ra = reinterpret_cast<const uint16_t*>(row);
+#pragma unroll
+            for (int n1 = 0; n1 < E; ++n1) {
+                const int xx = j + n1 * T;
+                const float w = sx * ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx]));  // window is 1 on [flat]
+                x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
+            }
+        } else {
+            const uint8_t* ra = reinterpret_cast<const uint8_t*>(row);
+#pragma unroll
+            for (int n1 = 0; n1 < E; ++n1) {
+                const int xx = j + n1 * T;
+                const float w = sx * ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx]));
+                x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
+            }
+        }
+    };
     if constexpr (BULK) {
         __shared__ uint64_t bar[Cf::NT / 32];
         const int w = threadIdx.x >> 5;
@@ -58,9 +83,11 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
         // the warp's rows land at the first 16-byte boundary of its first
         // transform's array (8 (H + E + 1) bytes, so 2G H bpp + 8 fit), which
         // the transforms overwrite only after all lanes have read their pixels
-        // (the first exchange follows a __syncwarp)
-        char* stage = reinterpret_cast<char*>(
-            (reinterpret_cast<uintptr_t>(sm + (w * W::G) * W::STRIDE) + 15) & ~static_cast<uintptr_t>(15));
+        // (the first exchange follows a __syncwarp); the pointer is formed by
+        // arithmetic on sm (no integer round trip), so the reads stay
+        // shared-memory loads
+        float2* const first = sm + (w * W::G) * W::STRIDE;
+        char* stage = reinterpret_cast<char*>(first) + ((16u - (smem_addr(first) & 15u)) & 15u);
         if ((threadIdx.x & 31) == 0) {
             const uint32_t bytes = (uint32_t)(2 * W::G * H * bpp);
             const size_t y0w = 2 * ((size_t)blockIdx.x * P + w * W::G);
@@ -73,25 +100,9 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
             if ((threadIdx.x & 31) == 0) atomicOr(err, 2);
             mbar_wait(&bar[w], 0);
         }
-        row = stage + (size_t)(tr - w * W::G) * 2 * H * bpp;
-    }
-    float2 x[E];
-    if (bits == 16) {
-        const uint16_t* ra = reinterpret_cast<const uint16_t*>(row);
-#pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) {
-            const int xx = j + n1 * T;
-            const float w = sx * __ldg(&tuk[xx]);
-            x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
-        }
+        load(stage + (size_t)(tr - w * W::G) * 2 * H * bpp);
     } else {
-        const uint8_t* ra = reinterpret_cast<const uint8_t*>(row);
-#pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) {
-            const int xx = j + n1 * T;
-            const float w = sx * __ldg(&tuk[xx]);
-            x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
-        }
+        load(static_cast<const char*>(holos) + ((size_t)a * H * H + (size_t)ya * H) * bpp);
     }
     fft_warp_regs<H, -1>(x, s, j, tw);
     __syncwarp();
@@ -101,18 +112,14 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
         for (int k2 = 0; k2 < T; ++k2) s[warp_out_pos<H>(j, q, k2)] = x[q * T + k2];
     }
     __syncwarp();
-    // separate the two real rows on the kx band: Xa = (Z(k) + conj Z(-k))/2, Xb = (Z(k) - conj Z(-k))/(2i)
+    // separate the two real rows on the kx band: Xa = (Z(k) + conj Z(-k))/2, Xb = (Z(k) - conj Z(-k))/(2i);
+    // rows ya (even) and yb = ya + 1 of column c are adjacent in inter: one 16-byte store
+    float4* dst = reinterpret_cast<float4*>(inter + (size_t)a * F * H + ya);
     for (int c = j; c < F; c += T) {
         const int k = x0 + c, km = (H - k) & (H - 1);
         const float2 z = s[W::pad(k)], zm = s[W::pad(km)];
-        tile[c * TP + 2 * tr] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-        tile[c * TP + 2 * tr + 1] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
-    }
-    __syncthreads();
-    float2* dst = inter + (size_t)a * F * H + 2 * blockIdx.x * P;
-    for (int i = threadIdx.x; i < F * 2 * P; i += Cf::NT) {
-        const int c = i / (2 * P), r = i % (2 * P);
-        dst[(size_t)c * H + r] = tile[c * TP + r];
+        dst[(size_t)c * (H / 2)] = make_float4(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y), 0.5f * (z.y + zm.y),
+                                               -0.5f * (z.x - zm.x));
     }
 }
 

@@ -172,17 +172,30 @@ struct WarpFFT {
     __host__ __device__ static constexpr int pad(int i) { return i + (i >> LOG_T); }
 };
 
-// x[k1] *= W_N^(DIR j k1), k1 = 1 .. E-1, from the [k1][j] table (L1-cached
-// loads, all independent).
+// x[k1] *= W_N^(DIR j k1), k1 = 1 .. E-1, from the [k1][j] table.  For
+// E >= 16 only the factors of k1 = b (b < 8) and k1 = 8a are loaded and
+// W^(j (8a + b)) = W^(8ja) W^(jb) is formed in registers: 7 + E/8 - 1 loads
+// instead of E - 1 (the loads' L1 latency, not their arithmetic, bounded the
+// FFT passes), at about one extra rounding per factor.
 template <int N, int DIR>
 __device__ __forceinline__ void twiddle_lane(float2 (&x)[WarpFFT<N>::E], const float2* __restrict__ twr, int j) {
     using W = WarpFFT<N>;
     constexpr int E = W::E, T = W::T;
+    constexpr int R = E >= 16 ? 8 : E;  // k1 = R a + b
+    float2 wb[R];
 #pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) {
-        float2 w = __ldg(&twr[k1 * T + j]);
-        if constexpr (DIR > 0) w.y = -w.y;
-        x[k1] = c_mul(x[k1], w);
+    for (int b = 1; b < R; ++b) {
+        wb[b] = __ldg(&twr[b * T + j]);
+        if constexpr (DIR > 0) wb[b].y = -wb[b].y;
+        x[b] = c_mul(x[b], wb[b]);
+    }
+#pragma unroll
+    for (int a = 1; a < E / R; ++a) {
+        float2 wa = __ldg(&twr[R * a * T + j]);
+        if constexpr (DIR > 0) wa.y = -wa.y;
+        x[R * a] = c_mul(x[R * a], wa);
+#pragma unroll
+        for (int b = 1; b < R; ++b) x[R * a + b] = c_mul(x[R * a + b], c_mul(wa, wb[b]));
     }
 }
 

@@ -50,4 +50,12 @@ inline std::vector<double> tukey_factor(int n, float alpha) {
     return t;
 }
 
+// Indices [x, y] where tukey_factor(n, alpha) is exactly 1 (its flat middle,
+// same bounds as above): kernels skip the table there.
+inline int2 tukey_flat(int n, float alpha) {
+    const int b1 = (int)std::round(alpha * (n - 1) / 2);
+    const int b2 = (int)std::round((n - 1) * (1 - alpha / 2));
+    return make_int2(b1 + 1, b2 < n - 1 ? b2 : n - 1);
+}
+
 }  // namespace tdm

@@ -87,7 +87,7 @@ __device__ __forceinline__ int cap_col(const Params& p, int k, int q) {
 
 template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
-k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, const float2* __restrict__ tw,
+k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, int2 flat, const float2* __restrict__ tw,
            float2* __restrict__ r1) {
     using C = CapCfg<F>;
     using W = typename C::W;
@@ -101,7 +101,7 @@ k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, con
 #pragma unroll
     for (int n1 = 0; n1 < E; ++n1) {
         const int xx = j + n1 * T;
-        x[n1] = c_scale(src[xx], __ldg(&tuk[xx]) * wy);
+        x[n1] = c_scale(src[xx], ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx])) * wy);
     }
     fft_warp_regs<F, -1>(x, sm + tr * W::STRIDE, j, tw);
     float2* dst = r1 + ((size_t)a * F + y) * F;
@@ -118,7 +118,8 @@ k_cap_rows(const float2* __restrict__ fields, const float* __restrict__ tuk, con
 template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_rows_form(const float* __restrict__ unwrapped, const float* __restrict__ amp, const double* __restrict__ beta,
-                int born, const float* __restrict__ tuk, const float2* __restrict__ tw, float2* __restrict__ fields,
+                int born, const float* __restrict__ tuk, int2 flat, const float2* __restrict__ tw,
+                float2* __restrict__ fields,
                 float2* __restrict__ r1) {
     using C = CapCfg<F>;
     using W = typename C::W;
@@ -138,7 +139,7 @@ k_cap_rows_form(const float* __restrict__ unwrapped, const float* __restrict__ a
         const int xx = j + n1 * T;
         const float2 f = form_value(fr, xx, F, unwrapped[row + xx], amp[row + xx], born);
         fields[row + xx] = f;
-        x[n1] = c_scale(f, __ldg(&tuk[xx]) * wy);
+        x[n1] = c_scale(f, ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx])) * wy);
     }
     fft_warp_regs<F, -1>(x, sm + tr * W::STRIDE, j, tw);
     float2* dst = r1 + row;
@@ -641,10 +642,12 @@ int cap_impl(tdm_ctx* c, int a0, int n, bool form) {
         if (form) {
             Launch l(c, K_CAP_ROWS);
             k_cap_rows_form<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(
-                c->p.deroul ? b.unwrapped : b.phase, b.amp, b.beta, c->p.born, b.tuk_f, b.tw, b.fields + g0 * FF, b.r1);
+                c->p.deroul ? b.unwrapped : b.phase, b.amp, b.beta, c->p.born, b.tuk_f, c->tuk_f_flat, b.tw,
+                b.fields + g0 * FF, b.r1);
         } else {
             Launch l(c, K_CAP_ROWS);
-            k_cap_rows<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(b.fields + g0 * FF, b.tuk_f, b.tw, b.r1);
+            k_cap_rows<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(b.fields + g0 * FF, b.tuk_f,
+                                                                             c->tuk_f_flat, b.tw, b.r1);
         }
         {
             Launch l(c, K_CAP_COLS);

@@ -361,6 +361,8 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     // tables
     const std::vector<float2> tw = twiddle_table();
     std::vector<double> th = tukey_factor(p.H, 0.05f), tf = tukey_factor(F, 0.1f);
+    c->tuk_h_flat = tukey_flat(p.H, 0.05f);
+    c->tuk_f_flat = tukey_flat(F, 0.1f);
     std::vector<float> thf(th.begin(), th.end()), tff(tf.begin(), tf.end());
     std::vector<float> stabf(stab.begin(), stab.end());
     if (cudaMemcpy(b.tw, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||

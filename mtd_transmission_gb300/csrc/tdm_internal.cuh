@@ -104,6 +104,7 @@ struct tdm_ctx {
     int chunk_cap = 64;          // angles of per-chunk scratch: min(128, max_angles rounded up to 16)
     int nsamp = 0;
     int device = 0;
+    int2 tuk_h_flat{0, -1}, tuk_f_flat{0, -1};  // where the hologram / field windows are exactly 1
     int n_fields = 0;            // angles held in b.fields / b.posspec
     int n_spectra = 0;           // angles held in b.spectra
     int n_caps = 0;              // angles held in b.rec (cap records)
