@@ -168,10 +168,8 @@ struct VCfg {
     static constexpr int NT = B * W::T;
     static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
     static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;  // pass-2 transform stride, 2 mod 16
-    static constexpr int LSZ = L + 2;                                  // pass-2 phasor stride, 2 mod 16
-    static constexpr int LSG = L + 4;                                  // pass-2 gradient stride, 4 mod 32
-    static constexpr size_t SMEM_COLS =
-        ((size_t)B * VS + (size_t)2 * P * LSZ) * sizeof(float2) + (size_t)2 * P * LSG * sizeof(float);
+    static constexpr size_t SMEM_COLS = (size_t)B * VS * sizeof(float2);
+    static constexpr int COLS_CTAS = 3;  // pass-2 CTAs per SM the registers are bounded for
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
@@ -226,53 +224,50 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
 // Pass 2: columns X = F + x of the mirror (columns X and L-1-X are the same
 // image column): gy like gx, then Q = gx + i gy and its FFT along y.  The
 // columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
-// pass 3.
+// pass 3.  The loads and the gy epilogue run CTA-wide with the NC = 8
+// columns fastest (contiguous in global memory); the phasor and gx are read
+// again from global memory (L2) in the epilogue rather than kept in shared
+// memory, which leaves room for a third CTA per SM.
 template <int L>
-__global__ void __launch_bounds__(VCfg<L>::NT)
+__global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
 k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
               const float2* __restrict__ tw, float2* __restrict__ qc) {
     using C = VCfg<L>;
     using W = typename C::W;
-    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P, NC = 2 * P, NT = C::NT;
-    // Strides chosen for the staging pattern (a warp writes NC = 8 columns x 4
-    // rows): transform arrays and phasors 2 mod 16 float2 apart, gradients
-    // 4 mod 32 floats apart, so the 32 lanes of each store hit distinct banks.
-    constexpr int VS = C::VS, LS = C::LSZ, LG = C::LSG;
+    constexpr int F = L / 2, T = W::T, NC = 2 * C::P, NT = C::NT;
+    // Transform arrays VS = 2 mod 16 float2 apart: a warp's 8 columns x 4 rows
+    // land in distinct banks.
+    constexpr int VS = C::VS;
     extern __shared__ float2 sm[];
-    float2* szp = sm + C::B * VS;                               // NC x LS exp(i phase) along the mirror column
-    float* sgx = reinterpret_cast<float*>(szp + NC * LS);       // NC x LG gx along the mirror column
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
-    const bool zk = tr < NC;
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
+    auto src = [&](int Y, int c) { return ((size_t)a * F + mirror(Y, F)) * F + x0 + c; };
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, Y = i / NC;
-        const size_t src = ((size_t)a * F + mirror(Y, F)) * F + x0 + c;
-        const float2 z = zph[src];
-        szp[c * LS + Y] = z;
-        sgx[c * LG + Y] = gxh[src];
-        sm[c * VS + W::pad(Y)] = z;
-        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * VS + W::pad(Y)])[c & 1] = phase[src];
+        const size_t o = src(Y, c);
+        sm[c * VS + W::pad(Y)] = zph[o];
+        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * VS + W::pad(Y)])[c & 1] = phase[o];
     }
     __syncthreads();
     float2* s = sm + tr * VS;
     fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
     __syncthreads();
-    if (zk) {  // warp-uniform
-        const int c = tr;
-        const float2* sp = sm + (NC + (c >> 1)) * VS;
-#pragma unroll 8
-        for (int n1 = 0; n1 < E; ++n1) {
-            const int Y = j + n1 * T;
-            const float2 z = szp[c * LS + Y];
-            const float2 g = s[j + n1 * (T + 1)];
-            const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
-            const float2 q = sp[j + n1 * (T + 1)];
-            s[j + n1 * (T + 1)] = make_float2(sgx[c * LG + Y], (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
-        }
-        __syncwarp();
-        fft_warp_call<L, -1>(s, j, tw);
+    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi; Q = gx + i gy into the Z arrays
+#pragma unroll 4
+    for (int i = threadIdx.x; i < NC * L; i += NT) {
+        const int c = i % NC, Y = i / NC;
+        const size_t o = src(Y, c);
+        const float2 z = zph[o];
+        const float gx = gxh[o];
+        float2* gp = &sm[c * VS + W::pad(Y)];
+        const float2 g = *gp;
+        const float2 q = sm[(NC + (c >> 1)) * VS + W::pad(Y)];
+        const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
+        *gp = make_float2(gx, (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
     }
+    __syncthreads();
+    if (tr < NC) fft_warp_call<L, -1>(s, j, tw);  // warp-uniform
     __syncthreads();
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
