@@ -58,7 +58,8 @@ __device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, in
     const int fdx = ((kx + ps.x) & (F - 1)) - N, fdy = ((ky + ps.y) & (F - 1)) - N;
     if (!(fz >= 0.0) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;
     const int ti = (fdy + N) * F + fdx + N;
-    *sf = s_tabf[ti];
+    // sqrt(r^2 - fd^2) in float: computed from the exact integer when r^2 < 2^24 (equal to the table)
+    *sf = p.r2i ? __fsqrt_rn((float)(p.r2i - fdx * fdx - fdy * fdy)) : s_tabf[ti];
     const float d = *sf - (float)fz;
     const float fr = d - floorf(d);
     // round(sqrt(fdz^2) - fzm0) in FP64 (fonctions.cpp:921); the FP32 value

@@ -245,6 +245,10 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     p.disc_thr = (int)std::min<double>(std::ceil(lim), 2.0 * N * N + 1);
     // cap heights sqrt(rayon^2 - fd^2) exactly as fonctions.cpp:920, and the z band
     const double r2 = p.rayon * p.rayon;
+    // rayon is an integer: below 2^24, rayon^2 - fd^2 is an exact float and
+    // its correctly rounded float sqrt equals (float)sqrt in double (checked
+    // for every integer below 2^24), so the kernels compute the float table
+    p.r2i = r2 < 16777216.0 ? (int)r2 : 0;
     std::vector<double> stab((size_t)F * F, std::numeric_limits<double>::quiet_NaN());
     double smin = std::numeric_limits<double>::infinity();
     for (int fdy = -N; fdy < N; ++fdy)

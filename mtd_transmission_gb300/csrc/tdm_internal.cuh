@@ -26,6 +26,7 @@ struct Params {
     int born, c_aber, deroul;
     int disc_thr;            // fd^2 < disc_thr  <=>  fd^2 < COEF_NA_OBJ_LIMIT * N^2
     int zmin, band;          // cap planes z in [zmin, zmin + band)
+    int r2i;                 // rayon^2 when below 2^24 (cap heights as float sqrt of exact integers), else 0
     double rayon, inv_rayon;
     float cap_scale;         // (k0/pi)*(-2pi) of retroPropag_Born, k0 in float
     float dx2;               // tailleTheoPixelUborn^2
