@@ -196,8 +196,8 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 // column is covered by a fraction of the angles: the CTA first lists, in
 // ascending order, the angles whose window covers row Y and any of its 32
 // columns.  The lanes then take 32 consecutive listed angles at a time, the
-// next group's records loaded while the current one is added; groups without
-// a hit are skipped.  An angle hits a column at most once, at one plane, and
+// records of the next two groups loaded while the current one is added;
+// groups without a hit are skipped.  An angle hits a column at most once, at one plane, and
 // the column's running sums live in FP64 in shared memory.  When the group's
 // planes are distinct (seen through a plane -> lane ownership table) every
 // lane adds its own hit; otherwise lanes sharing a plane are grouped and the
@@ -280,11 +280,12 @@ k_accumulate(const float4* __restrict__ rec, const int2* __restrict__ posspec, i
             }
             return r;
         };
-        float4 nxt = fetch(lane);
+        float4 nxt = fetch(lane), nxt2 = fetch(32 + lane);
         __syncwarp();
         for (int g0 = 0; g0 < listed; g0 += 32) {
             const float4 r = nxt;
-            nxt = fetch(g0 + 32 + lane);
+            nxt = nxt2;
+            nxt2 = fetch(g0 + 64 + lane);
             const int z = __float_as_int(r.z);
             const int e = z >= 0 ? z - zmin : -1;
             if (!__any_sync(0xffffffffu, e >= 0)) continue;
