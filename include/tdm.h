@@ -93,6 +93,14 @@ int tdm_derive(const tdm_geom* geom, tdm_derived* out);
  * (pretraitement_hors_axe_CPU/Correction_aberration.cpp:36-149; main.cpp:192-208). */
 int tdm_set_mask(tdm_ctx* ctx, const uint8_t* mask);
 
+/* Reference intensity, H*H float (the Intensite_ref.pgm image of the ROI, host
+ * or device memory), or NULL to clear it.  While set, every hologram pixel is
+ * divided by the reference amplitude sqrt(I_ref) (1 where I_ref is 0) before
+ * the extraction.  Replaces initRef (pretraitement_hors_axe_CPU/fonctions.cpp:46-61)
+ * and the division of main.cpp:147.  Off by default, as in the reference,
+ * where those lines are commented out (main.cpp:109,147). */
+int tdm_set_reference_intensity(tdm_ctx* ctx, const float* intensity);
+
 /* Off-axis extraction of n holograms (H*H samples each, uint8 when bits == 8,
  * uint16 when bits == 16) into the context's spectrum stack; the F*F crops
  * are also copied to spectra_out (n*F*F complex) when it is not NULL.

@@ -29,7 +29,7 @@ EXPORTS = (
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
     "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
-    "tdm_join", "tdm_set_schedule",
+    "tdm_join", "tdm_set_schedule", "tdm_set_reference_intensity",
 )
 
 
@@ -108,6 +108,7 @@ def lib():
     L.tdm_batch_launch.argtypes = [P, P]
     L.tdm_autotune.argtypes = [P, P, I, I, ctypes.POINTER(I)]
     L.tdm_set_schedule.argtypes = [P, I, I]
+    L.tdm_set_reference_intensity.argtypes = [P, P]
     L.tdm_join.argtypes = [P]
     L.tdm_batch_destroy.argtypes = [P]
     L.tdm_adjoint.argtypes = [P, P, I, P, P, P]
@@ -230,6 +231,13 @@ class Context:
 
     def set_mask(self, mask=None):
         self._check(lib().tdm_set_mask(self._h, ptr(mask)), "tdm_set_mask")
+
+    def set_reference_intensity(self, intensity=None):
+        """tdm_set_reference_intensity: H x H float32 Intensite_ref image (holograms are
+        divided by its square root before extraction), or None to clear it."""
+        if intensity is not None and isinstance(intensity, np.ndarray):
+            intensity = np.ascontiguousarray(intensity, np.float32)
+        self._check(lib().tdm_set_reference_intensity(self._h, ptr(intensity)), "tdm_set_reference_intensity")
 
     @staticmethod
     def _bits(holos) -> int:

@@ -35,7 +35,8 @@ struct ExtractCfg {
 };
 
 // Row pass.  tuk is the 1D hologram window, exactly 1 on [flat.x, flat.y]
-// (not read there).  BULK: each warp's 2G rows (its G row pairs, consecutive in
+// (not read there); ref_inv (may be null) is the H x H reciprocal of the
+// reference amplitude, applied to every pixel first (main.cpp:147).  BULK: each warp's 2G rows (its G row pairs, consecutive in
 // memory) are staged in shared memory by one bulk copy and read from there;
 // requires a 16-byte aligned stack.  Otherwise the lanes load the pixels
 // directly.  A bulk copy that does not complete within the poll bound sets
@@ -43,7 +44,8 @@ struct ExtractCfg {
 template <int H, bool BULK>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT, ExtractCfg<H>::ROWS_CTAS)
 k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk, int2 flat,
-               const float2* __restrict__ tw, float2* __restrict__ inter, int F, int x0, int* __restrict__ err) {
+               const float* __restrict__ ref_inv, const float2* __restrict__ tw, float2* __restrict__ inter, int F,
+               int x0, int* __restrict__ err) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, P = Cf::P;
@@ -73,6 +75,14 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
                 const int xx = j + n1 * T;
                 const float w = sx * ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx]));
                 x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
+            }
+        }
+        if (ref_inv) {  // pixel / reference amplitude, before the window (it scales each product)
+            const float* qa = ref_inv + (size_t)ya * H;
+#pragma unroll
+            for (int n1 = 0; n1 < E; ++n1) {
+                const int xx = j + n1 * T;
+                x[n1] = make_float2(x[n1].x * __ldg(&qa[xx]), x[n1].y * __ldg(&qa[H + xx]));
             }
         }
     };

@@ -39,7 +39,8 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
         const char* src = static_cast<const char*>(holos) + (size_t)h0 * bytes_per;
         {
             Launch l(c, K_EXTRACT_ROWS);
-            rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->tuk_h_flat, c->b.tw,
+            rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->tuk_h_flat,
+                                                                c->use_ref ? c->b.ref_inv : nullptr, c->b.tw,
                                                                 c->b.inter, p.F,
                                                                 p.x0, c->b.err);
         }

@@ -82,7 +82,7 @@ void free_all(tdm_ctx* c) {
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0], b.rec_buf[1], b.posspec_vol[0],
                     b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
-                    b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit};
+                    b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit, b.ref_inv};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = Buffers{};
@@ -452,6 +452,36 @@ int tdm_set_mask(tdm_ctx* c, const uint8_t* mask) {
     }
     TDM_CU(cudaStreamSynchronize(c->stream));
     return build_aberration(c, mask);
+}
+
+// initRef (fonctions.cpp:46-61): the reference amplitude is sqrt(I_ref), 1
+// where I_ref is 0; kept as its float reciprocal (double arithmetic, one
+// rounding), multiplied into each pixel by the extraction row pass.
+int tdm_set_reference_intensity(tdm_ctx* c, const float* intensity) {
+    if (!c) return TDM_EINVAL;
+    cudaSetDevice(c->device);
+    if (int rc = tdm_synchronize(c)) return rc;  // no queued extraction may still read the table
+    if (!intensity) {
+        c->use_ref = false;
+        return TDM_OK;
+    }
+    const size_t HH = (size_t)c->p.H * c->p.H;
+    std::vector<float> in(HH);
+    if (is_device_ptr(intensity)) {
+        TDM_CU(cudaMemcpy(in.data(), intensity, HH * sizeof(float), cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(in.data(), intensity, HH * sizeof(float));
+    }
+    std::vector<float> inv(HH);
+    for (size_t i = 0; i < HH; ++i) {
+        const double v = in[i];
+        if (!(v >= 0)) return fail(c, TDM_EINVAL, "tdm_set_reference_intensity: negative or NaN intensity");
+        inv[i] = (float)(v != 0 ? 1.0 / std::sqrt(v) : 1.0);
+    }
+    if (!c->b.ref_inv && dev_alloc(c, &c->b.ref_inv, HH)) return fail(c, TDM_ENOMEM, "reference table allocation");
+    TDM_CU(cudaMemcpy(c->b.ref_inv, inv.data(), HH * sizeof(float), cudaMemcpyHostToDevice));
+    c->use_ref = true;
+    return TDM_OK;
 }
 
 int tdm_synchronize(tdm_ctx* c) {

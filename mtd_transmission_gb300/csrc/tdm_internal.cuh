@@ -37,6 +37,7 @@ struct Params {
 struct Buffers {
     float2* tw = nullptr;          // kTwTotal twiddles (twiddle_table)
     float* tuk_h = nullptr;        // H, hologram Tukey alpha 0.05 (1D factor)
+    float* ref_inv = nullptr;      // H*H, 1 / reference amplitude (tdm_set_reference_intensity), on first use
     float* tuk_f = nullptr;        // F, field Tukey alpha 0.1 (1D factor)
     double* s_tab = nullptr;       // F*F, sqrt(rayon^2 - fd^2) at [fdy+N][fdx+N]
     float* s_tabf = nullptr;       // float copy
@@ -106,6 +107,7 @@ struct tdm_ctx {
     int nsamp = 0;
     int device = 0;
     int2 tuk_h_flat{0, -1}, tuk_f_flat{0, -1};  // where the hologram / field windows are exactly 1
+    bool use_ref = false;        // holograms divided by the reference amplitude (b.ref_inv)
     int n_fields = 0;            // angles held in b.fields / b.posspec
     int n_spectra = 0;           // angles held in b.spectra
     int n_caps = 0;              // angles held in b.rec (cap records)

@@ -99,7 +99,7 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
         const int m = n - h0 < chunk ? n - h0 : chunk;
         k_extract_rows<H, false><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
             static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), tukey_flat(H, 0.05f),
-            s.twiddle, s.scratch, F,
+            nullptr, s.twiddle, s.scratch, F,
             x0, nullptr);
         k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
             s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0, nullptr);

@@ -142,7 +142,20 @@ def extract(holo: np.ndarray, cfg: Config) -> np.ndarray:
     return out
 
 
-def extract_stack(holos: np.ndarray, cfg: Config) -> np.ndarray:
+def reference_amplitude(intensity: np.ndarray) -> np.ndarray:
+    """initRef (pretraitement_hors_axe_CPU/fonctions.cpp:46-61): sqrt of the
+    reference intensity, 1 where the intensity is 0."""
+    i = np.asarray(intensity, np.float64)
+    return np.where(i != 0, np.sqrt(np.where(i != 0, i, 1.0)), 1.0)
+
+
+def extract_stack(holos: np.ndarray, cfg: Config, ref_intensity: np.ndarray | None = None) -> np.ndarray:
+    """holo2TF_UBorn per hologram; with ref_intensity each hologram is first
+    divided by the reference amplitude (main.cpp:147, commented out in the
+    reference's own run)."""
+    if ref_intensity is not None:
+        amp = reference_amplitude(ref_intensity)
+        return np.stack([extract(np.asarray(h, np.float64) / amp, cfg) for h in holos])
     return np.stack([extract(h, cfg) for h in holos])
 
 

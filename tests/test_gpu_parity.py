@@ -315,3 +315,32 @@ def test_schedules_keep_results():
         for chunk, lanes in ((64, 3), (8, 9), (0, 1), (129, 1)):
             with pytest.raises(TdmError):
                 ctx.set_schedule(chunk, lanes)
+
+
+def test_reference_intensity():
+    """tdm_set_reference_intensity divides every pixel by sqrt(I_ref) (1 where
+    I_ref is 0) before the extraction, as initRef and main.cpp:147 of the
+    reference; clearing it gives the plain extraction back bit for bit, and a
+    negative intensity is refused."""
+    acq, ph, d = small_case("plain_512_born", M=3)
+    H, F = acq.ccd_roix, 2 * acq.nxmax
+    rng = np.random.default_rng(5)
+    iref = rng.uniform(500.0, 3000.0, (H, H)).astype(np.float32)
+    iref[rng.random((H, H)) < 0.01] = 0.0
+    cfg = oracle_cfg(acq)
+    ref = oracle.extract_stack(d["holos"].astype(np.float64), cfg, ref_intensity=iref)
+    holos = np.ascontiguousarray(d["holos"])
+    with Context(Geometry.from_acquisition(acq), 3) as ctx:
+        plain = np.zeros((3, F, F), np.complex64)
+        ctx.extract(holos, spectra_out=plain)
+        ctx.set_reference_intensity(iref)
+        out = np.zeros_like(plain)
+        ctx.extract(holos, spectra_out=out)
+        for a in range(3):
+            assert rel_l2(out[a], ref[a]) <= TOL, a
+        ctx.set_reference_intensity(None)
+        again = np.zeros_like(plain)
+        ctx.extract(holos, spectra_out=again)
+        assert np.array_equal(again, plain)
+        with pytest.raises(TdmError):
+            ctx.set_reference_intensity(-iref)

@@ -166,3 +166,15 @@ def test_oracle_forward_adjoint_pair():
         np.add.at(counts, cell[1:], 1.0)
     ref = oracle.reconstruction(np.zeros((M, F, F), np.complex128), pos, cfg, want_otf=False, want_indice=False)
     np.testing.assert_array_equal(counts, ref["counts"])
+
+
+def test_reference_amplitude_rule():
+    """initRef (fonctions.cpp:46-61): sqrt of the intensity, 1 where it is 0;
+    a unit reference leaves the extraction unchanged."""
+    i = np.array([[0.0, 4.0], [9.0, 2.0]])
+    np.testing.assert_array_equal(oracle.reference_amplitude(i), [[1.0, 2.0], [3.0, np.sqrt(2.0)]])
+    acq, ph, d = small_case("plain_512_born", M=1)
+    cfg = oracle_cfg(acq)
+    h = d["holos"].astype(np.float64)
+    ones = np.ones((acq.ccd_roix, acq.ccd_roix))
+    np.testing.assert_array_equal(oracle.extract_stack(h, cfg, ref_intensity=ones), oracle.extract_stack(h, cfg))
