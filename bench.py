@@ -184,6 +184,41 @@ def cpu_baseline(acq, ph, seed, sample_angles: int, threads: int):
             "sample_wall_s": time.perf_counter() - t0}
 
 
+def fft_check(acq, threads: int):
+    """The oracle's FFT against scipy.fft (workers = threads) on the transform
+    sizes of one volume: the hologram (H^2), the field (F^2), the Volkov mirror
+    ((2F)^2) and the volume (D^3), complex128, ms per transform.  Returns the
+    timings and the CPU seconds per volume that scipy's FFT would save where it
+    is faster: per hologram one H^2, per angle two F^2 and nine (2F)^2
+    transforms, and one D^3 transform."""
+    import numpy as np
+    import scipy.fft
+
+    import oracle
+    oracle.set_threads(threads)
+    rng = np.random.default_rng(0)
+    H, F, D, M = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final, acq.nb_holo
+    out = {}
+    for name, shape, reps in (("hologram", (H, H), 3), ("field", (F, F), 10), ("mirror", (2 * F, 2 * F), 5),
+                              ("volume", (D, D, D), 1)):
+        a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        ofn = oracle.fft3d if len(shape) == 3 else oracle.fft2d
+        ofn(a)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            ofn(a)
+        t_o = (time.perf_counter() - t0) / reps
+        scipy.fft.fftn(a, workers=threads)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            scipy.fft.fftn(a, workers=threads)
+        t_s = (time.perf_counter() - t0) / reps
+        out[name] = {"shape": list(shape), "oracle_ms": round(1e3 * t_o, 3), "scipy_ms": round(1e3 * t_s, 3)}
+    gain = lambda k: max(0.0, out[k]["oracle_ms"] - out[k]["scipy_ms"]) / 1e3  # noqa: E731
+    saved = M * (gain("hologram") + 2 * gain("field") + 9 * gain("mirror")) + gain("volume")
+    return out, saved
+
+
 def run_reference(args, acq, ph, seed):
     threads = os.cpu_count() or 1
     import oracle
@@ -592,6 +627,16 @@ def main():
                    "sample": f"{args.cpu_sample} of {acq.nb_holo} holograms through extraction, fields and cap "
                              f"mapping ({r['per_angle_s']:.3f} s/angle), extrapolated, plus one full "
                              f"{acq.dim_final}^3 volume stage ({r['volume_s']:.1f} s)"}
+            # the reference's default thread count (recon.txt NB_THREADS 4)
+            r4 = cpu_baseline(acq, ph, seed, max(2, args.cpu_sample // 3), 4)
+            cpu["nb_threads_4"] = {"value": 1.0 / r4["seconds_per_volume"], "cores": 4,
+                                   "sample": f"{max(2, args.cpu_sample // 3)} holograms, extrapolated, plus one "
+                                             f"volume stage ({r4['volume_s']:.1f} s)"}
+            # the oracle's FFT against scipy.fft on the same sizes: the baseline
+            # with the faster of the two (a conservative speed-up)
+            fft, saved = fft_check(acq, threads)
+            cpu["fft_check"] = fft
+            cpu["value_with_faster_fft"] = 1.0 / max(r["seconds_per_volume"] - saved, 1e-9)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT,
             "holograms_per_s": round(value * acq.nb_holo, 1), "n_gpus": world, "steps": args.steps,
