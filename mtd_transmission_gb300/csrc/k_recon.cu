@@ -165,7 +165,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
     const int a = blockIdx.y, kx0 = blockIdx.x * B;
     const int2 ps = posspec[a];
     if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
-#pragma unroll 8
+#pragma unroll  // every load in flight before the first store
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
         sm[t * W::STRIDE + W::pad(ky)] = r1[((size_t)a * F + ky) * F + kx0 + t];
@@ -400,7 +400,7 @@ k_ypass(float2* __restrict__ vol, const float2* __restrict__ tw) {
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int z0 = blockIdx.x * B, X = blockIdx.y;
-#pragma unroll 8
+#pragma unroll  // every load in flight before the first store (latency-bound at 8)
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, Y = i / B;
         sm[t * W::STRIDE + W::pad(Y)] = vol[((size_t)Y * D + X) * D + z0 + t];
@@ -427,7 +427,7 @@ k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float sca
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int z0 = (zblock0 + blockIdx.x) * B, Y = blockIdx.y;
-#pragma unroll 8
+#pragma unroll  // every load in flight before the first store (latency-bound at 8)
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, X = i / B;
         sm[t * W::STRIDE + W::pad(X)] = vol[((size_t)Y * D + X) * D + z0 + t];
@@ -470,7 +470,7 @@ k_fxpass(const float* __restrict__ re, const float* __restrict__ im, const float
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int z0 = blockIdx.x * B, Y = blockIdx.y;
     const int par = (3 * (D / 2)) & 1;
-#pragma unroll 8
+#pragma unroll  // every load in flight before the first store
     for (int r = 0; r < B * D / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i / D, X = i % D, Z = z0 + t;
         const size_t o = ((size_t)Z * D + Y) * D + X;
