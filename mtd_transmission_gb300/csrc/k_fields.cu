@@ -120,7 +120,7 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, x0 = blockIdx.x * B;
-#pragma unroll 8
+#pragma unroll  // every staging load in flight before the first store
     for (int r0 = 0; r0 < B * F / NT; ++r0) {
         const int i = threadIdx.x + r0 * NT, t = i % B, r = i / B;
         sm[t * W::STRIDE + W::pad(r)] = I1[((size_t)a * F + r) * F + x0 + t];
@@ -169,7 +169,9 @@ struct VCfg {
     static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
     static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;  // pass-2 transform stride, 2 mod 16
     static constexpr size_t SMEM_COLS = (size_t)B * VS * sizeof(float2);
-    static constexpr int COLS_CTAS = 3;  // pass-2 CTAs per SM the registers are bounded for
+    // pass-2 CTAs per SM the registers are bounded for (up to L = 512; the
+    // 1024-point mirror runs 384 threads a CTA and needs its registers)
+    static constexpr int COLS_CTAS = L <= 512 ? 3 : 1;
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
@@ -194,10 +196,10 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
     const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
     const float2* zr = zph + (ab ? rb : ra);
     if (zk) {
-#pragma unroll 8
+#pragma unroll  // every staging load in flight before the first store
         for (int n1 = 0; n1 < E; ++n1) s[j + n1 * (T + 1)] = zr[mirror(j + n1 * T, F)];
     } else {
-#pragma unroll 8
+#pragma unroll  // every staging load in flight before the first store
         for (int n1 = 0; n1 < E; ++n1) {
             const int mx = mirror(j + n1 * T, F);
             s[j + n1 * (T + 1)] = make_float2(phase[ra + mx], phase[rb + mx]);
@@ -242,7 +244,7 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
     auto src = [&](int Y, int c) { return ((size_t)a * F + mirror(Y, F)) * F + x0 + c; };
-#pragma unroll 4
+#pragma unroll  // every staging load in flight before the first store
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, Y = i / NC;
         const size_t o = src(Y, c);
@@ -355,7 +357,7 @@ k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ pha
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
     const int a = blockIdx.y, c0 = blockIdx.x * B;
-#pragma unroll 8
+#pragma unroll  // every staging load in flight before the first store
     for (int r = 0; r < B * L / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
         float2 v;
