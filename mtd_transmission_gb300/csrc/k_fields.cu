@@ -286,11 +286,10 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
 // ky > L/2.  The row's left half comes from the stored right half of row -ky.
 template <int L>
 struct TamMul {
-    const float2* tw;
     int r;
     float nrm, ky;
-    __device__ __forceinline__ float2 operator()(int kx, float2 Q) const {
-        const float2 w = __ldg(&tw[((kx + r) & (L - 1)) * (kTwN / L)]);  // exp(-2 pi i (kx+ky)/L)
+    // w = exp(-2 pi i (kx + ky)/L)
+    __device__ __forceinline__ float2 operator()(int kx, float2 w, float2 Q) const {
         // Qm = conj(Q^(-k)) = -exp(+2 pi i (kx+ky)/L) conj(Q)
         const float2 Qm = make_float2(-(w.x * Q.x - w.y * Q.y), -(-w.y * Q.x - w.x * Q.y));
         const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y + Qm.y) * nrm);
@@ -298,8 +297,8 @@ struct TamMul {
         const float kxv = kappa(kx, L);
         const float k2 = kxv * kxv + ky * ky;
         const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
-        const float den = kTwoPi * k2;
-        return (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y / den, -num.x / den);
+        const float rden = 1.0f / (kTwoPi * k2);
+        return (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y * rden, -num.x * rden);
     }
 };
 
@@ -337,8 +336,23 @@ k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw
         }
         x[n1] = v;
     }
-    fft_warp_filter<L, -1>(x, sm + tr * W::STRIDE, j, tw,
-                           TamMul<L>{tw, r, 1.0f / ((float)L * (float)L), kappa(r, L)});
+    // forward FFT along x, tampon, inverse FFT: fft_warp_filter with the
+    // twiddle exp(-2 pi i (kx + r)/L) of bin kx = j + q T + E k2 formed as the
+    // lane's factor for (j + q T + r) times the compile-time root exp(-2 pi i k2/T)
+    float2 wl[E / T];
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) wl[q] = __ldg(&tw[((j + q * T + r) & (L - 1)) * (kTwN / L)]);
+    const TamMul<L> tam{r, 1.0f / ((float)L * (float)L), kappa(r, L)};
+    float2* s = sm + tr * W::STRIDE;
+    fft_warp_regs<L, -1>(x, s, j, tw);
+    static_for<0, E / T>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        static_for<0, T>([&](auto kc) {
+            constexpr int k2 = decltype(kc)::value;
+            x[q * T + k2] = tam(j + q * T + E * k2, twc<T, k2, -1>(wl[q]), x[q * T + k2]);
+        });
+    });
+    fft_warp_regs_rev<L, +1>(x, s, j, tw);
     if (active) {
         float2* dst = tq + ((size_t)a * L + r) * F - F;
 #pragma unroll
