@@ -169,8 +169,10 @@ struct VCfg {
     static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
     static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;  // pass-2 transform stride, 2 mod 16
     static constexpr size_t SMEM_COLS = (size_t)B * VS * sizeof(float2);
-    // pass-2 CTAs per SM the registers are bounded for (up to L = 512; the
-    // 1024-point mirror runs 384 threads a CTA and needs its registers)
+    // CTAs per SM the registers of passes 1 and 2 are bounded for (up to
+    // L = 512; the 1024-point mirror runs 384 threads a CTA and needs its
+    // registers).  Alone the passes run faster at 2 CTAs; with four chunks in
+    // flight the smaller footprint leaves room for the other streams' CTAs.
     static constexpr int COLS_CTAS = L <= 512 ? 3 : 1;
 };
 
@@ -180,7 +182,7 @@ struct VCfg {
 // only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi is kept:
 // gx[Y][X] = sign(X) gxh[m(Y)][m(X)].
 template <int L>
-__global__ void __launch_bounds__(VCfg<L>::NT)
+__global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
 k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ tw,
               float* __restrict__ gxh) {
     using C = VCfg<L>;
