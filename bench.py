@@ -151,6 +151,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(values, world: int, device):
+    """Element-wise maximum of per-rank timings over the job's ranks (the
+    slowest rank sets the whole job's time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), device=device, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(world: int, steps: int, seconds: float) -> float:
+    """Units per second of the whole job: each of the `world` replicas
+    processed `steps` units in at most `seconds`."""
+    return world * steps / seconds
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -541,11 +558,8 @@ def main():
         prof = ctx.profile_read()
         ctx.profile(False)
         ctx.set_schedule(*SCHEDULE)
-    t_max = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    ms_max = float(t_max.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks([ms], world, "cuda")[0]
+    value = whole_job_rate(world, args.steps, ms_max / 1e3)
 
     # end to end: pinned host holograms and outputs through the C ABI.  Sync:
     # tdm_pipeline per step (returns with the volume in host memory).
@@ -584,13 +598,10 @@ def main():
                 ctx.pipeline_async(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
             ctx.synchronize()
             e2e_trials_s.append(time.perf_counter() - t0)
-    t_e = torch.tensor(e2e_trials_s + [e2e_sync_s], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
-    t_e = t_e.tolist()
-    e2e_trials = [world * args.e2e_steps / s for s in t_e[:-1]]
+    t_e = max_over_ranks(e2e_trials_s + [e2e_sync_s], world, "cuda")
+    e2e_trials = [whole_job_rate(world, args.e2e_steps, s) for s in t_e[:-1]]
     e2e_value = statistics.median(e2e_trials) if e2e_trials else None
-    e2e_sync = world * args.e2e_steps / t_e[-1] if args.e2e_steps > 0 else None
+    e2e_sync = whole_job_rate(world, args.e2e_steps, t_e[-1]) if args.e2e_steps > 0 else None
     h2d = int(h_holos.numel() * h_holos.element_size())
     d2h = int(2 * D ** 3 * 4 + D ** 3)
 
