@@ -37,7 +37,7 @@ if ROOT not in sys.path:
 
 METRIC = "512³ volumes/s (600 holos): plain vs batched/TV-adjoint; rel-L2≤1e-4 vs FP64"
 UNIT = "volumes/s"
-E2E_TRIALS = 3
+E2E_TRIALS = 5
 SCHEDULE = (16, 4)  # angles per chunk, chunks in flight (tdm_set_schedule)
 
 # Algorithmic bytes per launch unit: the compulsory input and output bytes of
