@@ -62,6 +62,7 @@ def algorithmic_bytes(name, acq, hits_per_angle, band):
     }
     per_volume = {
         "gather": hits_per_angle * acq.nb_holo * 10 + band * D * D * 8,
+        "zpass": band * D * D * 8 + D ** 3 * 8 + D ** 3,
         "ypass": 2 * D ** 3 * 8,
         "xpass": D ** 3 * 8 + 2 * D ** 3 * 4,
     }
@@ -630,6 +631,13 @@ def main():
                     "peak_source": f"{peak_kind} hbm_gbs",
                     "launches_per_step": n_launch, "ms_per_step": round(t_step_ms, 4),
                     "algorithmic_bytes_per_step": int(bytes_step)}
+        # every kernel with algorithmic bytes: achieved GB/s and fraction of the HBM peak
+        roof_all = {}
+        for k, (t_ms, _) in kern.items():
+            b = per_angle[k] * M if k in per_angle else per_volume.get(k)
+            if b and t_ms > 0:
+                gbs = b / (t_ms / 1e3) / 1e9
+                roof_all[k] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
@@ -664,6 +672,7 @@ def main():
                     "sync_mode": "tdm_pipeline per step, each call returns with the volume in host memory"},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "roofline_all": roof_all,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][0])},
