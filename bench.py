@@ -152,6 +152,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def schedule_for(angles: int):
+    """SCHEDULE, with its chunks in flight limited to the context's scratch
+    capacity (min(128, angles rounded up to 16) angles)."""
+    cap = min(128, (angles + 15) // 16 * 16)
+    return SCHEDULE[0], max(1, min(SCHEDULE[1], cap // SCHEDULE[0]))
+
+
 def max_over_ranks(values, world: int, device):
     """Element-wise maximum of per-rank timings over the job's ranks (the
     slowest rank sets the whole job's time)."""
@@ -452,7 +459,7 @@ def workload_config(acq, args):
                         f"Volkov + aberration correction, {acq.dim_final}^3 volume",
             "holograms": acq.nb_holo, "hologram_px": acq.ccd_roix, "field_px": 2 * acq.nxmax,
             "volume": acq.dim_final, "parallelism": f"replicas x{args.gpus}",
-            "schedule": {"chunk": SCHEDULE[0], "lanes": SCHEDULE[1]},
+            "schedule": {"chunk": schedule_for(acq.nb_holo)[0], "lanes": schedule_for(acq.nb_holo)[1]},
             "l2": "inputs larger than L2: 1.26 GB of holograms per step (no flush needed)"}
 
 
@@ -509,7 +516,8 @@ def main():
     M, D = acq.nb_holo, acq.dim_final
     ctx = Context(Geometry.from_acquisition(acq), M)
     ctx.set_mask(mask)
-    ctx.set_schedule(*SCHEDULE)
+    sched = schedule_for(M)
+    ctx.set_schedule(*sched)
     re = torch.empty((D, D, D), dtype=torch.float32, device="cuda")
     im = torch.empty_like(re)
     otf = torch.empty((D, D, D), dtype=torch.uint8, device="cuda")
@@ -547,7 +555,7 @@ def main():
     # next call (launches that share the GPU would have overlapping durations)
     prof, prof_ms = {}, 0.0
     if not args.no_profile_pass:
-        ctx.set_schedule(SCHEDULE[0], 1)
+        ctx.set_schedule(sched[0], 1)
         ctx.profile(True)
         ev0.record(stream)
         for _ in range(args.steps):
@@ -558,7 +566,7 @@ def main():
         prof_ms = ev0.elapsed_time(ev1)
         prof = ctx.profile_read()
         ctx.profile(False)
-        ctx.set_schedule(*SCHEDULE)
+        ctx.set_schedule(*sched)
     ms_max = max_over_ranks([ms], world, "cuda")[0]
     value = whole_job_rate(world, args.steps, ms_max / 1e3)
 
@@ -677,7 +685,7 @@ def main():
             "clocks": clocks,
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][0])},
             "profiled_ms_per_step": round(prof_ms / args.steps, 3),
-            "profile_schedule": {"chunk": SCHEDULE[0], "lanes": 1},
+            "profile_schedule": {"chunk": sched[0], "lanes": 1},
         }
         if not args.no_forms:
             ctx.close()

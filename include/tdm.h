@@ -79,7 +79,8 @@ typedef struct {
 } tdm_derived;
 
 /* Creates a context on the current CUDA device for stacks of up to
- * max_angles holograms.  Replaces the FFTW plan set-up of both programs
+ * max_angles holograms (at most 65535: TDM_EUNSUPPORTED above).  A context is
+ * used by one host thread at a time.  Replaces the FFTW plan set-up of both programs
  * (pretraitement_hors_axe_CPU/main.cpp:91-105,180-189; Reconstruction/main.cpp:131,185,318). */
 int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out);
 int tdm_destroy(tdm_ctx* ctx);

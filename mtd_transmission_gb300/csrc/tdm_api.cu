@@ -216,6 +216,10 @@ int tdm_derive(const tdm_geom* g, tdm_derived* d) {
 int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     if (!geom || !out || max_angles <= 0) return TDM_EINVAL;
     *out = nullptr;
+    if (max_angles > 65535) {  // a voxel's hit count is kept in 16 bits while its column is gathered
+        fprintf(stderr, "tdm_create: at most 65535 angles per stack\n");
+        return TDM_EUNSUPPORTED;
+    }
     std::string why;
     if (int rc = check_geom(geom, why)) {
         fprintf(stderr, "tdm_create: %s\n", why.c_str());

@@ -344,3 +344,10 @@ def test_reference_intensity():
         assert np.array_equal(again, plain)
         with pytest.raises(TdmError):
             ctx.set_reference_intensity(-iref)
+
+
+def test_too_many_angles_refused():
+    """Hit counts are gathered in 16 bits per voxel: more than 65535 angles is refused at creation."""
+    acq, ph, d = small_case("plain_512_born", M=1)
+    with pytest.raises(TdmError):
+        Context(Geometry.from_acquisition(acq), 65536)
