@@ -156,6 +156,71 @@ struct DerivMul {
     }
 };
 
+// Mirror derivative from F-point transforms.  A row z of F samples has the
+// half-sample-symmetric 2F-point mirror m (m[F + x] = m[F - 1 - x] = z[x]),
+// whose spectrum is a DCT-II of z; its spectral derivative (gradient_fft4 on
+// the mirror: FFT, x i 2 pi kappa(k)/2F with kappa(k) = k/2F signed, inverse)
+// is a DST of kappa times that DCT.  Both run as F-point transforms of the
+// row permuted by mirror_pos (even samples, then odd samples reversed): with
+// V that transform,
+//     W[k] = (i pi / 2F) (e^{i pi k/F} V[F - k] - (1 - 2k/F) V[k]),  W[0] = 0,
+// and the unnormalised inverse w of W is the derivative at X = F + x,
+// x = mirror_pos(m): w[m] for m < F/2, -w[m] otherwise.  The mirror's Nyquist
+// bin is zero, so the reference's Nyquist factor -1/2 does not enter.  This
+// is the right half of the 2F-point filter (fft_warp_filter with DerivMul on
+// the mirror), from two F-point transforms instead of two 2F-point ones.
+__host__ __device__ constexpr int mirror_pos(int m, int F) { return m < F / 2 ? 2 * m : 2 * (F - 1 - m) + 1; }
+
+// x[n1] holds row sample mirror_pos(j + T n1) on entry and the derivative at
+// X = F + mirror_pos(j + T n1) on return; s is the transform's exchange array.
+template <int F>
+__device__ __forceinline__ void mirror_derivative(float2 (&x)[WarpFFT<F>::E], float2* s, int j,
+                                                  const float2* __restrict__ tw) {
+    using W = WarpFFT<F>;
+    constexpr int E = W::E, T = W::T, L = 2 * F;
+    fft_warp_regs<F, -1>(x, s, j, tw);
+    // bin k = (j + qT) + E k2 is in x[qT + k2]; bin F - k is held by lane T - j of
+    // the transform, register (E/T - 1 - q)T + (T - 1 - k2), and for lane 0 by
+    // itself, register (T - k2) mod T when q = 0, (E/T - q)T + T - 1 - k2 otherwise
+    const int src = ((threadIdx.x & 31) & ~(T - 1)) + ((T - j) & (T - 1));
+    float2 el[E / T];  // e^{i pi (j + qT)/F}
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) {
+        const float2 t = __ldg(&tw[(j + q * T) * (kTwN / L)]);
+        el[q] = make_float2(t.x, -t.y);
+    }
+    constexpr float c = 0.5f * kTwoPi / (float)L;  // pi / 2F
+    float2 y[E];
+    static_for<0, E / T>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        static_for<0, T>([&](auto kc) {
+            constexpr int k2 = decltype(kc)::value;
+            const float2 pv = x[(E / T - 1 - q) * T + (T - 1 - k2)];
+            float2 vm = make_float2(__shfl_sync(0xffffffffu, pv.x, src), __shfl_sync(0xffffffffu, pv.y, src));
+            if (j == 0) vm = x[q == 0 ? (T - k2) % T : (E / T - q) * T + (T - 1 - k2)];
+            const int k = j + q * T + E * k2;
+            const float2 e = twc<2 * T, k2, 1>(el[q]);  // e^{i pi k/F}
+            const float2 t = c_sub(c_mul(e, vm), c_scale(x[q * T + k2], 1.0f - 2.0f * (float)k / (float)F));
+            y[q * T + k2] = k == 0 ? make_float2(0.0f, 0.0f) : make_float2(-c * t.y, c * t.x);
+        });
+    });
+    fft_warp_regs_rev<F, +1>(y, s, j, tw);
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) x[n1] = (j + n1 * T < F / 2) ? y[n1] : make_float2(-y[n1].x, -y[n1].y);
+}
+
+// Pass 1 in CTAs of 4 image row pairs: 8 row transforms of Z, then 4 of the
+// pairs' packed phases, F-point each (mirror_derivative).
+template <int F>
+struct RCfg {
+    using W = WarpFFT<F>;
+    static constexpr int P = 4;                 // row pairs per CTA
+    static constexpr int B = 3 * P;             // transforms per CTA
+    static constexpr int NT = B * W::T;
+    static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
+    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
+};
+
 // Transforms of the two Volkov derivative passes: per pair of image rows (or
 // columns), the Z = exp(i phi) transform of each, then one transform of both
 // phases packed as phi_a + i phi_b.  The 2P Z transforms come first so that
@@ -177,17 +242,18 @@ struct VCfg {
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
-// row, and the spectral x derivative of a mirror row is odd about the row's
-// centre (its Nyquist bin is zero), so only image rows y are transformed and
-// only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi is kept:
-// gx[Y][X] = sign(X) gxh[m(Y)][m(X)].
+// row, and only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi
+// is kept: gx[Y][X] = sign(X) gxh[m(Y)][m(X)].  Each image row's x derivative
+// on that half comes from F-point transforms (mirror_derivative): one of Z
+// per row, one of the packed phases phi_a + i phi_b per pair.
 template <int L>
-__global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
+__global__ void __launch_bounds__(RCfg<L / 2>::NT)
 k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ tw,
               float* __restrict__ gxh) {
-    using C = VCfg<L>;
+    constexpr int F = L / 2;
+    using C = RCfg<F>;
     using W = typename C::W;
-    constexpr int F = L / 2, T = W::T, E = W::E, P = C::P;
+    constexpr int T = W::T, E = W::E, P = C::P;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const bool zk = tr < 2 * P;                       // Z transform of one row, else packed phases of a pair
@@ -197,30 +263,33 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
     float2* s = sm + tr * W::STRIDE;
     const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
     const float2* zr = zph + (ab ? rb : ra);
+    float2 x[E];
     if (zk) {
-#pragma unroll  // every staging load in flight before the first store
-        for (int n1 = 0; n1 < E; ++n1) s[j + n1 * (T + 1)] = zr[mirror(j + n1 * T, F)];
+#pragma unroll
+        for (int n1 = 0; n1 < E; ++n1) x[n1] = zr[mirror_pos(j + n1 * T, F)];
     } else {
-#pragma unroll  // every staging load in flight before the first store
+#pragma unroll
         for (int n1 = 0; n1 < E; ++n1) {
-            const int mx = mirror(j + n1 * T, F);
-            s[j + n1 * (T + 1)] = make_float2(phase[ra + mx], phase[rb + mx]);
+            const int p = mirror_pos(j + n1 * T, F);
+            x[n1] = make_float2(phase[ra + p], phase[rb + p]);
         }
     }
-    __syncwarp();
-    fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
+    mirror_derivative<F>(x, s, j, tw);
+    __syncwarp();  // the transform's exchanges are done with s
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) s[W::pad(mirror_pos(j + n1 * T, F))] = x[n1];
     __syncthreads();
     if (zk) {
         const float2* sp = sm + (2 * P + pair) * W::STRIDE;
         float* out = gxh + (ab ? rb : ra);
 #pragma unroll
-        for (int n1 = E / 2; n1 < E; ++n1) {
-            const int X = j + n1 * T;
-            const float2 z = zr[X - F];  // mirror(X) = X - F on the right half
-            const float2 g = s[j + n1 * (T + 1)];
+        for (int n1 = 0; n1 < E; ++n1) {
+            const int xx = j + n1 * T;
+            const float2 z = zr[xx];
+            const float2 g = s[W::pad(xx)];
             const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
-            const float2 q = sp[j + n1 * (T + 1)];
-            out[X - F] = (ax - (ab ? q.y : q.x)) * kInvTwoPi;
+            const float2 q = sp[W::pad(xx)];
+            out[xx] = (ax - (ab ? q.y : q.x)) * kInvTwoPi;
         }
     }
 }
@@ -494,7 +563,8 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
-    const size_t sm_vrows = (size_t)VC::B * VC::W::STRIDE * sizeof(float2);
+    using RC = RCfg<F>;
+    const size_t sm_vrows = RC::SMEM;
     const size_t sm_vcols = VC::SMEM_COLS;
     if (allow_smem(k_field_rows<F>, FC::SMEM) || allow_smem(k_field_cols<F>, FC::SMEM) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
@@ -524,7 +594,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                k_volkov_rows<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vrows, c->stream>>>(b.phase, b.zph, b.tw,
+                k_volkov_rows<L><<<dim3(F / (2 * RC::P), m), RC::NT, sm_vrows, c->stream>>>(b.phase, b.zph, b.tw,
                                                                                                      b.gx);
             }
             {
