@@ -221,23 +221,27 @@ struct RCfg {
     static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
-// Transforms of the two Volkov derivative passes: per pair of image rows (or
-// columns), the Z = exp(i phi) transform of each, then one transform of both
-// phases packed as phi_a + i phi_b.  The 2P Z transforms come first so that
-// a warp never mixes the two kinds.
+// Pass 2 in CTAs of NC = 8 mirror columns: 12 F-point derivative transforms
+// (8 of Z, one per column, then 4 of the columns' packed phases), then the NC
+// 2F-point transforms of Q along the column.  The two phases map threads to
+// transforms separately (the two sizes may differ in lanes per transform).
 template <int L>
 struct VCfg {
-    using W = WarpFFT<L>;
-    static constexpr int P = 4;                 // row or column pairs per CTA
-    static constexpr int B = 3 * P;             // transforms per CTA
-    static constexpr int NT = B * W::T;
-    static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
-    static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;  // pass-2 transform stride, 2 mod 16
-    static constexpr size_t SMEM_COLS = (size_t)B * VS * sizeof(float2);
-    // CTAs per SM the registers of passes 1 and 2 are bounded for (up to
-    // L = 512; the 1024-point mirror runs 384 threads a CTA and needs its
-    // registers).  Alone the passes run faster at 2 CTAs; with four chunks in
-    // flight the smaller footprint leaves room for the other streams' CTAs.
+    using W = WarpFFT<L>;                        // Q transforms
+    using WF = WarpFFT<L / 2>;                   // derivative transforms
+    static constexpr int P = 4;                  // column pairs per CTA
+    static constexpr int NC = 2 * P;             // columns per CTA
+    static constexpr int BF = 3 * P;             // derivative transforms per CTA
+    static_assert(NC % WF::G == 0, "a warp holds one kind of derivative transform");
+    static constexpr int NT = BF * WF::T > NC * W::T ? BF * WF::T : NC * W::T;
+    // array strides 2 mod 16 float2: a warp's 8 columns x 4 rows of the staging
+    // loops land in distinct banks
+    static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;
+    static constexpr int FS = WF::LEN + ((2 - WF::LEN % 16) + 16) % 16;
+    static constexpr size_t SMEM_COLS = ((size_t)BF * FS + (size_t)NC * VS) * sizeof(float2);
+    // CTAs per SM the registers are bounded for (up to L = 512; larger mirrors
+    // need their registers).  Alone the pass runs faster at 2 CTAs; with four
+    // chunks in flight the smaller footprint leaves room for the other streams' CTAs.
     static constexpr int COLS_CTAS = L <= 512 ? 3 : 1;
 };
 
@@ -297,55 +301,74 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
 // Pass 2: columns X = F + x of the mirror (columns X and L-1-X are the same
 // image column): gy like gx, then Q = gx + i gy and its FFT along y.  The
 // columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
-// pass 3.  The loads and the gy epilogue run CTA-wide with the NC = 8
-// columns fastest (contiguous in global memory); the phasor and gx are read
-// again from global memory (L2) in the epilogue rather than kept in shared
-// memory, which leaves room for a third CTA per SM.
+// pass 3.  Along a column the y derivative of the even mirror is odd and gx is
+// even, so Q[L-1-Y] = conj(Q[Y]): the derivatives come from F-point transforms
+// on the half Y = F + y (mirror_derivative) and the other half by conjugation.
+// The loads and the gy epilogue run CTA-wide with the NC columns fastest
+// (contiguous in global memory); the phasor and gx are read from L2 in the
+// epilogue.
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
 k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
               const float2* __restrict__ tw, float2* __restrict__ qc) {
     using C = VCfg<L>;
     using W = typename C::W;
-    constexpr int F = L / 2, T = W::T, NC = 2 * C::P, NT = C::NT;
-    // Transform arrays VS = 2 mod 16 float2 apart: a warp's 8 columns x 4 rows
-    // land in distinct banks.
-    constexpr int VS = C::VS;
+    using WF = typename C::WF;
+    constexpr int F = L / 2, NC = C::NC, NT = C::NT, VS = C::VS, FS = C::FS;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    float2* sq = sm + C::BF * FS;  // NC Q arrays of the 2F-point transforms
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
-    auto src = [&](int Y, int c) { return ((size_t)a * F + mirror(Y, F)) * F + x0 + c; };
+    auto src = [&](int y, int c) { return ((size_t)a * F + y) * F + x0 + c; };
+    // image row y goes to element m of the permuted column, mirror_pos(m) = y
+    auto slot = [&](int y) { return (y & 1) ? F - 1 - (y >> 1) : (y >> 1); };
 #pragma unroll  // every staging load in flight before the first store
-    for (int i = threadIdx.x; i < NC * L; i += NT) {
-        const int c = i % NC, Y = i / NC;
-        const size_t o = src(Y, c);
-        sm[c * VS + W::pad(Y)] = zph[o];
-        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * VS + W::pad(Y)])[c & 1] = phase[o];
+    for (int i = threadIdx.x; i < NC * F; i += NT) {
+        const int c = i % NC, y = i / NC;
+        const size_t o = src(y, c);
+        const int e = WF::pad(slot(y));
+        sm[c * FS + e] = zph[o];
+        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * FS + e])[c & 1] = phase[o];
     }
     __syncthreads();
-    float2* s = sm + tr * VS;
-    fft_warp_filter_call<L, -1>(s, j, tw, DerivMul<L>{});
+    {
+        const int tr = threadIdx.x / WF::T, j = threadIdx.x % WF::T;
+        if (tr < C::BF) {  // warp-uniform
+            float2* s = sm + tr * FS;
+            float2 x[WF::E];
+#pragma unroll
+            for (int n1 = 0; n1 < WF::E; ++n1) x[n1] = s[WF::pad(j + n1 * WF::T)];
+            mirror_derivative<F>(x, s, j, tw);
+            __syncwarp();
+#pragma unroll
+            for (int n1 = 0; n1 < WF::E; ++n1) s[WF::pad(mirror_pos(j + n1 * WF::T, F))] = x[n1];
+        }
+    }
     __syncthreads();
-    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi; Q = gx + i gy into the Z arrays
+    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi at Y = F + y; Q = gx + i gy there
+    // and conj(Q) at Y = F - 1 - y
 #pragma unroll 4
-    for (int i = threadIdx.x; i < NC * L; i += NT) {
-        const int c = i % NC, Y = i / NC;
-        const size_t o = src(Y, c);
+    for (int i = threadIdx.x; i < NC * F; i += NT) {
+        const int c = i % NC, y = i / NC;
+        const size_t o = src(y, c);
         const float2 z = zph[o];
         const float gx = gxh[o];
-        float2* gp = &sm[c * VS + W::pad(Y)];
-        const float2 g = *gp;
-        const float2 q = sm[(NC + (c >> 1)) * VS + W::pad(Y)];
+        const float2 g = sm[c * FS + WF::pad(y)];
+        const float2 q = sm[(NC + (c >> 1)) * FS + WF::pad(y)];
         const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
-        *gp = make_float2(gx, (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi);
+        const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi;
+        sq[c * VS + W::pad(F + y)] = make_float2(gx, gy);
+        sq[c * VS + W::pad(F - 1 - y)] = make_float2(gx, -gy);
     }
     __syncthreads();
-    if (tr < NC) fft_warp_call<L, -1>(s, j, tw);  // warp-uniform
+    {
+        const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
+        if (tr < NC) fft_warp_call<L, -1>(sq + tr * VS, j, tw);  // warp-uniform
+    }
     __syncthreads();
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, ky = i / NC;
-        qc[((size_t)a * L + ky) * F + x0 + c] = sm[c * VS + W::pad(ky)];
+        qc[((size_t)a * L + ky) * F + x0 + c] = sq[c * VS + W::pad(ky)];
     }
 }
 
