@@ -8,10 +8,13 @@
 //  volkov     deroul_volkov4_total_sym_paire (src/deroulement_volkov4.cpp:14-92) on
 //             the 2F x 2F even mirror.  A 2D spectral derivative along x is the
 //             1D spectral derivative of each row (kappa depends on kx only), so
-//             gradient_fft4 becomes a row pass and a column pass; the two real
-//             fields of integ_grad4 share one complex 2D FFT (x + i y) and are
-//             separated by Hermitian symmetry.  Literal kappa (Nyquist -1/2),
-//             literal Re() projections, zero-frequency term 0.
+//             gradient_fft4 becomes a row pass and a column pass, each computed
+//             from F-point transforms (the mirror's spectrum is a DCT of the row,
+//             its derivative a DST: mirror_derivative); the two real fields of
+//             integ_grad4 share one complex 2D FFT (x + i y) and are separated by
+//             Hermitian symmetry.  Literal kappa (the mirror's Nyquist bin is
+//             zero, so its -1/2 factor does not enter the derivatives), literal
+//             Re() projections, zero-frequency term 0.
 //  fit/form   aberCorr2 / ampliCorr2 (Correction_aberration.cpp:166-217) and the
 //             Born/Rytov formation (main.cpp:289-316).  The least-squares
 //             projection onto degree-4 polynomials is computed in a basis that is
