@@ -150,15 +150,6 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
 }
 
 // ---------------------------------------------------------------- Volkov unwrap
-// i 2 pi kappa(k) / L: the spectral derivative factor of gradient_fft4.
-template <int L>
-struct DerivMul {
-    __device__ __forceinline__ float2 operator()(int k, float2 z) const {
-        const float c = kTwoPi * kappa(k, L) / (float)L;
-        return make_float2(-c * z.y, c * z.x);
-    }
-};
-
 // Mirror derivative from F-point transforms.  A row z of F samples has the
 // half-sample-symmetric 2F-point mirror m (m[F + x] = m[F - 1 - x] = z[x]),
 // whose spectrum is a DCT-II of z; its spectral derivative (gradient_fft4 on
@@ -170,8 +161,8 @@ struct DerivMul {
 // and the unnormalised inverse w of W is the derivative at X = F + x,
 // x = mirror_pos(m): w[m] for m < F/2, -w[m] otherwise.  The mirror's Nyquist
 // bin is zero, so the reference's Nyquist factor -1/2 does not enter.  This
-// is the right half of the 2F-point filter (fft_warp_filter with DerivMul on
-// the mirror), from two F-point transforms instead of two 2F-point ones.
+// is the right half of the 2F-point filter (FFT of the mirror, x i 2 pi
+// kappa(k)/2F, inverse), from two F-point transforms instead of two 2F-point ones.
 __host__ __device__ constexpr int mirror_pos(int m, int F) { return m < F / 2 ? 2 * m : 2 * (F - 1 - m) + 1; }
 
 // x[n1] holds row sample mirror_pos(j + T n1) on entry and the derivative at
