@@ -203,6 +203,53 @@ __device__ __forceinline__ void mirror_derivative(float2 (&x)[WarpFFT<F>::E], fl
     for (int n1 = 0; n1 < E; ++n1) x[n1] = (j + n1 * T < F / 2) ? y[n1] : make_float2(-y[n1].x, -y[n1].y);
 }
 
+// 2F-point FFT of a column with Q[2F-1-Y] = conj(Q[Y]) from one F-point
+// transform.  With u[y] = Q[F + y], a = Re u, b = Im u,
+//     FFT(Q)[k] = 2 (-1)^k e^{i pi k/2F} R[k],
+//     R[k] = sum_y a[y] cos(pi k (y + 1/2)/F) + b[y] sin(pi k (y + 1/2)/F),
+// real.  The cosine sum is a DCT-II of a and the sine sum a DCT-II of
+// b' = (-1)^y b read backwards, so both come from C = DCT-II(a + i b') (the
+// first half of mirror_derivative): with w = e^{-i pi k/2F},
+//     C[k] = (w V[k] + conj(w) V[F-k]) / 2,  C[F-k] = i (w V[k] - conj(w) V[F-k]) / 2,
+//     R[k] = Re C[k] + Im C[F-k],  R[2F-k] = Im C[F-k] - Re C[k],  R[F] = Im C[0].
+// x holds a + i b' permuted by mirror_pos (x[n1] = element j + T n1) on
+// entry; out(k, value) receives every bin k in [0, 2F) once.
+template <int F, class Out>
+__device__ __forceinline__ void symmetric_fft(float2 (&x)[WarpFFT<F>::E], float2* s, int j,
+                                              const float2* __restrict__ tw, Out&& out) {
+    using W = WarpFFT<F>;
+    constexpr int E = W::E, T = W::T, L = 2 * F;
+    fft_warp_regs<F, -1>(x, s, j, tw);
+    __syncwarp();  // the transform is done with s, which out() may overwrite
+    const int src = ((threadIdx.x & 31) & ~(T - 1)) + ((T - j) & (T - 1));  // holder of bin F - k
+    float2 wl[E / T];  // e^{-i pi (j + qT)/2F}
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) wl[q] = __ldg(&tw[(j + q * T) * (kTwN / (2 * L))]);
+    static_for<0, E / T>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        static_for<0, T>([&](auto kc) {
+            constexpr int k2 = decltype(kc)::value;
+            const float2 pv = x[(E / T - 1 - q) * T + (T - 1 - k2)];
+            float2 vm = make_float2(__shfl_sync(0xffffffffu, pv.x, src), __shfl_sync(0xffffffffu, pv.y, src));
+            if (j == 0) vm = x[q == 0 ? (T - k2) % T : (E / T - q) * T + (T - 1 - k2)];
+            const int k = j + q * T + E * k2;
+            const float2 w = twc<4 * T, k2, -1>(wl[q]);  // e^{-i pi k/2F}
+            const float2 a = c_mul(w, x[q * T + k2]), b = c_mul(c_conj(w), vm);
+            const float ck = 0.5f * (a.x + b.x);          // Re C[k]
+            const float cf = 0.5f * (a.x - b.x);          // Im C[F-k] = Re((w V[k] - conj(w) V[F-k]) / 2)
+            const float sg = (k & 1) ? -2.0f : 2.0f;      // 2 (-1)^k
+            if (k == 0) {
+                out(0, make_float2(2.0f * ck, 0.0f));
+                out(F, make_float2(0.0f, 2.0f * 0.5f * (a.y + b.y)));  // 2 i Im C[0]
+            } else {
+                const float r1 = sg * (ck + cf), r2 = -sg * (cf - ck);
+                out(k, make_float2(r1 * w.x, -r1 * w.y));         // 2 (-1)^k conj(w) R[k]
+                out(L - k, make_float2(r2 * w.x, r2 * w.y));      // -2 (-1)^k w R[2F-k]
+            }
+        });
+    });
+}
+
 // Pass 1 in CTAs of 4 image row pairs: 8 row transforms of Z, then 4 of the
 // pairs' packed phases, F-point each (mirror_derivative).
 template <int F>
@@ -216,23 +263,22 @@ struct RCfg {
 };
 
 // Pass 2 in CTAs of NC = 8 mirror columns: 12 F-point derivative transforms
-// (8 of Z, one per column, then 4 of the columns' packed phases), then the NC
-// 2F-point transforms of Q along the column.  The two phases map threads to
-// transforms separately (the two sizes may differ in lanes per transform).
+// (8 of Z, one per column, then 4 of the columns' packed phases), then NC
+// F-point transforms giving the 2F-point FFT of Q along each column
+// (symmetric_fft).  Bins [0, F) of a column's FFT are staged in its Q array,
+// bins [F, 2F) in the derivative array of the same index.
 template <int L>
 struct VCfg {
-    using W = WarpFFT<L>;                        // Q transforms
-    using WF = WarpFFT<L / 2>;                   // derivative transforms
+    using WF = WarpFFT<L / 2>;
     static constexpr int P = 4;                  // column pairs per CTA
     static constexpr int NC = 2 * P;             // columns per CTA
     static constexpr int BF = 3 * P;             // derivative transforms per CTA
     static_assert(NC % WF::G == 0, "a warp holds one kind of derivative transform");
-    static constexpr int NT = BF * WF::T > NC * W::T ? BF * WF::T : NC * W::T;
-    // array strides 2 mod 16 float2: a warp's 8 columns x 4 rows of the staging
-    // loops land in distinct banks
-    static constexpr int VS = W::LEN + ((2 - W::LEN % 16) + 16) % 16;
+    static constexpr int NT = BF * WF::T;
+    // array stride 2 mod 16 float2 and at least F: a warp's 8 columns x 4 rows
+    // of the staging loops land in distinct banks
     static constexpr int FS = WF::LEN + ((2 - WF::LEN % 16) + 16) % 16;
-    static constexpr size_t SMEM_COLS = ((size_t)BF * FS + (size_t)NC * VS) * sizeof(float2);
+    static constexpr size_t SMEM_COLS = (size_t)(BF + NC) * FS * sizeof(float2);
     // CTAs per SM the registers are bounded for (up to L = 512; larger mirrors
     // need their registers).  Alone the pass runs faster at 2 CTAs; with four
     // chunks in flight the smaller footprint leaves room for the other streams' CTAs.
@@ -297,21 +343,21 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
 // columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
 // pass 3.  Along a column the y derivative of the even mirror is odd and gx is
 // even, so Q[L-1-Y] = conj(Q[Y]): the derivatives come from F-point transforms
-// on the half Y = F + y (mirror_derivative) and the other half by conjugation.
-// The loads and the gy epilogue run CTA-wide with the NC columns fastest
-// (contiguous in global memory); the phasor and gx are read from L2 in the
-// epilogue.
+// on the half Y = F + y (mirror_derivative), and so does the FFT of Q
+// (symmetric_fft).  The loads and the gy epilogue run CTA-wide with the NC
+// columns fastest (contiguous in global memory); the phasor and gx are read
+// from L2 in the epilogue.
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
 k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
               const float2* __restrict__ tw, float2* __restrict__ qc) {
     using C = VCfg<L>;
-    using W = typename C::W;
     using WF = typename C::WF;
-    constexpr int F = L / 2, NC = C::NC, NT = C::NT, VS = C::VS, FS = C::FS;
+    constexpr int F = L / 2, NC = C::NC, NT = C::NT, FS = C::FS, T = WF::T, E = WF::E;
     extern __shared__ float2 sm[];
-    float2* sq = sm + C::BF * FS;  // NC Q arrays of the 2F-point transforms
+    float2* sq = sm + C::BF * FS;  // NC arrays: Q of each column (permuted), then its FFT bins [0, F)
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
     auto src = [&](int y, int c) { return ((size_t)a * F + y) * F + x0 + c; };
     // image row y goes to element m of the permuted column, mirror_pos(m) = y
     auto slot = [&](int y) { return (y & 1) ? F - 1 - (y >> 1) : (y >> 1); };
@@ -324,22 +370,19 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
         reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * FS + e])[c & 1] = phase[o];
     }
     __syncthreads();
-    {
-        const int tr = threadIdx.x / WF::T, j = threadIdx.x % WF::T;
-        if (tr < C::BF) {  // warp-uniform
-            float2* s = sm + tr * FS;
-            float2 x[WF::E];
+    {  // y derivatives of Z (transforms 0 .. NC-1) and of the packed phases
+        float2* s = sm + tr * FS;
+        float2 x[E];
 #pragma unroll
-            for (int n1 = 0; n1 < WF::E; ++n1) x[n1] = s[WF::pad(j + n1 * WF::T)];
-            mirror_derivative<F>(x, s, j, tw);
-            __syncwarp();
+        for (int n1 = 0; n1 < E; ++n1) x[n1] = s[WF::pad(j + n1 * T)];
+        mirror_derivative<F>(x, s, j, tw);
+        __syncwarp();
 #pragma unroll
-            for (int n1 = 0; n1 < WF::E; ++n1) s[WF::pad(mirror_pos(j + n1 * WF::T, F))] = x[n1];
-        }
+        for (int n1 = 0; n1 < E; ++n1) s[WF::pad(mirror_pos(j + n1 * T, F))] = x[n1];
     }
     __syncthreads();
-    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi at Y = F + y; Q = gx + i gy there
-    // and conj(Q) at Y = F - 1 - y
+    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi and Q = gx + i gy at Y = F + y;
+    // the Q array takes gx + i (-1)^y gy, permuted (symmetric_fft's input)
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * F; i += NT) {
         const int c = i % NC, y = i / NC;
@@ -350,19 +393,25 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
         const float2 q = sm[(NC + (c >> 1)) * FS + WF::pad(y)];
         const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
         const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi;
-        sq[c * VS + W::pad(F + y)] = make_float2(gx, gy);
-        sq[c * VS + W::pad(F - 1 - y)] = make_float2(gx, -gy);
+        sq[c * FS + WF::pad(slot(y))] = make_float2(gx, (y & 1) ? -gy : gy);
     }
     __syncthreads();
-    {
-        const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
-        if (tr < NC) fft_warp_call<L, -1>(sq + tr * VS, j, tw);  // warp-uniform
+    if (tr < NC) {  // warp-uniform
+        float2* s = sq + tr * FS;
+        float2* hi = sm + tr * FS;  // the derivative array of the same index, free now
+        float2 x[E];
+#pragma unroll
+        for (int n1 = 0; n1 < E; ++n1) x[n1] = s[WF::pad(j + n1 * T)];
+        symmetric_fft<F>(x, s, j, tw, [&](int k, float2 v) {
+            if (k < F) s[k] = v;
+            else hi[k - F] = v;
+        });
     }
     __syncthreads();
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * L; i += NT) {
         const int c = i % NC, ky = i / NC;
-        qc[((size_t)a * L + ky) * F + x0 + c] = sq[c * VS + W::pad(ky)];
+        qc[((size_t)a * L + ky) * F + x0 + c] = ky < F ? sq[c * FS + ky] : sm[c * FS + ky - F];
     }
 }
 
