@@ -12,9 +12,12 @@ namespace extract {
 
 // Both passes run on the warp-resident FFT (fft_warp.cuh) in CTAs of 8
 // warps.  The row pass packs two real rows into one complex transform and
-// keeps the crop's kx band, written column-major (inter[a][c][y]): each lane
-// stores the two rows' values of one column as one 16-byte word (the CTA's
-// other row pairs fill the rest of each column segment).  The column pass
+// keeps the crop's kx band, written column-major (inter[a][c][y]): the two
+// rows' values of one column are one 16-byte word, and the CTA's row pairs
+// fill one segment of each column, stored whole from a shared-memory tile
+// (16-byte pieces of distinct lines, one per lane, cost the L1 a wavefront
+// each and L2 a partial-sector write; the tile took both passes from 1.83 to
+// 1.80 ms per 600 holograms and the step from 5.32 to 5.26 ms).  The column pass
 // then reads whole columns contiguously and writes the crop rows through a
 // shared-memory tile (and, on request, the crop's partial specular-peak
 // winners, one record per warp).
@@ -28,7 +31,13 @@ struct ExtractCfg {
     // would allow 3 up to H = 1024, but capping to 80 registers for them
     // spills and measured slower than 2)
     static constexpr int ROWS_CTAS = H >= 2048 ? 1 : 2;
-    static size_t smem_rows(int) { return (size_t)P * W::STRIDE * sizeof(float2); }
+    // band columns per round of the row pass's output tile (CB x (P + 1)
+    // 16-byte words, about 18 KB; the odd stride keeps both its column-wise
+    // fill and its row-wise drain free of bank conflicts)
+    static constexpr int CB = 1024 / P;
+    static size_t smem_rows(int) {
+        return (size_t)P * W::STRIDE * sizeof(float2) + (size_t)CB * (P + 1) * sizeof(float4);
+    }
     static size_t smem_cols(int F) { return ((size_t)C * W::STRIDE + (size_t)F * (C + 1)) * sizeof(float2); }
     static dim3 grid_rows(int m) { return dim3(H / (2 * P), m); }
     static dim3 grid_cols(int F, int m) { return dim3(F / C, m); }
@@ -123,13 +132,27 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
     }
     __syncwarp();
     // separate the two real rows on the kx band: Xa = (Z(k) + conj Z(-k))/2, Xb = (Z(k) - conj Z(-k))/(2i);
-    // rows ya (even) and yb = ya + 1 of column c are adjacent in inter: one 16-byte store
-    float4* dst = reinterpret_cast<float4*>(inter + (size_t)a * F * H + ya);
-    for (int c = j; c < F; c += T) {
-        const int k = x0 + c, km = (H - k) & (H - 1);
-        const float2 z = s[W::pad(k)], zm = s[W::pad(km)];
-        dst[(size_t)c * (H / 2)] = make_float4(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y), 0.5f * (z.y + zm.y),
-                                               -0.5f * (z.x - zm.x));
+    // rows ya (even) and yb = ya + 1 of column c are adjacent in inter (one
+    // 16-byte word), and the CTA's P row pairs are one 16P-byte segment of
+    // each column.  The words go through the tile, CB columns at a time, so
+    // that each column segment is written by consecutive lanes (whole lines)
+    // rather than as 16-byte pieces of distinct lines.
+    float4* tile = reinterpret_cast<float4*>(sm + P * W::STRIDE);
+    float4* dst = reinterpret_cast<float4*>(inter + (size_t)a * F * H + 2 * blockIdx.x * P);
+    for (int cb = 0; cb < F; cb += Cf::CB) {
+        const int nc = min(Cf::CB, F - cb);
+        for (int c = j; c < nc; c += T) {
+            const int k = x0 + cb + c, km = (H - k) & (H - 1);
+            const float2 z = s[W::pad(k)], zm = s[W::pad(km)];
+            tile[c * (P + 1) + tr] = make_float4(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y), 0.5f * (z.y + zm.y),
+                                                 -0.5f * (z.x - zm.x));
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nc * P; i += Cf::NT) {
+            const int c = i / P, p = i % P;
+            dst[(size_t)(cb + c) * (H / 2) + p] = tile[c * (P + 1) + p];
+        }
+        if (cb + Cf::CB < F) __syncthreads();  // the tile is refilled
     }
 }
 

@@ -64,6 +64,32 @@ def test_extract_8bit():
         assert rel_l2(out[a], ref[a]) <= TOL
 
 
+@pytest.mark.parametrize("roix,nxmax", [(256, 128), (512, 128), (1024, 256)])
+def test_extract_wide_band(roix, nxmax):
+    """Crops wider than one round of the row pass's output tile (64 band
+    columns per round for 256- and 512-pixel holograms, 128 above): the
+    context path against the oracle, and the allocation-free entry point
+    bit for bit against the context path."""
+    import torch
+    from mtd_transmission_gb300 import api
+    acq, ph, d = small_case("plain_512_born", M=2, ccd_roix=roix, nxmax=nxmax, circle_cx=roix // 2,
+                            circle_cy=roix // 2, dim_final=max(4 * nxmax, 128))
+    ref = oracle.extract_stack(d["holos"].astype(np.float64), oracle_cfg(acq))
+    F = 2 * acq.nxmax
+    holos = torch.from_numpy(np.ascontiguousarray(d["holos"])).cuda()
+    out = torch.zeros((2, F, F), dtype=torch.complex64, device="cuda")
+    with Context(Geometry.from_acquisition(acq), 2) as ctx:
+        ctx.extract(holos, spectra_out=out)
+        ctx.synchronize()
+    na = torch.full((2, F, F), complex("nan"), dtype=torch.complex64, device="cuda")
+    assert api.extract_noalloc(Geometry.from_acquisition(acq), holos, na, torch.cuda.current_stream().cuda_stream) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(na, out)
+    o = out.cpu().numpy()
+    for a in range(2):
+        assert rel_l2(o[a], ref[a]) <= TOL, a
+
+
 @pytest.mark.parametrize("case", ["born", "rytov"])
 def test_fields_parity(case, request):
     acq, cfg, d, spec, fields, pos, dbg = request.getfixturevalue(case)
