@@ -78,9 +78,9 @@ def ncu_traffic_per_launch(name, acq):
     if acq.ccd_roix != 1024 or acq.nxmax != 128 or acq.dim_final != 512:
         return None
     if name == "volkov_cols":
-        return 16.835072e6
+        return 16.83968e6 + 0.001024e6
     if name == "extract_rows":
-        return 33.61408e6 + 0.312576e6
+        return 33.616128e6 + 0.341504e6
     if name == "gather":
         return 648.724224e6 * acq.nb_holo / 600 + 419.033088e6
     return None
