@@ -69,6 +69,55 @@ def algorithmic_bytes(name, acq, hits_per_angle, band):
     return per_angle, per_volume
 
 
+# Algorithmic bytes per stage of the path, compulsory input plus output of the
+# stage as a whole (the intermediates between a stage's kernels are not
+# counted; hits = NA-disc bins per angle):
+#   extraction   per hologram  H^2 2 (uint16) + F^2 8 (complex crop)
+#   fields       per angle     F^2 8 + F^2 8
+#   cap mapping  per angle     F^2 8 + hits (8 + 4) 2
+#   volume       per volume    D^3 12 (zeroing) + D^3 12 (normalise, 3D IFFT) + D^3 8 (two f32 volumes)
+# Each stage's time is the sum of its kernels' event times (one chunk in
+# flight).  The fields' last step (forming the field from the unwrapped phase
+# and the fits) runs fused into the cap mapping's row pass, and is timed there.
+STAGE_KERNELS = {
+    "extraction": ("extract_rows", "extract_cols", "argmax"),
+    "fields": ("field_rows", "field_cols", "volkov_rows", "volkov_cols", "volkov_integ_rows",
+               "volkov_integ_cols", "aber_fit", "form"),
+    "cap_mapping": ("cap_rows", "cap_cols"),
+    "volume": ("gather", "zpass", "ypass", "xpass"),
+}
+
+
+def stage_bytes(acq, hits_per_angle):
+    H, F, D, M = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final, acq.nb_holo
+    return {
+        "extraction": M * (H * H * 2 + F * F * 8),
+        "fields": M * (F * F * 8 * 2),
+        "cap_mapping": M * (F * F * 8 + hits_per_angle * (8 + 4) * 2),
+        "volume": D ** 3 * (12 + 12 + 8),
+    }
+
+
+def stage_roofline(acq, hits_per_angle, kern_ms, step_ms, peak):
+    """Achieved GB/s and fraction of the HBM peak per stage (from the per-kernel
+    event times kern_ms, ms per step), and for the whole path over the live
+    step time step_ms."""
+    b = stage_bytes(acq, hits_per_angle)
+    out = {}
+    for st, ks in STAGE_KERNELS.items():
+        t = sum(kern_ms.get(k, 0.0) for k in ks)
+        if t > 0:
+            gbs = b[st] / (t / 1e3) / 1e9
+            out[st] = {"bytes_per_step": int(b[st]), "ms_per_step": round(t, 4), "achieved_gbs": round(gbs, 1),
+                       "frac": round(gbs / peak, 4)}
+    tot = sum(b.values())
+    if step_ms > 0:
+        gbs = tot / (step_ms / 1e3) / 1e9
+        out["whole_path_live"] = {"bytes_per_step": int(tot), "ms_per_step": round(step_ms, 4),
+                                  "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    return out
+
+
 # DRAM bytes (read + write) per launch from one ncu capture of the kernel
 # (profiles/<kernel>_rytov_1024_*.md): the row pass and the Volkov passes on
 # the 64-hologram case (a launch processes 16 angles in every case), the
@@ -681,6 +730,8 @@ def main():
             "gpu_launches": int(launches),
             "roofline": roof,
             "roofline_all": roof_all,
+            "roofline_stages": stage_roofline(acq, hits, {k: v[0] for k, v in kern.items()}, ms_max / args.steps,
+                                              peak),
             "cpu_baseline": cpu,
             "clocks": clocks,
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][0])},
