@@ -83,10 +83,14 @@ typedef struct {
  * used by one host thread at a time.  Replaces the FFTW plan set-up of both programs
  * (pretraitement_hors_axe_CPU/main.cpp:91-105,180-189; Reconstruction/main.cpp:131,185,318). */
 int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out);
+/* Releases the context and its device memory (no counterpart: the reference's
+ * programs exit without releasing their plans). */
 int tdm_destroy(tdm_ctx* ctx);
 const char* tdm_last_error(const tdm_ctx* ctx);
+/* Derived quantities of the context's geometry, and without a context (host
+ * arithmetic only): the manip constructors' derived members
+ * (pretraitement_hors_axe_CPU/manip.cpp:43-57,104; Reconstruction/src/manip.cpp:64-94). */
 int tdm_get_derived(const tdm_ctx* ctx, tdm_derived* out);
-/* Derived quantities without a context (host arithmetic only). */
 int tdm_derive(const tdm_geom* geom, tdm_derived* out);
 
 /* Aberration mask, F*F uint8 (Image_mask.pgm); NULL selects the unit mask.
@@ -140,7 +144,9 @@ int tdm_reconstruct(tdm_ctx* ctx, const float* fields_in, const int32_t* posspec
                     float* absorption_out, uint8_t* otf_out, uint32_t* counts_out);
 
 /* Holograms to volume in one call, fields kept on the device (tomo_pipeline).
- * Equivalent to tdm_extract + tdm_fields + tdm_reconstruct. */
+ * Equivalent to tdm_extract + tdm_fields + tdm_reconstruct.  Replaces the two
+ * programs run back to back (pretraitement_hors_axe_CPU/main.cpp:31-363, then
+ * Reconstruction/main.cpp:57-384) without the field files between them. */
 int tdm_pipeline(tdm_ctx* ctx, const void* holos, int bits, int n, float* indice_out, float* absorption_out,
                  uint8_t* otf_out, uint32_t* counts_out, int32_t* posspec_out);
 
@@ -295,13 +301,18 @@ int tdm_profile_read(tdm_ctx* ctx, int index, const char** name, double* total_m
 int tdm_extract_val(const char* path, const char* key, double def, double* out);
 /* extract_string (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:44-79). */
 int tdm_extract_string(const char* path, const char* key, char* out, size_t cap);
-/* Fills a tdm_geom from recon.txt and config_manip.txt. */
+/* Fills a tdm_geom from recon.txt and config_manip.txt, as the manip
+ * constructors read them (pretraitement_hors_axe_CPU/manip.cpp:9-157,
+ * Reconstruction/src/manip.cpp:10-163). */
 int tdm_read_geom(const char* recon_txt, const char* config_manip_txt, tdm_geom* out);
 /* Binary PGM (P5) reader, 8- or 16-bit (16-bit samples are big-endian in the
  * file).  Replaces charger_image2D_OCV (pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:24-40)
  * with native sample depth: *bits is set to 8 or 16; the ROI is the top-left
  * roi x roi corner.  buf receives roi*roi samples (uint8 or uint16). */
 int tdm_read_pgm(const char* path, int roi, void* buf, int* bits);
+/* Size and maximum sample value of a PGM file (the image size that
+ * charger_image2D_OCV takes from the decoded image,
+ * pretraitement_hors_axe_CPU/src/IO_fonctions.cpp:26,32). */
 int tdm_pgm_info(const char* path, int* width, int* height, int* maxval);
 /* Float32 multi-page TIFF writer (SAV3D_Tiff_Optimized,
  * Reconstruction/src/fonctions.cpp:2286-2357, pages of dim_x x dim_y, resolution
