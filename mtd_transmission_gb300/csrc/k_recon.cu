@@ -51,20 +51,28 @@ __device__ __forceinline__ double cap_fzm0(const Params& p, int2 ps) {
 // position ps and height fz (fonctions.cpp:903-921), or -1 outside the NA
 // disc or for a skipped angle; *sf is sqrt(r^2 - fd^2) in float for the
 // cell's weight.  A plane outside the cap band sets *err and gives -1.
-__device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, int kx, int ky,
+// fzf = (float)fz, converted once by the caller: FP64 instructions run at a
+// small fraction of the FP32 rate on this GPU, so the per-bin path is FP32
+// and FP64 is used only in the rare rounding-boundary branch.
+__device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, float fzf, int kx, int ky,
                                          const double* __restrict__ s_tab, const float* __restrict__ s_tabf,
                                          float* sf, int* __restrict__ err) {
     const int F = p.F, N = p.N;
     const int fdx = ((kx + ps.x) & (F - 1)) - N, fdy = ((ky + ps.y) & (F - 1)) - N;
-    if (!(fz >= 0.0) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;
+    if (!(fzf >= 0.0f) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;  // fz is sqrt(c) >= 0 or -1
     const int ti = (fdy + N) * F + fdx + N;
     // sqrt(r^2 - fd^2) in float: computed from the exact integer when r^2 < 2^24 (equal to the table)
     *sf = p.r2i ? __fsqrt_rn((float)(p.r2i - fdx * fdx - fdy * fdy)) : s_tabf[ti];
-    const float d = *sf - (float)fz;
+    const float d = *sf - fzf;
     const float fr = d - floorf(d);
     // round(sqrt(fdz^2) - fzm0) in FP64 (fonctions.cpp:921); the FP32 value
     // decides unless it lies within 1e-3 of a rounding boundary.
-    const float koz = (fabsf(fr - 0.5f) > 1e-3f) ? floorf(d + 0.5f) : (float)round(s_tab[ti] - fz);
+    float koz;
+    if (fabsf(fr - 0.5f) > 1e-3f) {
+        koz = floorf(d + 0.5f);
+    } else {
+        koz = (float)round(s_tab[ti] - fz);
+    }
     const int z = (int)koz + p.D / 2;
     if (z < p.zmin || z >= p.zmin + p.band) {
         if (err) atomicOr(err, 1);
@@ -75,9 +83,10 @@ __device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, in
 
 // Cap-cell weight (k0/pi)(-2pi) sdz dx^2 (-1)^(kx+ky) of retroPropag_Born
 // (fonctions.cpp:902,927) with the recentring sign of the per-field spectrum.
-__device__ __forceinline__ float cap_weight(const Params& p, float sf, int kx, int ky) {
+// ir = (float)p.inv_rayon, converted once by the caller.
+__device__ __forceinline__ float cap_weight(const Params& p, float sf, float ir, int kx, int ky) {
     const float sg = ((kx + ky) & 1) ? -p.dx2 : p.dx2;
-    return p.cap_scale * (sf * (float)p.inv_rayon) * sg;
+    return p.cap_scale * (sf * ir) * sg;
 }
 
 // Voxel column of FFT bin kx of an angle with specular coordinate q (x or y):
@@ -174,16 +183,17 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
     fft_warp<F, -1>(sm + tr * W::STRIDE, j, tw);
     __syncthreads();
     const double fz = s_fz;
+    const float fzf = (float)fz, ir = (float)p.inv_rayon;
 #pragma unroll 2
     for (int r = 0; r < B * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % B, ky = i / B, kx = kx0 + t;
         const size_t o = ((size_t)a * F + ky) * F + kx;
         float sf = 0.f;
-        const int z = cap_plane(p, ps, fz, kx, ky, s_tab, s_tabf, &sf, err);
+        const int z = cap_plane(p, ps, fz, fzf, kx, ky, s_tab, s_tabf, &sf, err);
         float2 val = make_float2(0.f, 0.f);
         if (z >= 0) {
             const float2 v = sm[t * W::STRIDE + W::pad(ky)];
-            const float Bc = cap_weight(p, sf, kx, ky);
+            const float Bc = cap_weight(p, sf, ir, kx, ky);
             val = make_float2(-Bc * v.y, Bc * v.x);
         }
         rec[o] = make_float4(val.x, val.y, __int_as_float(z), 0.f);
@@ -531,6 +541,8 @@ k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, P
     __shared__ double red[8];
     if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
     __syncthreads();
+    const double fz = s_fz;
+    const float fzf = (float)fz;
     double m2 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F * F; i += gridDim.x * blockDim.x) {
         const int kx = i % F, ky = i / F;
@@ -543,7 +555,7 @@ k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, P
             d = make_float2(r.x, r.y);
         } else {
             float sf;
-            z = cap_plane(p, ps, s_fz, kx, ky, s_tab, s_tabf, &sf, err);
+            z = cap_plane(p, ps, fz, fzf, kx, ky, s_tab, s_tabf, &sf, err);
         }
         float2 v = make_float2(0.f, 0.f);
         if (z >= 0) {
@@ -578,10 +590,12 @@ k_cap_pack(const float2* __restrict__ caps, const int2* __restrict__ posspec, Pa
     __shared__ double s_fz;
     if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
     __syncthreads();
+    const double fz = s_fz;
+    const float fzf = (float)fz;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F * F; i += gridDim.x * blockDim.x) {
         const size_t o = (size_t)a * F * F + i;
         float sf;
-        const int z = cap_plane(p, ps, s_fz, i % F, i / F, s_tab, s_tabf, &sf, err);
+        const int z = cap_plane(p, ps, fz, fzf, i % F, i / F, s_tab, s_tabf, &sf, err);
         const float2 v = z >= 0 ? caps[o] : make_float2(0.f, 0.f);
         rec[o] = make_float4(v.x, v.y, __int_as_float(z), 0.f);
     }
