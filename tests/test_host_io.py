@@ -153,3 +153,19 @@ def test_tiff_2d_topleft(tmp_path):
     (tags, data), = _read_tiff(p)
     np.testing.assert_array_equal(data, img)
     assert tags[274] == 1
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """Without a CUDA device the library refuses the work (a status, an
+    exception) instead of computing anything on the host."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    acq, _, _ = simul.workload("plain_512_born")
+    g = Geometry.from_acquisition(acq)
+    with pytest.raises(api.TdmError):
+        api.Context(g, 4)
+    holos = np.zeros((2, acq.ccd_roix, acq.ccd_roix), np.uint16)
+    out = np.full((2, 2 * acq.nxmax, 2 * acq.nxmax), np.nan, np.complex64)
+    assert api.extract_noalloc(g, holos, out, 0) < api.TDM_OK   # host buffers: refused
+    assert np.isnan(out).all()  # nothing was written
