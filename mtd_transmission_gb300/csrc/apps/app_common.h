@@ -22,7 +22,7 @@ struct Paths {
 };
 
 // "-polar" / "-etat S" / "--help" as in pretraitement_hors_axe_CPU/main.cpp:37-61
-// and Reconstruction/main.cpp:63-86.  Polarisation mode is outside this build.
+// and Reconstruction/main.cpp:63-86.  Polarisation mode is not supported.
 inline int parse_args(int argc, char** argv, const char* prog) {
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
@@ -31,7 +31,7 @@ inline int parse_args(int argc, char** argv, const char* prog) {
             return 1;
         }
         if (a == "-polar" || a == "-etat") {
-            std::fprintf(stderr, "%s: polarisation mode (-polar/-etat) is not supported by this build\n", prog);
+            std::fprintf(stderr, "%s: polarisation mode (-polar/-etat) is not supported\n", prog);
             return 2;
         }
     }

@@ -1,7 +1,7 @@
 """ctypes wrapper of the FP64 CPU oracle (``tdm_oracle.cpp``).
 
 Test infrastructure only: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker.  Parity is unpinned:
+and the CPU-baseline leg of ``bench.py``, to produce reference values.  Parity is unpinned:
 the reference cannot be built here and ships no golden vectors for this path,
 so the oracle restates the reference functions (cited file:line in the C++).
 """

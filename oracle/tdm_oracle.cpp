@@ -1,7 +1,7 @@
 // FP64 CPU oracle for the tomographic diffractive microscopy hot path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke check
-// and the CPU-baseline leg of bench.py call it to produce reference values.
+// TEST INFRASTRUCTURE ONLY.  tests/, the smoke check and the CPU-baseline leg
+// of bench.py call it to produce reference values.
 // Nothing in the product (mtd_transmission_gb300/) links, loads or calls it.
 //
 // PARITY UNPINNED.  The reference (madeba/MTD_transmission) cannot be built in
