@@ -79,7 +79,9 @@ typedef struct {
 } tdm_derived;
 
 /* Creates a context on the current CUDA device for stacks of up to
- * max_angles holograms (at most 65535: TDM_EUNSUPPORTED above).  A context is
+ * max_angles holograms (TDM_EUNSUPPORTED above 65535, or above what the cap
+ * gather's per-CTA angle list allows for the geometry: about 24,000 angles
+ * at NXMAX 128, DIM_FINAL 512; the message gives the limit).  A context is
  * used by one host thread at a time.  Replaces the FFTW plan set-up of both programs
  * (pretraitement_hors_axe_CPU/main.cpp:91-105,180-189; Reconstruction/main.cpp:131,185,318). */
 int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out);
@@ -235,8 +237,10 @@ int tdm_batch_destroy(tdm_batch* batch);
  * reference: it is for callers that cannot allocate GPU memory, such as a
  * camera acquisition loop that must not stall on cudaMalloc between bursts of
  * frames, or a host application whose memory pool already owns the device.
- * Same result as tdm_extract, without a context: holos (n*H*H uint8/uint16)
- * and spectra_out (n*F*F complex) must be device memory; the work runs on
+ * Same result as tdm_extract on a context without a reference intensity
+ * (tdm_set_reference_intensity is not applied here), without a context: holos
+ * (n*H*H uint8/uint16, 2-byte aligned when 16-bit) and spectra_out (n*F*F
+ * complex, 8-byte aligned) must be memory of the current device; the work runs on
  * `stream` (a cudaStream_t, 0 for the default stream) and the call returns
  * without waiting.  Scratch lives in a fixed 4 MiB array inside the library
  * (held by every GPU that loads it until exit): CCD_ROIX * 2*NXMAX may not
@@ -250,6 +254,17 @@ int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n
  * band): the gather writes only these and the z pass reads only these.
  * Diagnostic; no counterpart in the reference. */
 int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
+
+/* Bounded device waits (no counterpart in the reference; the reference has no
+ * device code).  The extraction's row pass stages hologram rows with bulk
+ * copies and waits for each at most `polls` polls (default and maximum 2^24;
+ * a negative value restores the default) before it records an error; the
+ * call's tdm_synchronize then returns TDM_ECUDA ("a bulk copy of hologram rows
+ * did not complete").  After that first bound the warp still waits, up to the
+ * default bound, for its copy, so no copy is left in flight.  0 makes every
+ * first wait give up at once, which tests the error path without a fault.
+ * Waits for the context's queued work first. */
+int tdm_set_wait_limit(tdm_ctx* ctx, long long polls);
 
 /* Schedule of the per-angle stages (no counterpart in the reference): tdm_pipeline
  * streams the angles in chunks of `chunk` and keeps `lanes` consecutive chunks in

@@ -29,7 +29,7 @@ EXPORTS = (
     "tdm_pgm_info", "tdm_write_tiff_f32", "tdm_profile", "tdm_profile_count", "tdm_profile_read",
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
     "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
-    "tdm_join", "tdm_set_schedule", "tdm_set_reference_intensity",
+    "tdm_join", "tdm_set_schedule", "tdm_set_reference_intensity", "tdm_set_wait_limit",
 )
 
 
@@ -108,6 +108,7 @@ def lib():
     L.tdm_batch_launch.argtypes = [P, P]
     L.tdm_autotune.argtypes = [P, P, I, I, ctypes.POINTER(I)]
     L.tdm_set_schedule.argtypes = [P, I, I]
+    L.tdm_set_wait_limit.argtypes = [P, ctypes.c_longlong]
     L.tdm_set_reference_intensity.argtypes = [P, P]
     L.tdm_join.argtypes = [P]
     L.tdm_batch_destroy.argtypes = [P]
@@ -311,6 +312,10 @@ class Context:
         """tdm_set_schedule: angles per chunk and chunks in flight of the per-angle stages."""
         self._check(lib().tdm_set_schedule(self._h, chunk, lanes), "tdm_set_schedule")
 
+    def set_wait_limit(self, polls: int):
+        """tdm_set_wait_limit: polls of the extraction's first bounded wait on each bulk copy (-1: default)."""
+        self._check(lib().tdm_set_wait_limit(self._h, polls), "tdm_set_wait_limit")
+
     def autotune(self, holos, n=None) -> int:
         """tdm_autotune: picks the fastest schedule (chunk, lanes) on this stack; returns its chunk."""
         n = holos.shape[0] if n is None else n
@@ -338,8 +343,31 @@ def extract_noalloc(geom: Geometry, holos, spectra_out, stream: int = 0, n=None)
 
     For callers that cannot allocate GPU memory (an acquisition loop that must
     not stall on cudaMalloc, or an application whose memory pool owns the
-    device).  Returns the TDM status; the work is queued on `stream`."""
+    device).  Returns the TDM status; the work is queued on `stream`.
+
+    The library cannot see buffer sizes, so the arrays are checked here:
+    holos a contiguous CUDA tensor of at least n uint8/uint16 H x H images,
+    spectra_out a contiguous CUDA tensor holding at least n F x F complex
+    values (complex64, or float32 with a trailing 2)."""
+    import torch
+    H, F = geom.ccd_roix, 2 * geom.nxmax
     n = holos.shape[0] if n is None else n
+    for name, t in (("holos", holos), ("spectra_out", spectra_out)):
+        if not isinstance(t, torch.Tensor) or not t.is_cuda or not t.is_contiguous():
+            raise ValueError(f"extract_noalloc: {name} must be a contiguous CUDA tensor")
+    if holos.dtype not in (torch.uint8, torch.uint16, torch.int16) or tuple(holos.shape[1:]) != (H, H):
+        raise ValueError(f"extract_noalloc: holos must be (n, {H}, {H}) uint8 or uint16")
+    if not 0 < n <= holos.shape[0]:
+        raise ValueError(f"extract_noalloc: n={n} outside [1, {holos.shape[0]}]")
+    if spectra_out.device != holos.device:
+        raise ValueError("extract_noalloc: holos and spectra_out must be on the same device")
+    if spectra_out.dtype == torch.complex64:
+        ok = spectra_out.dim() == 3 and tuple(spectra_out.shape[1:]) == (F, F)
+    else:
+        ok = (spectra_out.dtype == torch.float32 and spectra_out.dim() == 4
+              and tuple(spectra_out.shape[1:]) == (F, F, 2))
+    if not ok or spectra_out.shape[0] < n:
+        raise ValueError(f"extract_noalloc: spectra_out must hold at least n={n} complex64 ({F}, {F}) spectra")
     return int(lib().tdm_extract_noalloc(ctypes.byref(geom), ptr(holos), Context._bits(holos), n, ptr(spectra_out),
                                          ctypes.c_void_p(stream)))
 

@@ -42,13 +42,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// Waits for the phase with the given parity to complete, for a bounded number
-// of polls (each try_wait itself suspends for a while).  Returns false when
-// the bound was reached; the caller records an error and must not reuse the
+// Waits for the phase with the given parity to complete, for at most `polls`
+// polls (each try_wait itself suspends for a while).  Returns false when the
+// bound was reached; the caller records an error and must not reuse the
 // destination, which an overdue copy may still write.
 constexpr uint32_t kMbarPolls = 1u << 24;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kMbarPolls; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t polls = kMbarPolls) {
+    for (uint32_t i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -48,13 +48,15 @@ struct ExtractCfg {
 // reference amplitude, applied to every pixel first (main.cpp:147).  BULK: each warp's 2G rows (its G row pairs, consecutive in
 // memory) are staged in shared memory by one bulk copy and read from there;
 // requires a 16-byte aligned stack.  Otherwise the lanes load the pixels
-// directly.  A bulk copy that does not complete within the poll bound sets
-// bit 1 of *err (the call then fails).
+// directly.  A bulk copy that does not complete within wait_polls polls sets
+// bit 1 of *err (the call then fails); the warp then waits for its copy again,
+// up to the full bound kMbarPolls, so that no copy is left in flight into the
+// shared memory of a finished CTA.
 template <int H, bool BULK>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT, ExtractCfg<H>::ROWS_CTAS)
 k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk, int2 flat,
                const float* __restrict__ ref_inv, const float2* __restrict__ tw, float2* __restrict__ inter, int F,
-               int x0, int* __restrict__ err) {
+               int x0, int* __restrict__ err, uint32_t wait_polls) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, P = Cf::P;
@@ -115,7 +117,7 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
             bulk_g2s(stage, static_cast<const char*>(holos) + ((size_t)a * H * H + y0w * H) * bpp, bytes, &bar[w]);
         }
         __syncwarp();
-        if (!mbar_wait(&bar[w], 0)) {
+        if (!mbar_wait(&bar[w], 0, wait_polls)) {
             if ((threadIdx.x & 31) == 0) atomicOr(err, 2);
             mbar_wait(&bar[w], 0);
         }
@@ -159,7 +161,7 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
 template <int H>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT)
 k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, float2* __restrict__ spectra,
-               int F, int x0, int y0, float2* __restrict__ argpart) {
+               int F, int x0, int y0, float4* __restrict__ argpart) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
     constexpr int T = W::T, E = W::E, C = Cf::C, TC = C + 1;
@@ -182,19 +184,19 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     __syncwarp();
     const float inv = 1.0f / ((float)H * (float)H);
     const int kx = x0 + c;
-    float best = -1.0f;
+    float best = -1.0f, second = -1.0f;
     int bi = 0x7fffffff;
     for (int r = j; r < F; r += T) {
         const int ky = y0 + r;
         const float sg = ((kx + ky) & 1) ? -inv : inv;
         const float2 z = c_scale(s[W::pad(ky)], sg);
         tile[r * TC + tr] = z;
-        if (argpart) argmax_take(best, bi, z, r * F + c);
+        if (argpart) argmax_take(best, bi, second, z, r * F + c);
     }
     if (argpart) {  // this warp's partial winner of the specular search (8 records per CTA)
-        argmax_warp(best, bi);
+        argmax_warp(best, bi, second);
         if ((threadIdx.x & 31) == 0)
-            argpart[((size_t)a * gridDim.x + blockIdx.x) * 8 + (threadIdx.x >> 5)] = make_float2(best, __int_as_float(bi));
+            argpart[((size_t)a * gridDim.x + blockIdx.x) * 8 + (threadIdx.x >> 5)] = argmax_record(best, bi, second);
     }
     __syncthreads();
     float2* dst = spectra + (size_t)a * F * F + c0;

@@ -42,7 +42,7 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
             rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->tuk_h_flat,
                                                                 c->use_ref ? c->b.ref_inv : nullptr, c->b.tw,
                                                                 c->b.inter, p.F,
-                                                                p.x0, c->b.err);
+                                                                p.x0, c->b.err, c->wait_polls);
         }
         {
             Launch l(c, K_EXTRACT_COLS);

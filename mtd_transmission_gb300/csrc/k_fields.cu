@@ -48,15 +48,15 @@ __device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F 
 // the spectra come straight from the holograms), then argmax_final in
 // k_field_rows, the first consumer.
 __global__ void __launch_bounds__(256) k_argmax_part(const float2* __restrict__ spectra, int F,
-                                                     float2* __restrict__ part) {
+                                                     float4* __restrict__ part) {
     const int a = blockIdx.y, sl = blockIdx.x;
     const int per = F * F / kArgSlices, i0 = sl * per;
     const float2* s = spectra + (size_t)a * F * F;
-    float best = -1.0f;
+    float best = -1.0f, second = -1.0f;
     int bi = 0x7fffffff;
-    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) argmax_take(best, bi, s[i], i);
-    argmax_block(best, bi);
-    if (threadIdx.x == 0) part[(size_t)a * kArgSlices + sl] = make_float2(best, __int_as_float(bi));
+    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) argmax_take(best, bi, second, s[i], i);
+    argmax_block(best, bi, second);
+    if (threadIdx.x == 0) part[(size_t)a * kArgSlices + sl] = argmax_record(best, bi, second);
 }
 
 // ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
@@ -74,7 +74,7 @@ struct FieldCfg {
 
 template <int F>
 __global__ void __launch_bounds__(FieldCfg<F>::NT)
-k_field_rows(const float2* __restrict__ spectra, const float2* __restrict__ argpart, int nparts,
+k_field_rows(const float2* __restrict__ spectra, const float4* __restrict__ argpart, int nparts,
              int2* __restrict__ posspec, float2* __restrict__ specval, int normalize, const float2* __restrict__ tw,
              float2* __restrict__ I1) {
     using C = FieldCfg<F>;
@@ -83,9 +83,9 @@ k_field_rows(const float2* __restrict__ spectra, const float2* __restrict__ argp
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
-    const int bi = argmax_final(argpart + (size_t)a * nparts, nparts);
-    const int2 p = make_int2(bi % F, bi / F);
     const float2* spec = spectra + (size_t)a * F * F;
+    const int bi = argmax_final(argpart + (size_t)a * nparts, nparts, spec, F * F);
+    const int2 p = make_int2(bi % F, bi / F);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         posspec[a] = p;
         specval[a] = spec[bi];

@@ -217,12 +217,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 // the integer pipe (fp_bits.cuh), so the FP64 pipe only adds.
 constexpr int kGW = 8;  // warps per CTA
 
-// Dynamic shared memory of k_accumulate: per warp the band's sums, counts and
-// owners plus a 32-lane staging row, and the CTA's list of n angles at most.
-size_t gather_smem(int band, int n) {
-    return (size_t)kGW * band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 7) & ~7) + (size_t)n * sizeof(int2);
-}
+size_t gather_smem(int band, int n) { return gather_smem_bytes(band, n); }
 
 template <int D>
 __global__ void __launch_bounds__(kGW * 32)
@@ -696,7 +691,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     const Params& p = c->p;
     const size_t sm_a = gather_smem(p.band, n);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
-    if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
+    if (sm_a > kMaxSmemPerCta) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
@@ -801,7 +796,7 @@ int adjoint_impl(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bo
     const Params& p = c->p;
     const size_t sm_a = gather_smem(p.band, n);
     const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
-    if (sm_a > 227 * 1024) return TDM_EUNSUPPORTED;
+    if (sm_a > kMaxSmemPerCta) return TDM_EUNSUPPORTED;
     if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
@@ -827,6 +822,13 @@ int adjoint_impl(tdm_ctx* c, const float4* recs, int n, float* xn, float* xk, bo
 }
 
 }  // namespace
+
+// Dynamic shared memory of k_accumulate: per warp the band's sums, counts and
+// owners plus a 32-lane staging row, and the CTA's list of n angles at most.
+size_t gather_smem_bytes(int band, int n) {
+    return (size_t)kGW * band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
+           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 7) & ~7) + (size_t)n * sizeof(int2);
+}
 
 int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
     switch (c->p.F) {

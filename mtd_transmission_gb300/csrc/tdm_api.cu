@@ -6,6 +6,7 @@
 #include <limits>
 #include <vector>
 
+#include "bulk_copy.cuh"
 #include "host_tables.h"
 #include "tdm_internal.cuh"
 
@@ -283,6 +284,15 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     if (p.zmin < 0 || p.zmin + p.band > D) {
         delete c;
         fprintf(stderr, "tdm_create: Ewald caps exceed the DIM_FINAL volume along z\n");
+        return TDM_EUNSUPPORTED;
+    }
+    if (gather_smem_bytes(p.band, max_angles) > kMaxSmemPerCta) {
+        // the gather keeps each CTA's list of angles in shared memory
+        int most = 0;
+        while (gather_smem_bytes(p.band, most + 1) <= kMaxSmemPerCta) ++most;
+        delete c;
+        fprintf(stderr, "tdm_create: at most %d angles for this geometry (the cap gather's angle list of a "
+                        "%d-plane cap band must fit one CTA's shared memory)\n", most, p.band);
         return TDM_EUNSUPPORTED;
     }
     // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:885-902): k0 is a float
@@ -736,7 +746,9 @@ int tdm_reconstruct(tdm_ctx* c, const float* fields_in, const int32_t* posspec_i
 // Scratch of the per-angle stages (the buffers sized chunk_cap angles) seen
 // from chunk slot s on: the slots [s, s + chunk) of each.
 struct ChunkScratch {
-    float2 *inter, *argpart, *I1, *zph, *qc, *tq, *r1;
+    float2* inter;
+    float4* argpart;
+    float2 *I1, *zph, *qc, *tq, *r1;
     float *phase, *amp, *gx, *unwrapped, *fit_part;
     double* beta;
     unsigned* fit_done;
@@ -1092,6 +1104,14 @@ int tdm_batch_destroy(tdm_batch* b) {
 }
 
 // ---------------------------------------------------------------- autotuning
+int tdm_set_wait_limit(tdm_ctx* c, long long polls) {
+    if (!c || polls > (long long)kMbarPolls) return fail(c, TDM_EINVAL, "tdm_set_wait_limit: at most 2^24 polls");
+    cudaSetDevice(c->device);
+    if (int rc = tdm_synchronize(c)) return rc;  // queued extractions keep the bound they were launched with
+    c->wait_polls = polls < 0 ? kMbarPolls : (uint32_t)polls;
+    return TDM_OK;
+}
+
 int tdm_set_schedule(tdm_ctx* c, int chunk, int lanes) {
     if (!c || chunk < 1 || lanes < 1 || lanes > kMaxLanes || chunk * lanes > c->chunk_cap)
         return fail(c, TDM_EINVAL, "tdm_set_schedule: need 1 <= lanes <= 8 and chunk * lanes <= the chunk capacity");

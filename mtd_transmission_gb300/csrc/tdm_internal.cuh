@@ -46,7 +46,7 @@ struct Buffers {
     float2* spectra = nullptr;     // max_angles x F*F
     int2* posspec = nullptr;       // max_angles
     float2* specval = nullptr;     // max_angles
-    float2* argpart = nullptr;     // chunk x kArgPartsMax partial winners of the specular search
+    float4* argpart = nullptr;     // chunk x kArgPartsMax partial winners of the specular search
     float2* I1 = nullptr;          // chunk x F*F
     float* phase = nullptr;        // chunk x F*F
     float* amp = nullptr;          // chunk x F*F
@@ -107,6 +107,7 @@ struct tdm_ctx {
     int nsamp = 0;
     int device = 0;
     int2 tuk_h_flat{0, -1}, tuk_f_flat{0, -1};  // where the hologram / field windows are exactly 1
+    uint32_t wait_polls = 1u << 24;  // polls of a bulk copy's first wait in the extraction (tdm_set_wait_limit)
     bool use_ref = false;        // holograms divided by the reference amplitude (b.ref_inv)
     int n_fields = 0;            // angles held in b.fields / b.posspec
     int n_spectra = 0;           // angles held in b.spectra
@@ -144,6 +145,10 @@ struct tdm_ctx {
 
 // Kernel launchers (defined in the kernel translation units).
 namespace tdm {
+// Dynamic shared memory of the cap gather for a cap band of `band` planes and
+// n angles (the CTA keeps its list of angles in shared memory).
+size_t gather_smem_bytes(int band, int n);
+constexpr size_t kMaxSmemPerCta = 227 * 1024;
 // Scope around one kernel launch on c->stream: counts the launch and, when
 // profiling is on, brackets it with a pair of CUDA events.
 cudaEvent_t prof_event(tdm_ctx* c);

@@ -9,6 +9,7 @@
 // scratch (the row-pass intermediate) in a fixed array compiled into this
 // library.  Every GPU that loads the library holds that array until the
 // process exits.
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -61,8 +62,12 @@ int device_symbols(int dev, Symbols& out) {
             const std::vector<double> t = tukey_factor(H, 0.05f);  // hologram window, main.cpp:105
             for (int i = 0; i < H; ++i) tk[tukey_offset(H) + i] = (float)t[i];
         }
+        // A copy from pageable host memory may return before the data has
+        // reached the device; the tables must be complete before any kernel
+        // on any stream (or another thread that sees ready) reads them.
         if (cudaMemcpy(s.twiddle, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(s.tukey, tk.data(), kTukeyLen * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaMemcpy(s.tukey, tk.data(), kTukeyLen * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaDeviceSynchronize() != cudaSuccess) {
             cudaGetLastError();
             return TDM_ECUDA;
         }
@@ -72,13 +77,14 @@ int device_symbols(int dev, Symbols& out) {
     return TDM_OK;
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory of device dev.
+bool on_device(const void* p, int dev) {
     cudaPointerAttributes at;
     if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
 }
 
 template <int H>
@@ -100,7 +106,7 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
         k_extract_rows<H, false><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
             static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), tukey_flat(H, 0.05f),
             nullptr, s.twiddle, s.scratch, F,
-            x0, nullptr);
+            x0, nullptr, 0u);
         k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
             s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0, nullptr);
     }
@@ -129,12 +135,17 @@ extern "C" int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int 
                      H, H, (size_t)H * F * sizeof(float2), kScratchBytes);
         return TDM_EUNSUPPORTED;
     }
-    if (!on_device(holos) || !on_device(spectra_out)) {
-        std::fprintf(stderr, "tdm_extract_noalloc: holograms and spectra must be in device memory\n");
-        return TDM_EINVAL;
-    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return TDM_ECUDA;
+    if (!on_device(holos, dev) || !on_device(spectra_out, dev)) {
+        std::fprintf(stderr, "tdm_extract_noalloc: holograms and spectra must be in the current device's memory\n");
+        return TDM_EINVAL;
+    }
+    // the kernels store complex values as float2 and read 16-bit samples as uint16
+    if ((reinterpret_cast<uintptr_t>(spectra_out) & 7) || (bits == 16 && (reinterpret_cast<uintptr_t>(holos) & 1))) {
+        std::fprintf(stderr, "tdm_extract_noalloc: spectra must be 8-byte aligned and 16-bit holograms 2-byte aligned\n");
+        return TDM_EINVAL;
+    }
     Symbols s;
     if (int rc = device_symbols(dev, s)) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -162,3 +162,79 @@ def test_tv_reconstruction_beats_single_pass_and_resumes():
     assert rep["misfit_last"] < rep["misfit_first"]
     assert full.min() >= 0.0 and full.max() <= 0.05
     np.testing.assert_array_equal(half, full)
+
+
+def geometry_stated(M=400):
+    """The regularised-reconstruction workload at its stated size: a 256^3
+    index volume and 400 Ewald caps of 128^2 (NXMAX 64), specular positions
+    on the Fermat spiral out to 0.9 NXMAX."""
+    acq, _, _ = simul.workload("plain_512_born")
+    acq = replace(acq, nb_holo=M)
+    N = acq.nxmax
+    t = simul.spiral_tilts(M, N)
+    pos = np.concatenate([N + t[:, 0], N + t[:, 1]]).astype(np.int32)
+    return acq, pos
+
+
+def test_operator_pair_at_stated_size():
+    """256^3 -> 400 caps of 128^2: forward and adjoint against the FP64
+    oracle, the dot-product test, and central differences with eps = 1e-3 on
+    32 random voxels against A^H (A x - y)."""
+    import torch
+    acq, pos = geometry_stated()
+    cfg = oracle_cfg(acq)
+    D, F, M = acq.dim_final, 2 * acq.nxmax, acq.nb_holo
+    assert (D, F, M) == (256, 128, 400)
+    rng = np.random.default_rng(12)
+    xn = rng.standard_normal((D, D, D)).astype(np.float32)
+    xk = rng.standard_normal((D, D, D)).astype(np.float32)
+    y = (rng.standard_normal((M, F, F)) + 1j * rng.standard_normal((M, F, F))).astype(np.complex64)
+    with Context(Geometry.from_acquisition(acq), M) as ctx:
+        caps = ctx.forward(xn, xk, n=M, posspec=pos)
+        an, ak = ctx.adjoint(y, n=M, posspec=pos, absorption_out=np.zeros((D, D, D), np.float32))
+        ref_f = oracle.forward_caps(xn.astype(np.float64), xk.astype(np.float64), pos.astype(np.float64), cfg)
+        assert np.array_equal(caps != 0, ref_f != 0)
+        assert rel_l2(caps, ref_f) <= TOL
+        del ref_f
+        ref_a = oracle.adjoint_caps(y.astype(np.complex128), pos.astype(np.float64), cfg)
+        assert rel_l2(an, ref_a.real) <= TOL
+        assert rel_l2(ak, ref_a.imag) <= TOL
+        del ref_a
+        lhs = np.vdot(y.astype(np.complex128), caps.astype(np.complex128))
+        rhs = np.vdot((an + 1j * ak).astype(np.complex128), xn + 1j * xk.astype(np.float64))
+        assert abs(lhs - rhs) / abs(lhs) <= TOL
+        # finite differences on device buffers (f in FP64 from the FP32 caps)
+        p = torch.from_numpy(pos).cuda()
+        x0 = torch.zeros((D, D, D), device="cuda")
+        xt = torch.zeros_like(x0)
+        for v in (x0, xt):
+            idx = torch.from_numpy(rng.integers(0, D, (64, 3))).cuda()
+            v[idx[:, 0], idx[:, 1], idx[:, 2]] = torch.from_numpy(0.02 * rng.standard_normal(64)).float().cuda()
+        out = torch.empty((M, F, F), dtype=torch.complex64, device="cuda")
+
+        def fwd(x):
+            ctx.forward(x, None, n=M, posspec=p, caps_out=out)
+            ctx.synchronize()
+            return out.to(torch.complex128)
+
+        yt = fwd(xt)
+
+        def f(x):
+            r = fwd(x) - yt
+            return 0.5 * float(torch.vdot(r.flatten(), r.flatten()).real)
+
+        r0 = (fwd(x0) - yt).to(torch.complex64).contiguous()
+        g = torch.empty_like(x0)
+        ctx.adjoint(r0, n=M, posspec=p, index_out=g)
+        ctx.synchronize()
+        eps = 1e-3
+        fd, ga = [], []
+        for v in rng.integers(0, D, (32, 3)):
+            v = tuple(int(c) for c in v)
+            xp, xm = x0.clone(), x0.clone()
+            xp[v] += eps
+            xm[v] -= eps
+            fd.append((f(xp) - f(xm)) / (2 * eps))
+            ga.append(float(g[v]))
+    fd, ga = np.array(fd), np.array(ga)
+    assert np.abs(fd - ga).max() <= 1e-3 * np.abs(ga).max()

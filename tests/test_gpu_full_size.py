@@ -3,15 +3,16 @@
 rytov_1024: 600 x 1024^2 uint16 holograms, 256^2 fields, 512^3 volume.
 large_2048: 1000 x 2048^2 uint16 holograms, 512^2 fields, 1024^3 volume.
 
-Per stage against the FP64 oracle on sampled angles: extraction, specular
-positions, fields.  Over the whole stack, size-independent properties: the
-pipeline's volume equals the one of the separate entry points and does not
-depend on the schedule or on repetition (bit for bit), hit counts match the
-reference's cap-cell arithmetic (exact on sampled planes, exact in total),
-and the OTF marks hit cells only.  The volume stage against the oracle at
-512^3 (from the GPU's own fields), and, at 1024^3 where an FP64 volume does
-not fit a test's host memory, by the dot-product test of the forward
-operator and its adjoint over all 1000 caps.
+Against the FP64 oracle on every angle: specular positions (from the
+holograms; bit for bit) and hit counts (the whole volume, from the oracle's
+positions).  At 512^3 also every angle's spectrum and field, the volume
+stage from the GPU's fields and the end-to-end volume against the oracle's
+own; at 1024^3, where an FP64 volume does not fit a test's host memory,
+spectra and fields on sampled angles and the dot-product test of the
+forward operator and its adjoint over all 1000 caps.  Size-independent
+properties over the whole stack: the pipeline's volume equals the one of the
+separate entry points and does not depend on the schedule or on repetition
+(bit for bit), and the OTF marks hit cells only.
 """
 from __future__ import annotations
 
@@ -26,6 +27,22 @@ from tests.helpers import c64, oracle_cfg, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
+
+
+def _oracle_positions(holos, cfg, F, keep_spectra, batch=25):
+    """The oracle's extraction (holo2TF_UBorn) and specular search (coordSpec)
+    on every hologram of a device stack, in host-memory batches; returns the
+    spectra (when kept) and the positions as x values then y values."""
+    M = holos.shape[0]
+    specs, idx = [], []
+    for a0 in range(0, M, batch):
+        s = oracle.extract_stack(holos[a0:a0 + batch].cpu().numpy().astype(np.float64), cfg)
+        idx += [oracle.coord_spec(x) for x in s]
+        if keep_spectra:
+            specs.append(s)
+    idx = np.asarray(idx, np.int64)
+    pos = np.concatenate([idx % F, idx // F]).astype(np.int32)
+    return (np.concatenate(specs) if keep_spectra else None), pos
 
 
 def _run(name):
@@ -43,11 +60,21 @@ def _run(name):
     M, D, F = acq.nb_holo, acq.dim_final, 2 * acq.nxmax
     cfg = oracle_cfg(acq)
     oracle.set_threads(os.cpu_count() or 1)
+    # every angle through the oracle's extraction and specular search; at
+    # 512^3 also its fields (all angles), the basis of the end-to-end volume
+    full = D <= 512
+    ref_spec_all, ref_pos_all = _oracle_positions(holos, cfg, F, keep_spectra=full)
     sample = [0, M // 2, M - 1]
-    h_sample = np.stack([holos[a].cpu().numpy() for a in sample])
-    ref_spec = oracle.extract_stack(h_sample.astype(np.float64), cfg)
-    ref_fields, ref_pos = oracle.fields(ref_spec, cfg, mask)
-    out = {"acq": acq, "cfg": cfg, "M": M, "D": D, "F": F}
+    if full:
+        ref_fields_all, ref_pos_f = oracle.fields(ref_spec_all, cfg, mask)
+        assert np.array_equal(ref_pos_f.astype(np.int32), ref_pos_all)
+        ref_spec, ref_fields = ref_spec_all[sample], ref_fields_all[sample]
+    else:
+        h_sample = np.stack([holos[a].cpu().numpy() for a in sample])
+        ref_spec = oracle.extract_stack(h_sample.astype(np.float64), cfg)
+        ref_fields, _ = oracle.fields(ref_spec, cfg, mask)
+    ref_pos = ref_pos_all.reshape(2, M)[:, sample].ravel()
+    out = {"acq": acq, "cfg": cfg, "M": M, "D": D, "F": F, "ref_pos_all": ref_pos_all}
     with Context(Geometry.from_acquisition(acq), M) as ctx:
         ctx.set_mask(mask)
         vol = lambda dt: torch.empty((D, D, D), dtype=dt, device="cuda")  # noqa: E731
@@ -73,17 +100,22 @@ def _run(name):
         ctx.synchronize()
         out["same_as_stages"] = bool(np.array_equal(pos, pos2) and torch.equal(re, re3) and torch.equal(im, im3))
         del re2, im2, re3, im3
-        # stage errors on the sampled angles
-        out["spec_err"] = [rel_l2(spec[a].cpu().numpy(), ref_spec[i]) for i, a in enumerate(sample)]
-        fo = np.zeros((len(sample), F, F), np.complex64)
-        po = np.zeros(2 * len(sample), np.int32)
-        ctx.fields(c64(ref_spec), fields_out=fo, posspec_out=po)
-        out["pos_sample"] = (pos.reshape(2, M)[:, sample], ref_pos.reshape(2, -1).astype(np.int32))
-        out["pos_from_ref_spec"] = (po, ref_pos.astype(np.int32))
-        out["field_err"] = [rel_l2(fo[i], ref_fields[i]) for i in range(len(sample))]
+        # stage errors: extraction and fields (from the oracle's spectra) on
+        # every angle at 512^3, on the sampled angles at 1024^3
+        angles = range(M) if full else sample
+        refs = ref_spec_all if full else ref_spec
+        out["spec_err"] = [rel_l2(spec[a].cpu().numpy(), refs[i]) for i, a in enumerate(angles)]
+        src = ref_spec_all if full else ref_spec
+        fo = np.zeros(src.shape, np.complex64)
+        po = np.zeros(2 * src.shape[0], np.int32)
+        ctx.fields(c64(src), fields_out=fo, posspec_out=po)
+        out["pos_from_ref_spec"] = (po, ref_pos_all if full else ref_pos)
+        ref_f = ref_fields_all if full else ref_fields
+        out["field_err"] = [rel_l2(fo[i], ref_f[i]) for i in range(src.shape[0])]
         out.update(pos=pos, fields=fields, re=re, im=im, otf=otf, cnt=cnt, ctx_geom=Geometry.from_acquisition(acq))
-        if D <= 512:
+        if full:
             out["fields_host"] = fields.cpu().numpy()
+            out["ref_fields_all"] = ref_fields_all
         else:
             out["dot"] = _dot_product(ctx, M, D, F, pos)
     return out
@@ -108,25 +140,25 @@ def _dot_product(ctx, M, D, F, pos):
 
 
 def _counts_check(out):
-    """Hit counts against the reference's cap-cell arithmetic: the total, and every cell of 4 planes."""
+    """Hit counts against the reference's cap-cell arithmetic applied to the
+    oracle's specular positions of every angle: the whole volume, slab by
+    slab; and the OTF marks hit cells only."""
     import torch
     cfg, M, D = out["cfg"], out["M"], out["D"]
-    cells = oracle.cap_cells(out["pos"].astype(np.float64), cfg)
-    total = sum(c[1].size for c in cells if c is not None)
+    cells = oracle.cap_cells(out["ref_pos_all"].astype(np.float64), cfg)
+    flat = np.concatenate([(c[1].astype(np.int64) * D + c[2]) * D + c[3] for c in cells if c is not None])
     cnt = out["cnt"]
-    assert int(cnt.sum(dtype=torch.int64).item()) == total
-    zlo = min(int(c[1].min()) for c in cells if c is not None)
-    zhi = max(int(c[1].max()) for c in cells if c is not None)
-    zs = [zlo, zlo + 1, D // 2, zhi - 1, zhi]
-    for z in zs:
-        ref = np.zeros(D * D, np.int64)
-        for c in cells:
-            if c is None:
-                continue
-            on = c[1] == z
-            np.add.at(ref, c[2][on] * D + c[3][on], 1)
-        got = cnt[z].cpu().numpy().astype(np.int64).ravel()
-        assert np.array_equal(got, ref), z
+    assert int(cnt.sum(dtype=torch.int64).item()) == flat.size
+    plane = D * D
+    zlo, zhi = int(flat.min() // plane), int(flat.max() // plane)
+    assert not bool(cnt[:zlo].any()) and not bool(cnt[zhi + 1:].any())
+    step = max(1, (1 << 26) // plane)
+    for z0 in range(zlo, zhi + 1, step):
+        z1 = min(z0 + step, zhi + 1)
+        sel = flat[(flat >= z0 * plane) & (flat < z1 * plane)] - z0 * plane
+        ref = np.bincount(sel, minlength=(z1 - z0) * plane)
+        got = cnt[z0:z1].cpu().numpy().astype(np.int64).ravel()
+        assert np.array_equal(got, ref), (z0, z1)
     hit = cnt > 0
     otf = out["otf"] != 0
     assert not bool((otf & ~hit).any())          # the OTF marks hit cells only
@@ -136,31 +168,41 @@ def _counts_check(out):
 def _stage_checks(out):
     assert out["same_schedule"]
     assert out["same_as_stages"]
-    assert max(out["spec_err"]) <= TOL, out["spec_err"]
-    got, ref = out["pos_sample"]
-    np.testing.assert_array_equal(got, ref)
+    assert max(out["spec_err"]) <= TOL, max(out["spec_err"])
+    # specular positions of every angle, from the holograms, equal the oracle's
+    np.testing.assert_array_equal(out["pos"], out["ref_pos_all"])
     got, ref = out["pos_from_ref_spec"]
     np.testing.assert_array_equal(got, ref)
-    assert max(out["field_err"]) <= TOL, out["field_err"]
+    assert max(out["field_err"]) <= TOL, max(out["field_err"])
     _counts_check(out)
 
 
 def test_full_size_rytov_1024():
-    """600 x 1024^2 -> 512^3, plus the volume stage against the FP64 oracle
-    from the GPU's fields of all 600 angles."""
+    """600 x 1024^2 -> 512^3: every angle's specular position, spectrum and
+    field against the oracle; the volume stage from the GPU's fields; and the
+    end-to-end volume (holograms to volume) against the oracle's own, with
+    its hit counts."""
     out = _run("rytov_1024")
     _stage_checks(out)
-    ref = oracle.reconstruction(out["fields_host"], out["pos"].astype(np.float64), out["cfg"], want_otf=False)
-    D = out["D"]
-    np.testing.assert_array_equal(out["cnt"].cpu().numpy().astype(np.int64),
-                                  ref["counts"].astype(np.int64).reshape(D, D, D))
+    cfg, D = out["cfg"], out["D"]
+    pos = out["ref_pos_all"].astype(np.float64)
+    ref = oracle.reconstruction(out["fields_host"], pos, cfg, want_otf=False, want_counts=False)
     assert rel_l2(out["re"].cpu().numpy(), ref["indice"].real) <= TOL
     assert rel_l2(out["im"].cpu().numpy(), ref["indice"].imag) <= TOL
+    del ref
+    e2e = oracle.reconstruction(out["ref_fields_all"], pos, cfg, want_otf=False)
+    np.testing.assert_array_equal(out["cnt"].cpu().numpy().astype(np.int64),
+                                  e2e["counts"].astype(np.int64).reshape(D, D, D))
+    assert rel_l2(out["re"].cpu().numpy(), e2e["indice"].real) <= TOL
+    assert rel_l2(out["im"].cpu().numpy(), e2e["indice"].imag) <= TOL
 
 
 def test_full_size_large_2048():
-    """1000 x 2048^2 -> 1024^3 (an 8 GB spectrum), plus the dot-product test
-    of the forward operator and its adjoint at that size."""
+    """1000 x 2048^2 -> 1024^3 (an 8 GB spectrum): every angle's specular
+    position against the oracle's and the whole count volume against the
+    reference's cap-cell arithmetic on those positions; spectra and fields on
+    sampled angles; the dot-product test of the forward operator and its
+    adjoint at that size."""
     out = _run("large_2048")
     _stage_checks(out)
     assert out["dot"] <= 1e-5, out["dot"]

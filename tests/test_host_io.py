@@ -7,6 +7,8 @@ float32 multi-page TIFF writer.
 """
 from __future__ import annotations
 
+import ctypes
+
 import os
 import re
 import struct
@@ -167,5 +169,34 @@ def test_no_cpu_fallback_without_a_gpu():
         api.Context(g, 4)
     holos = np.zeros((2, acq.ccd_roix, acq.ccd_roix), np.uint16)
     out = np.full((2, 2 * acq.nxmax, 2 * acq.nxmax), np.nan, np.complex64)
-    assert api.extract_noalloc(g, holos, out, 0) < api.TDM_OK   # host buffers: refused
+    # host buffers: the C ABI itself refuses them (the Python wrapper refuses before the call)
+    assert api.lib().tdm_extract_noalloc(ctypes.byref(g), api.ptr(holos), 16, 2, api.ptr(out), None) < api.TDM_OK
     assert np.isnan(out).all()  # nothing was written
+    with pytest.raises(ValueError):
+        api.extract_noalloc(g, holos, out, 0)
+
+
+def test_noalloc_wrapper_checks_buffers():
+    """The Python wrapper of the allocation-free extraction checks what the C
+    ABI cannot see (buffer sizes, dtypes, devices) before calling it."""
+    import torch
+    acq, _, _ = simul.workload("plain_512_born")
+    g = Geometry.from_acquisition(acq)
+    H, F = acq.ccd_roix, 2 * acq.nxmax
+    holos = torch.zeros((2, H, H), dtype=torch.uint16)
+    out = torch.zeros((2, F, F), dtype=torch.complex64)
+    with pytest.raises(ValueError, match="CUDA"):
+        api.extract_noalloc(g, holos, out)
+    with pytest.raises(ValueError):
+        api.extract_noalloc(g, np.zeros((2, H, H), np.uint16), out)
+
+
+def test_gather_angle_limit_refused_at_create():
+    """The cap gather keeps each CTA's list of angles in shared memory: a
+    context whose angle count cannot fit is refused at creation (before any
+    device work), with the limit in the message, instead of failing later."""
+    acq, _, _ = simul.workload("rytov_1024")
+    g = Geometry.from_acquisition(acq)
+    with pytest.raises(api.TdmError) as e:
+        api.Context(g, 40000)
+    assert e.value.status == api.STATUS_CODES["TDM_EUNSUPPORTED"]

@@ -11,6 +11,8 @@ collected last so that a failure here does not hide the other tests.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -57,14 +59,29 @@ def test_noalloc_extract_matches_context_twice():
             assert rel_l2(c_o, c_r) <= TOL, a
 
 
+def _raw(geom, holos_ptr, n, out_ptr):
+    """The C entry point itself, without the Python wrapper's buffer checks."""
+    return api.lib().tdm_extract_noalloc(ctypes.byref(geom), holos_ptr, 16, n, out_ptr, None)
+
+
 def test_noalloc_extract_rejections():
     import torch
     acq, holos = _case("plain_512_born", 1)
     F = 2 * acq.nxmax
+    g = Geometry.from_acquisition(acq)
     out = torch.zeros((1, F, F, 2), dtype=torch.float32, device="cuda")
+    einval, eunsup = api.STATUS_CODES["TDM_EINVAL"], api.STATUS_CODES["TDM_EUNSUPPORTED"]
     # holograms in host memory: the entry point takes device buffers only
-    assert api.extract_noalloc(Geometry.from_acquisition(acq), holos.cpu(), out) == api.STATUS_CODES["TDM_EINVAL"]
+    assert _raw(g, api.ptr(holos.cpu()), 1, api.ptr(out)) == einval
+    # spectra not 8-byte aligned, 16-bit holograms not 2-byte aligned: refused before any launch
+    wide = torch.zeros(2 * F * F + 2, dtype=torch.float32, device="cuda")
+    assert _raw(g, api.ptr(holos), 1, ctypes.c_void_p(wide.data_ptr() + 4)) == einval
+    hb = torch.zeros(holos.numel() + 1, dtype=torch.uint16, device="cuda")
+    assert _raw(g, ctypes.c_void_p(hb.data_ptr() + 1), 1, api.ptr(out)) == einval
     # a 2048^2 hologram with 512^2 crops needs 8 MiB of scratch, beyond the fixed 4 MiB
     big = Geometry.from_acquisition(acq)
     big.ccd_roix, big.nxmax, big.circle_cx, big.circle_cy = 2048, 256, 512, 512
-    assert api.extract_noalloc(big, holos, out) == api.STATUS_CODES["TDM_EUNSUPPORTED"]
+    assert _raw(big, api.ptr(holos), 1, api.ptr(out)) == eunsup
+    # the wrapper refuses buffers too small for n before calling the library
+    with pytest.raises(ValueError):
+        api.extract_noalloc(g, holos, out, n=2)
