@@ -295,11 +295,13 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
                         "%d-plane cap band must fit one CTA's shared memory)\n", most, p.band);
         return TDM_EUNSUPPORTED;
     }
-    // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:885-902): k0 is a float
+    // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:885-902): k0 is a
+    // float, and that file defines PI as 3.14159 (:2), which the cap weight keeps
+    const double pi_ref = 3.14159;
     const float n0f = (float)geom->n0;
-    const float kv = (float)(2 * M_PI / geom->lambda0);
+    const float kv = (float)(2 * pi_ref / geom->lambda0);
     const float k0 = kv * n0f;
-    p.cap_scale = (float)(((double)k0 / M_PI) * (-2 * M_PI));
+    p.cap_scale = (float)(((double)k0 / pi_ref) * (-2 * pi_ref));
     p.dx2 = (float)std::pow(c->dv.tp_uborn, 2);
     const double k_v = 2 * M_PI / geom->lambda0;  // main.cpp:346-347
     p.out_scale = (float)(std::pow(c->dv.delta_f, 3) * (-1 / (2 * geom->n0 * k_v * k_v)));

@@ -1,9 +1,11 @@
 """ctypes wrapper of the FP64 CPU oracle (``tdm_oracle.cpp``).
 
 Test infrastructure only: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py``, to produce reference values.  Parity is unpinned:
-the reference cannot be built here and ships no golden vectors for this path,
-so the oracle restates the reference functions (cited file:line in the C++).
+and the CPU-baseline leg of ``bench.py``, to produce reference values.  The
+restatement follows the reference functions (cited file:line in the C++) and
+is pinned on them: ``oracle.reference_build`` runs the reference's own source
+files, compiled into ``oracle/_ref/``, on the same inputs
+(``tests/test_oracle_pinned.py``).
 """
 from __future__ import annotations
 

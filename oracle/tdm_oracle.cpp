@@ -4,16 +4,21 @@
 // of bench.py call it to produce reference values.
 // Nothing in the product (mtd_transmission_gb300/) links, loads or calls it.
 //
-// PARITY UNPINNED.  The reference (madeba/MTD_transmission) cannot be built in
-// this environment (FFTW3, OpenCV4, libtiff and HDF5 are absent) and ships no
-// tests, golden vectors or fixtures for this path.  This oracle is a
-// line-by-line FP64 restatement of the reference's own functions; every
-// function below cites the reference file:line it follows.  Its FFT replaces
-// FFTW3 (unpinned version; DFT with FFTW's sign and scaling conventions:
-// FORWARD = exp(-2*pi*i*jk/n), BACKWARD = exp(+2*pi*i*jk/n), both unnormalised)
-// and is cross-checked against numpy.fft in the tests.  The least-squares
-// solve replaces OpenCV's cv::solve(DECOMP_NORMAL): normal equations A^T A,
-// A^T b followed by Gaussian elimination with partial pivoting.
+// PARITY PINNED ON THE REFERENCE'S OWN CODE.  The reference's programs
+// cannot be built as they stand (FFTW3, OpenCV4, libtiff and HDF5 are absent)
+// and it ships no tests, golden vectors or fixtures for this path.  This
+// oracle is a line-by-line FP64 restatement of the reference's functions;
+// every function below cites the reference file:line it follows.  The
+// reference's own source files for the path are compiled, against stand-in
+// headers, into oracle/_ref/ (oracle/ref/build_ref.py), and
+// tests/test_oracle_pinned.py compares this restatement with them on the
+// same inputs (window and counts bit for bit, positions exactly, values at
+// FP64 round-off).  Its FFT replaces FFTW3 (DFT with FFTW's sign and scaling
+// conventions: FORWARD = exp(-2*pi*i*jk/n), BACKWARD = exp(+2*pi*i*jk/n),
+// both unnormalised) and is cross-checked against numpy.fft in the tests.  The
+// least-squares solve replaces OpenCV's cv::solve(DECOMP_NORMAL): normal
+// equations A^T A, A^T b followed by Gaussian elimination with partial
+// pivoting (OpenCV is not available to the pin; checked against numpy).
 //
 // Undefined behaviour in the reference is given a pinned oracle policy:
 //  * Volkov DC term (deroulement_volkov4.cpp:189 reads tampon[nbPix], one past
@@ -44,12 +49,17 @@ using cd = std::complex<double>;
 namespace {
 
 // ---------------------------------------------------------------------------
-// FFT (FFTW conventions).  Radix-2 iterative Cooley-Tukey, power-of-two sizes.
+// FFT (FFTW conventions).  Radix-2 iterative Cooley-Tukey for power-of-two
+// sizes; other sizes (the reference's own configuration has NXMAX 125: 250-
+// and 500-point transforms) by a recursive mixed-radix decomposition
+// (decimation in time, n = p m: p transforms of m points on the stride-p
+// subsequences combined by p-point DFTs with twiddles W_n^(q k)).
 // ---------------------------------------------------------------------------
 struct Plan {
     int n = 0, logn = 0;
-    std::vector<cd> tw;     // exp(-2 pi i k / n), k < n/2
+    std::vector<cd> tw;     // exp(-2 pi i k / n), k < n/2 (power of two); k < n (other sizes)
     std::vector<int> rev;
+    std::vector<int> radices;  // other sizes: the factors, small first
 };
 
 std::mutex g_plan_mu;
@@ -61,6 +71,27 @@ const Plan& get_plan(int n) {
     if (it != g_plans.end()) return *it->second;
     auto p = std::make_unique<Plan>();
     p->n = n;
+    if (n & (n - 1)) {
+        int m = n;
+        for (int r : {4, 2, 3, 5, 7})
+            while (m % r == 0) {
+                p->radices.push_back(r);
+                m /= r;
+            }
+        for (int r = 11; m > 1; r += 2)
+            while (m % r == 0) {
+                p->radices.push_back(r);
+                m /= r;
+            }
+        p->tw.resize(n);
+        for (int k = 0; k < n; ++k) {
+            long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)n;
+            p->tw[k] = cd((double)std::cos(a), (double)std::sin(a));
+        }
+        const Plan& ref = *p;
+        g_plans[n] = std::move(p);
+        return ref;
+    }
     int lg = 0;
     while ((1 << lg) < n) ++lg;
     p->logn = lg;
@@ -90,9 +121,44 @@ double omp_wall() {
 #endif
 }
 
+// out[0, len) = DFT of in[0], in[stride], ... (len points) with the plan's
+// radices from index fi on; len divides p.n.
+void fft_mixed(const cd* in, cd* out, int len, long stride, size_t fi, const Plan& p, int sign) {
+    if (len == 1) {
+        out[0] = in[0];
+        return;
+    }
+    const int r = p.radices[fi], m = len / r, step = p.n / len;  // W_len^e = tw[e step]
+    for (int q = 0; q < r; ++q) fft_mixed(in + q * stride, out + q * m, m, stride * r, fi + 1, p, sign);
+    auto w = [&](long e) {
+        const cd v = p.tw[(size_t)(e % len) * step];
+        return sign > 0 ? std::conj(v) : v;
+    };
+    cd t[16];
+    std::vector<cd> tv;
+    cd* tt = t;
+    if (r > 16) {
+        tv.resize(r);
+        tt = tv.data();
+    }
+    for (int k = 0; k < m; ++k) {
+        for (int q = 0; q < r; ++q) tt[q] = out[q * m + k] * w((long)q * k);
+        for (int j = 0; j < r; ++j) {
+            cd acc = 0;
+            for (int q = 0; q < r; ++q) acc += tt[q] * w((long)q * j * m);  // W_r^(q j)
+            out[k + j * m] = acc;
+        }
+    }
+}
+
 // In-place 1D DFT. sign = -1: FFTW_FORWARD, +1: FFTW_BACKWARD. Unnormalised.
 void fft1d(cd* x, const Plan& p, int sign) {
     const int n = p.n;
+    if (!p.radices.empty()) {
+        std::vector<cd> a(x, x + n);
+        fft_mixed(a.data(), x, n, 1, 0, p, sign);
+        return;
+    }
     for (int i = 0; i < n; ++i) {
         int j = p.rev[i];
         if (i < j) std::swap(x[i], x[j]);
@@ -456,12 +522,12 @@ void orc_tukey2d(int n, float alpha, double* out) {
 
 // Plain DFTs for cross-checks (FFTW sign conventions, unnormalised).
 int orc_fft2d(double* data, int dim, int sign) {
-    if (!is_pow2(dim)) return -1;
+    if (dim < 1) return -1;
     fft2d(reinterpret_cast<cd*>(data), dim, sign);
     return 0;
 }
 int orc_fft3d(double* data, int dim, int sign) {
-    if (!is_pow2(dim)) return -1;
+    if (dim < 1) return -1;
     fft3d(reinterpret_cast<cd*>(data), dim, sign);
     return 0;
 }
@@ -472,7 +538,7 @@ int orc_fft3d(double* data, int dim, int sign) {
 // out: F*F complex (interleaved re, im).  Returns 0, or -1 on a crop outside
 // the hologram spectrum (reference UB).
 int orc_extract(const double* holo, int H, int nxmax, int cx, int cy, const double* tukey, double* out) {
-    if (!is_pow2(H)) return -2;
+    if (H & 1) return -2;
     const int F = 2 * nxmax;
     const int x0 = cx - nxmax, y0 = cy - nxmax;
     if (x0 < 0 || y0 < 0 || x0 + F > H || y0 + F > H) return -1;
@@ -607,21 +673,23 @@ int orc_reconstruction(const double* fields, const double* posspec, int M, const
     orc_derive(cfg, &dv);
     const int N = cfg->nxmax, F = 2 * N, D = cfg->dim_final;
     const size_t P = (size_t)F * F, NT = (size_t)D * D * D;
-    if (!is_pow2(F) || !is_pow2(D)) return -2;
+    if ((F & 1) || (D & 1)) return -2;  // even sizes (the shifts are half-size rolls)
     std::vector<double> tuk = tukey2D(F, F, 0.1f);
     std::vector<cd> tf3d(NT);
     std::vector<double> sup(NT, 0.0);
     const int dec = (int)std::round(D / 2);
-    // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:884-902)
+    // retroPropag_Born constants (Reconstruction/src/fonctions.cpp:884-902);
+    // that file defines PI as 3.14159 (:2)
+    const double PI_REF = 3.14159;
     float n0f = (float)cfg->n0;
-    float kv = (float)(2 * M_PI / cfg->lambda0);
+    float kv = (float)(2 * PI_REF / cfg->lambda0);
     float k0 = kv * n0f;
     const double rayon = dv.rayon;
-    const double cteNorm = -2 * M_PI;
+    const double cteNorm = -2 * PI_REF;
     const double r2 = rayon * rayon;
     const double norm_altitude = 1.0 / rayon;
     const int dimVolX = (int)std::round((double)D), dimPlanFinal = (int)std::round((double)D * D);
-    const cd cteUb2Pot(0, k0 / M_PI);
+    const cd cteUb2Pot(0, k0 / PI_REF);
     const double dx = dv.tp_uborn;
     const double coefnorm = std::pow(dx, 2);
     int bad = 0;

@@ -18,7 +18,7 @@ import pytest
 
 import oracle
 from mtd_transmission_gb300 import Context, Geometry, TdmError, api
-from tests.helpers import c64, oracle_cfg, small_case
+from tests.helpers import c64, planted_ties, small_case
 
 pytestmark = pytest.mark.gpu
 
@@ -32,41 +32,12 @@ def _fp32_decision(spec: np.ndarray) -> int:
     return int(np.argmax(v))  # first maximum
 
 
-def _planted_spectra(F: int, M: int, rng) -> np.ndarray:
-    """Random spectra with near ties planted at the top."""
-    s = (rng.standard_normal((M, F, F)) + 1j * rng.standard_normal((M, F, F))).astype(np.complex64)
-    s *= np.float32(0.25)
-    out = []
-    for a in range(M):
-        sp = s[a].ravel().copy()
-        m = np.float32(4.0)  # above every random magnitude; m^2 exact
-        p = int(rng.integers(1, F * F - 8))
-        kind = a % 5
-        if kind == 0:    # FP32 tie, FP64 larger at the later bin
-            sp[p] = m
-            sp[p + 3] = np.complex64(m + 1j * m * np.float32(2.0 ** -15))
-        elif kind == 1:  # exact tie: the first bin wins
-            sp[p] = m
-            sp[p + 5] = m
-        elif kind == 2:  # index 0 compared by |z|^2: (2, 0) ties with |z| = 4
-            sp[0] = np.float32(2.0)
-            sp[p] = m
-        elif kind == 3:  # index 0 larger in FP64 only: |z0|^2 = 4 (1 + 2^-30) against 4
-            sp[0] = np.complex64(2.0 + 1j * 2.0 * np.float32(2.0 ** -15))
-            sp[p] = m
-        else:            # the same at a value that is not a power of two: FP32 ties, FP64 larger later
-            sp[p] = np.complex64(m * np.float32(1.0 + 2.0 ** -23))
-            sp[p + 2] = np.complex64(m * np.float32(1.0 + 2.0 ** -23) + 1j * m * np.float32(2.0 ** -16))
-        out.append(sp.reshape(F, F))
-    return np.stack(out)
-
-
 def test_specular_near_ties_match_fp64():
     acq, _, _ = small_case("plain_512_born", M=1)
     F = 2 * acq.nxmax
     M = 10
     rng = np.random.default_rng(7)
-    spec = _planted_spectra(F, M, rng)
+    spec = planted_ties(F, M, rng)
     ref = [oracle.coord_spec(spec[a].astype(np.complex128)) for a in range(M)]
     fp32 = [_fp32_decision(spec[a]) for a in range(M)]
     assert fp32 != ref  # the planted ties do separate FP32 from FP64

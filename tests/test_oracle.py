@@ -12,7 +12,7 @@ import oracle
 from tests.helpers import oracle_cfg, rel_l2, small_case
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 512])
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 250, 500, 200, 6])
 def test_fft2d_matches_numpy(n):
     rng = np.random.default_rng(n)
     a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
