@@ -40,7 +40,7 @@ struct ExtractCfg {
     }
     static size_t smem_cols(int F) { return ((size_t)C * W::STRIDE + (size_t)F * (C + 1)) * sizeof(float2); }
     static dim3 grid_rows(int m) { return dim3(H / (2 * P), m); }
-    static dim3 grid_cols(int F, int m) { return dim3(F / C, m); }
+    static dim3 grid_cols(int F, int m) { return dim3((F + C - 1) / C, m); }
 };
 
 // Row pass.  tuk is the 1D hologram window, exactly 1 on [flat.x, flat.y]
@@ -169,11 +169,12 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     float2* tile = sm + C * W::STRIDE;  // F x TC: [crop row][column in CTA]
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, c0 = blockIdx.x * C, c = c0 + tr;
+    const bool valid = c < F;  // the crop width need not be a multiple of C
     float2* s = sm + tr * W::STRIDE;
     const float2* src = inter + ((size_t)a * F + c) * H;
     float2 x[E];
 #pragma unroll
-    for (int n1 = 0; n1 < E; ++n1) x[n1] = src[j + n1 * T];
+    for (int n1 = 0; n1 < E; ++n1) x[n1] = valid ? src[j + n1 * T] : make_float2(0.f, 0.f);
     fft_warp_regs<H, -1>(x, s, j, tw);
     __syncwarp();
 #pragma unroll
@@ -191,7 +192,7 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
         const float sg = ((kx + ky) & 1) ? -inv : inv;
         const float2 z = c_scale(s[W::pad(ky)], sg);
         tile[r * TC + tr] = z;
-        if (argpart) argmax_take(best, bi, second, z, r * F + c);
+        if (argpart && valid) argmax_take(best, bi, second, z, r * F + c);
     }
     if (argpart) {  // this warp's partial winner of the specular search (8 records per CTA)
         argmax_warp(best, bi, second);
@@ -202,7 +203,7 @@ k_extract_cols(const float2* __restrict__ inter, const float2* __restrict__ tw, 
     float2* dst = spectra + (size_t)a * F * F + c0;
     for (int i = threadIdx.x; i < F * C; i += Cf::NT) {
         const int r = i / C, t = i % C;
-        dst[(size_t)r * F + t] = tile[r * TC + t];
+        if (c0 + t < F) dst[(size_t)r * F + t] = tile[r * TC + t];
     }
 }
 

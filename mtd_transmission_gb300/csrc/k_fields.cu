@@ -50,11 +50,11 @@ __device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F 
 __global__ void __launch_bounds__(256) k_argmax_part(const float2* __restrict__ spectra, int F,
                                                      float4* __restrict__ part) {
     const int a = blockIdx.y, sl = blockIdx.x;
-    const int per = F * F / kArgSlices, i0 = sl * per;
+    const int per = (F * F + kArgSlices - 1) / kArgSlices, i0 = sl * per, i1 = min(i0 + per, F * F);
     const float2* s = spectra + (size_t)a * F * F;
     float best = -1.0f, second = -1.0f;
     int bi = 0x7fffffff;
-    for (int i = i0 + threadIdx.x; i < i0 + per; i += blockDim.x) argmax_take(best, bi, second, s[i], i);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) argmax_take(best, bi, second, s[i], i);
     argmax_block(best, bi, second);
     if (threadIdx.x == 0) part[(size_t)a * kArgSlices + sl] = argmax_record(best, bi, second);
 }
@@ -702,8 +702,29 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
 
 }  // namespace
 
+int launch_argmax_part(tdm_ctx* c, const float2* spec, int m) {
+    Launch l(c, K_ARGMAX);
+    k_argmax_part<<<dim3(kArgSlices, m), 256, 0, c->stream>>>(spec, c->p.F, c->b.argpart);
+    return kArgSlices;
+}
+
+void launch_aber_fit(tdm_ctx* c, const float* unw, int m) {
+    Launch l(c, K_ABER_FIT);
+    k_aber_fit<<<dim3(kFitSlices, 2, m), kFitThreads, 0, c->stream>>>(unw, c->b.amp, c->b.samp_idx, c->b.samp_q,
+                                                                      c->nsamp, c->p.F, c->b.rinv, c->b.fit_part,
+                                                                      c->b.fit_done, c->b.beta);
+}
+
+void launch_form(tdm_ctx* c, const float* unw, int g0, int m) {
+    const size_t FF = (size_t)c->p.F * c->p.F;
+    Launch l(c, K_FORM);
+    k_form<<<dim3((unsigned)((FF + 255) / 256), m), 256, 0, c->stream>>>(unw, c->b.amp, c->b.beta, c->p.F, c->p.born,
+                                                                        c->b.fields + (size_t)g0 * FF);
+}
+
 int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp, int argparts,
                   bool form) {
+    if (c->p.F & (c->p.F - 1)) return launch_fields_generic(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
     switch (c->p.F) {
         case 64: return fields_impl<64>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
         case 128: return fields_impl<128>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);

@@ -1,0 +1,543 @@
+// Field formation and cap mapping for field sizes that are not powers of two.
+//
+// The reference's own configuration has NXMAX 125: 250 x 250 fields and a
+// 500 x 500 Volkov mirror (Tomo_config/config_manip.txt:16).  These passes
+// compute what the warp-resident passes of k_fields.cu and k_recon.cu
+// compute, on the same buffers and with the same algebra, but each transform
+// runs on the mixed-radix engine of fft_generic.cuh: one warp per transform,
+// its points in shared memory in natural order.  A row pass gives each warp
+// one row (coalesced loads and stores); a column pass stages kCols columns
+// CTA-wide and gives each warp one column.  The passes:
+//
+//  gk_field_rows / gk_field_cols   calc_Uborn2 (pretraitement_hors_axe_CPU/fonctions.cpp:348-374):
+//                                  shift by -posSpec, inverse FFT, shift by (N, N);
+//                                  phase, amplitude and phasor (fonctions.cpp:39-43)
+//  gk_volkov_rows / gk_volkov_cols deroul_volkov4_total_sym_paire (src/deroulement_volkov4.cpp:14-92):
+//                                  the mirror's derivatives from F-point transforms
+//                                  (a DCT-II of the row, its derivative a DST), and
+//                                  the 2F-point FFT of Q = gx + i gy along each column
+//                                  from one F-point transform (Q is conjugate-symmetric)
+//  gk_volkov_integ_rows / _cols    integ_grad4 (:162-191) and cut_quad4 (:247-276)
+//  gk_cap_rows(_form) / gk_cap_cols per-field spectrum (Reconstruction/main.cpp:203-217)
+//                                  and the cap records of retroPropag_Born
+//                                  (Reconstruction/src/fonctions.cpp:875-935)
+#include "tdm_internal.cuh"
+#include "fft_generic.cuh"
+#include "cap_geometry.cuh"
+#include "form.cuh"
+#include "argmax.cuh"
+
+namespace tdm {
+namespace {
+
+constexpr float kTwoPiG = 6.283185307179586f;
+constexpr float kInvTwoPiG = 0.15915494309189535f;
+constexpr int kRows = 8;  // warps (rows) per CTA of a row pass
+constexpr int kCols = 8;  // columns (warps) per CTA of a column pass
+
+template <class K>
+cudaError_t allow_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+__host__ __device__ constexpr int gmirror_pos(int m, int F) { return m < F / 2 ? 2 * m : 2 * (F - 1 - m) + 1; }
+// element m of the permuted sequence that holds row (or column) y: gmirror_pos(m) = y
+__host__ __device__ constexpr int gslot(int y, int F) { return (y & 1) ? F - 1 - (y >> 1) : (y >> 1); }
+
+__device__ __forceinline__ float gkappa(int k, int L) {  // init_kvect_shift, FFT_fonctions.cpp:7-17
+    return (float)(k < L / 2 ? k : k - L) / (float)L;
+}
+
+// exp(s 2 pi i k / M) from the 4F-entry table (M divides 4F).
+template <int Q, int M, int S>
+__device__ __forceinline__ float2 groot(const float2* __restrict__ wq, int k) {
+    float2 w = __ldg(&wq[(k % M) * (Q / M)]);
+    if constexpr (S > 0) w.y = -w.y;
+    return w;
+}
+
+// Mirror derivative from F-point transforms (the algebra of k_fields.cu's
+// mirror_derivative): a holds the row permuted by gmirror_pos on entry; on
+// return a[x] holds the derivative of the row's 2F-point even mirror at
+// X = F + x.  b is scratch.
+template <int F>
+__device__ __forceinline__ void gmirror_derivative(float2* a, float2* b, const float2* __restrict__ wq, int lane) {
+    constexpr int Q = 4 * F;
+    constexpr float c = 0.5f * kTwoPiG / (float)(2 * F);  // pi / 2F
+    gfft<F, -1, Q>(a, b, wq, lane);
+    for (int k = lane; k < F; k += 32) {
+        // W[k] = (i pi / 2F) (e^{i pi k/F} V[F-k] - (1 - 2k/F) V[k]), W[0] = 0
+        const float2 vm = a[k ? F - k : 0];
+        const float2 e = groot<Q, 2 * F, +1>(wq, k);
+        const float2 t = c_sub(c_mul(e, vm), c_scale(a[k], 1.0f - 2.0f * (float)k / (float)F));
+        b[k] = k == 0 ? make_float2(0.0f, 0.0f) : make_float2(-c * t.y, c * t.x);
+    }
+    __syncwarp();
+    gfft<F, +1, Q>(b, a, wq, lane);
+    for (int m = lane; m < F; m += 32) a[gmirror_pos(m, F)] = m < F / 2 ? b[m] : make_float2(-b[m].x, -b[m].y);
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------- field = shift(IFFT(shift(S)))
+template <int F>
+__global__ void __launch_bounds__(kRows * 32)
+gk_field_rows(const float2* __restrict__ spectra, const float4* __restrict__ argpart, int nparts,
+              int2* __restrict__ posspec, float2* __restrict__ specval, int normalize, const float2* __restrict__ wq,
+              float2* __restrict__ I1) {
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, r = blockIdx.x * kRows + w;
+    const float2* spec = spectra + (size_t)a * F * F;
+    const int bi = argmax_final(argpart + (size_t)a * nparts, nparts, spec, F * F);
+    const int2 p = make_int2(bi % F, bi / F);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        posspec[a] = p;
+        specval[a] = spec[bi];
+    }
+    if (r >= F) return;  // warp-uniform, after the CTA-wide search
+    float2 nrm = make_float2(1.0f, 0.0f);
+    if (normalize) {  // TF_UBorn * conj(spec) / |spec| (main.cpp:332-335)
+        const float2 s0 = spec[bi];
+        const float mod = sqrtf(s0.y * s0.y + s0.x * s0.x);
+        nrm = make_float2(s0.x / mod, -s0.y / mod);
+    }
+    float2* A = sm + w * 2 * F;
+    float2* B = A + F;
+    const float2* src = spec + (size_t)wrap_f(r + p.y, F) * F;
+    for (int n = lane; n < F; n += 32) {
+        const float2 v = src[wrap_f(n + p.x, F)];
+        A[n] = normalize ? c_mul(v, nrm) : v;
+    }
+    __syncwarp();
+    gfft<F, +1, 4 * F>(A, B, wq, lane);
+    float2* dst = I1 + ((size_t)a * F + r) * F;
+    for (int k = lane; k < F; k += 32) dst[k] = A[k];
+}
+
+// mode 1: phase/amplitude/phasor (C_ABER); mode 0: the field itself.
+template <int F>
+__global__ void __launch_bounds__(kCols * 32)
+gk_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ wq, float* __restrict__ phase,
+              float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields) {
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, x0 = blockIdx.x * kCols;
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int t = i % kCols, r = i / kCols;
+        if (x0 + t < F) sm[t * 2 * F + r] = I1[((size_t)a * F + r) * F + x0 + t];
+    }
+    __syncthreads();
+    if (x0 + w < F) gfft<F, +1, 4 * F>(sm + w * 2 * F, sm + w * 2 * F + F, wq, lane);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int t = i % kCols, y = i / kCols;
+        if (x0 + t >= F) continue;
+        const float2 u = sm[t * 2 * F + y];
+        const int yo = wrap_f(y + F / 2, F), xo = wrap_f(x0 + t + F / 2, F);
+        const size_t o = ((size_t)a * F + yo) * F + xo;
+        if (mode) {
+            const float m = hypotf(u.x, u.y);
+            phase[o] = atan2f(u.y, u.x);
+            amp[o] = m;
+            zph[o] = m > 0.0f ? make_float2(u.x / m, u.y / m) : make_float2(1.0f, 0.0f);
+        } else {
+            fields[o] = u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Volkov unwrap
+// Pass 1: rows.  Per image row pair, three transforms (the phasor Z of each
+// row, and the two rows' phases packed as a + i b); the x derivative on the
+// mirror's right half gives gx = (Re(-i dZ/dx / Z) - dphi/dx) / 2pi.
+constexpr int kPairs = 2;  // row pairs per CTA: 3 kPairs warps
+template <int F>
+__global__ void __launch_bounds__(3 * kPairs * 32)
+gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ wq,
+               float* __restrict__ gxh) {
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y;
+    const bool zk = w < 2 * kPairs;
+    const int pair = zk ? w >> 1 : w - 2 * kPairs, ab = w & 1;
+    const int ya = 2 * (blockIdx.x * kPairs + pair);
+    const bool live = ya < F;  // warp-uniform
+    float2* A = sm + w * 2 * F;
+    float2* B = A + F;
+    const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
+    if (live) {
+        const float2* zr = zph + (ab ? rb : ra);
+        for (int m = lane; m < F; m += 32) {
+            const int x = gmirror_pos(m, F);
+            A[m] = zk ? zr[x] : make_float2(phase[ra + x], phase[rb + x]);
+        }
+        __syncwarp();
+        gmirror_derivative<F>(A, B, wq, lane);
+    }
+    __syncthreads();
+    if (live && zk) {
+        const float2* zr = zph + (ab ? rb : ra);
+        const float2* q = sm + (2 * kPairs + pair) * 2 * F;
+        float* out = gxh + (ab ? rb : ra);
+        for (int x = lane; x < F; x += 32) {
+            const float2 z = zr[x], g = A[x], qv = q[x];
+            const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
+            out[x] = (ax - (ab ? qv.y : qv.x)) * kInvTwoPiG;
+        }
+    }
+}
+
+// Pass 2: columns X = F + x of the mirror, kCols per CTA: the y derivatives
+// (kCols Z columns, kCols/2 packed phase pairs), gy and Q = gx + i gy, then
+// the 2F-point FFT of Q along each column from one F-point transform of
+// gx + i (-1)^y gy permuted by gmirror_pos (the algebra of k_fields.cu's
+// symmetric_fft): with V that transform and w = e^{-i pi k/2F},
+//     FFT(Q)[k] = 2 (-1)^k conj(w) (Re C[k] + Im C[F-k]),
+//     FFT(Q)[2F-k] = -2 (-1)^k w (Im C[F-k] - Re C[k]),  FFT(Q)[F] = 2 i Im C[0],
+//     C[k] = (w V[k] + conj(w) V[F-k]) / 2.
+template <int F>
+__global__ void __launch_bounds__((kCols + kCols / 2) * 32)
+gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
+               const float2* __restrict__ wq, float2* __restrict__ qc) {
+    constexpr int L = 2 * F, Q4 = 4 * F;
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, x0 = blockIdx.x * kCols;
+    auto arr = [&](int t) { return sm + t * 2 * F; };  // warp t's pair of F-point arrays
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int c = i % kCols, y = i / kCols;
+        if (x0 + c >= F) continue;
+        const size_t o = ((size_t)a * F + y) * F + x0 + c;
+        const int e = gslot(y, F);
+        arr(c)[e] = zph[o];
+        reinterpret_cast<float*>(&arr(kCols + (c >> 1))[e])[c & 1] = phase[o];
+    }
+    __syncthreads();
+    const bool live = x0 + (w < kCols ? w : 2 * (w - kCols)) < F;  // warp-uniform
+    if (live) gmirror_derivative<F>(arr(w), arr(w) + F, wq, lane);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int c = i % kCols, y = i / kCols;
+        if (x0 + c >= F) continue;
+        const size_t o = ((size_t)a * F + y) * F + x0 + c;
+        const float2 z = zph[o], g = arr(c)[y], q = arr(kCols + (c >> 1))[y];
+        const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
+        const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPiG;
+        arr(c)[F + gslot(y, F)] = make_float2(gxh[o], (y & 1) ? -gy : gy);
+    }
+    __syncthreads();
+    if (w < kCols && x0 + w < F) {
+        float2* V = arr(w) + F;
+        float2* S = arr(w);
+        gfft<F, -1, Q4>(V, S, wq, lane);
+        // bins of this column: [0, F) into S, [F, 2F) into the phase pair's arrays
+        // (free now), after every lane has read V
+        float2 lo[(F + 31) / 32], hi[(F + 31) / 32];
+#pragma unroll
+        for (int u = 0; u < (F + 31) / 32; ++u) {
+            const int k = lane + 32 * u;
+            if (k >= F) break;
+            const float2 wk = groot<Q4, 2 * L, -1>(wq, k);  // e^{-i pi k/2F}
+            const float2 va = c_mul(wk, V[k]), vb = c_mul(c_conj(wk), V[k ? F - k : 0]);
+            const float ck = 0.5f * (va.x + vb.x), cf = 0.5f * (va.x - vb.x);
+            const float sg = (k & 1) ? -2.0f : 2.0f;
+            if (k == 0) {
+                lo[u] = make_float2(2.0f * ck, 0.0f);
+                hi[u] = make_float2(0.0f, va.y + vb.y);  // bin F
+            } else {
+                const float r1 = sg * (ck + cf), r2 = -sg * (cf - ck);
+                lo[u] = make_float2(r1 * wk.x, -r1 * wk.y);  // bin k
+                hi[u] = make_float2(r2 * wk.x, r2 * wk.y);   // bin 2F - k
+            }
+        }
+        __syncwarp();
+        float2* H = arr(kCols + (w >> 1)) + (w & 1) * F;
+#pragma unroll
+        for (int u = 0; u < (F + 31) / 32; ++u) {
+            const int k = lane + 32 * u;
+            if (k >= F) break;
+            S[k] = lo[u];
+            H[k == 0 ? 0 : F - k] = hi[u];  // bin F + j at H[j]
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCols * L; i += blockDim.x) {
+        const int c = i % kCols, ky = i / kCols;
+        if (x0 + c >= F) continue;
+        qc[((size_t)a * L + ky) * F + x0 + c] = ky < F ? arr(c)[ky] : arr(kCols + (c >> 1))[(c & 1) * F + ky - F];
+    }
+}
+
+// Pass 3: rows ky in [0, L/2] of FFT2(Q); integ_grad4's tampon; inverse FFT
+// along x; the quadrant-4 columns are kept (k_volkov_integ_rows' algebra).
+template <int F>
+__global__ void __launch_bounds__(kRows * 32)
+gk_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ wq, float2* __restrict__ tq) {
+    constexpr int L = 2 * F, Q4 = 4 * F;
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, r = blockIdx.x * kRows + w;
+    if (r > L / 2) return;  // warp-uniform; no CTA barrier below
+    float2* A = sm + w * 2 * L;
+    float2* B = A + L;
+    const int rp = r ? L - r : 0;
+    for (int X = lane; X < L; X += 32) {
+        if (X >= F) {
+            A[X] = qc[((size_t)a * L + r) * F + (X - F)];
+        } else {
+            const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
+            A[X] = make_float2(-u.x, u.y);
+        }
+    }
+    __syncwarp();
+    gfft<L, -1, Q4>(A, B, wq, lane);
+    const float nrm = 1.0f / ((float)L * (float)L), ky = gkappa(r, L);
+    for (int kx = lane; kx < L; kx += 32) {
+        const float2 wv = groot<Q4, L, -1>(wq, kx + r);  // exp(-2 pi i (kx + ky)/L)
+        const float2 Qv = A[kx];
+        const float2 Qm = make_float2(-(wv.x * Qv.x - wv.y * Qv.y), -(-wv.y * Qv.x - wv.x * Qv.y));
+        const float2 Gx = make_float2(0.5f * (Qv.x + Qm.x) * nrm, 0.5f * (Qv.y + Qm.y) * nrm);
+        const float2 Gy = make_float2(0.5f * (Qv.y - Qm.y) * nrm, -0.5f * (Qv.x - Qm.x) * nrm);
+        const float kxv = gkappa(kx, L);
+        const float k2 = kxv * kxv + ky * ky;
+        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
+        const float rden = 1.0f / (kTwoPiG * k2);
+        A[kx] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y * rden, -num.x * rden);
+    }
+    __syncwarp();
+    gfft<L, +1, Q4>(A, B, wq, lane);
+    float2* dst = tq + ((size_t)a * L + r) * F - F;
+    for (int X = F + lane; X < L; X += 32) dst[X] = A[X];
+}
+
+// Pass 4: columns of quadrant 4: inverse FFT along y, real part, phi + 2 pi IntM.
+template <int F>
+__global__ void __launch_bounds__(kCols * 32)
+gk_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ phase, const float2* __restrict__ wq,
+                     float* __restrict__ unwrapped) {
+    constexpr int L = 2 * F, Q4 = 4 * F;
+    extern __shared__ float2 sm[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, c0 = blockIdx.x * kCols;
+    for (int i = threadIdx.x; i < kCols * L; i += blockDim.x) {
+        const int t = i % kCols, ky = i / kCols;
+        if (c0 + t >= F) continue;
+        float2 v;
+        if (ky <= L / 2) {
+            v = tq[((size_t)a * L + ky) * F + c0 + t];
+        } else {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
+            const float2 u = tq[((size_t)a * L + (L - ky)) * F + c0 + t];
+            const float2 wv = groot<Q4, L, -1>(wq, ky);
+            v = make_float2(wv.x * u.x + wv.y * u.y, wv.x * u.y - wv.y * u.x);
+        }
+        sm[t * 2 * L + ky] = v;
+    }
+    __syncthreads();
+    if (c0 + w < F) gfft<L, +1, Q4>(sm + w * 2 * L, sm + w * 2 * L + L, wq, lane);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int t = i % kCols, y = i / kCols;
+        if (c0 + t >= F) continue;
+        const size_t o = ((size_t)a * F + y) * F + c0 + t;
+        unwrapped[o] = phase[o] + kTwoPiG * sm[t * 2 * L + F + y].x;
+    }
+}
+
+// ---------------------------------------------------------------- cap passes
+// Row pass of the per-field spectrum: x Tukey(0.1) in x and y, forward FFT
+// along x.  FORM: the field is formed on the fly from the chunk's unwrapped
+// phase, amplitude and fits (k_form's arithmetic) and also stored.
+template <int F, bool FORM>
+__global__ void __launch_bounds__(kRows * 32)
+gk_cap_rows(const float2* __restrict__ fields_in, const float* __restrict__ unwrapped, const float* __restrict__ amp,
+            const double* __restrict__ beta, int born, const float* __restrict__ tuk, int2 flat,
+            const float2* __restrict__ wq, float2* __restrict__ fields_out, float2* __restrict__ r1) {
+    extern __shared__ float2 sm[];
+    __shared__ float bf[2 * kNC];
+    if (FORM) {
+        if (threadIdx.x < 2 * kNC) bf[threadIdx.x] = (float)beta[(size_t)blockIdx.y * 2 * kNC + threadIdx.x];
+        __syncthreads();
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, y = blockIdx.x * kRows + w;
+    if (y >= F) return;
+    float2* A = sm + w * 2 * F;
+    const float wy = tuk[y];
+    const size_t row = ((size_t)a * F + y) * F;
+    FormRow fr;
+    if (FORM) fr = form_row(bf, y, F);
+    for (int x = lane; x < F; x += 32) {
+        float2 f;
+        if (FORM) {
+            f = form_value(fr, x, F, unwrapped[row + x], amp[row + x], born);
+            fields_out[row + x] = f;
+        } else {
+            f = fields_in[row + x];
+        }
+        A[x] = c_scale(f, ((x >= flat.x && x <= flat.y) ? 1.0f : __ldg(&tuk[x])) * wy);
+    }
+    __syncwarp();
+    gfft<F, -1, 4 * F>(A, A + F, wq, lane);
+    for (int k = lane; k < F; k += 32) r1[row + k] = A[k];
+}
+
+// Column pass: forward FFT along y, then per bin the cap record
+// (contribution, plane) as k_cap_cols writes it.
+template <int F>
+__global__ void __launch_bounds__(kCols * 32)
+gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ s_tab,
+            const float* __restrict__ s_tabf, Params p, const float2* __restrict__ wq, float4* __restrict__ rec,
+            int* __restrict__ err) {
+    extern __shared__ float2 sm[];
+    __shared__ double s_fz;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = blockIdx.y, kx0 = blockIdx.x * kCols;
+    const int2 ps = posspec[a];
+    if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int t = i % kCols, ky = i / kCols;
+        if (kx0 + t < F) sm[t * 2 * F + ky] = r1[((size_t)a * F + ky) * F + kx0 + t];
+    }
+    __syncthreads();
+    if (kx0 + w < F) gfft<F, -1, 4 * F>(sm + w * 2 * F, sm + w * 2 * F + F, wq, lane);
+    __syncthreads();
+    const double fz = s_fz;
+    const float fzf = (float)fz, ir = (float)p.inv_rayon;
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
+        const int t = i % kCols, ky = i / kCols, kx = kx0 + t;
+        if (kx >= F) continue;
+        const size_t o = ((size_t)a * F + ky) * F + kx;
+        float sf = 0.f;
+        const int z = cap_plane(p, ps, fz, fzf, kx, ky, s_tab, s_tabf, &sf, err);
+        float2 val = make_float2(0.f, 0.f);
+        if (z >= 0) {
+            const float2 v = sm[t * 2 * F + ky];
+            const float Bc = cap_weight(p, sf, ir, kx, ky);
+            val = make_float2(-Bc * v.y, Bc * v.x);
+        }
+        rec[o] = make_float4(val.x, val.y, __int_as_float(z), 0.f);
+    }
+}
+
+constexpr size_t warp_arrays(int n, int warps) { return (size_t)warps * 2 * n * sizeof(float2); }
+
+template <int F>
+int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp, int argparts,
+                 bool form) {
+    constexpr int L = 2 * F;
+    const Params& p = c->p;
+    Buffers& b = c->b;
+    const size_t FF = (size_t)F * F;
+    const size_t sm_rows = warp_arrays(F, kRows), sm_cols = warp_arrays(F, kCols);
+    const size_t sm_vrows = warp_arrays(F, 3 * kPairs), sm_vcols = warp_arrays(F, kCols + kCols / 2);
+    const size_t sm_irows = warp_arrays(L, kRows), sm_icols = warp_arrays(L, kCols);
+    if (allow_smem(gk_field_rows<F>, sm_rows) || allow_smem(gk_field_cols<F>, sm_cols) ||
+        allow_smem(gk_volkov_rows<F>, sm_vrows) || allow_smem(gk_volkov_cols<F>, sm_vcols) ||
+        allow_smem(gk_volkov_integ_rows<F>, sm_irows) || allow_smem(gk_volkov_integ_cols<F>, sm_icols))
+        return TDM_ECUDA;
+    const unsigned rows = (F + kRows - 1) / kRows, cols = (F + kCols - 1) / kCols;
+    for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
+        const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
+        const float2* spec = b.spectra + (size_t)g0 * FF;
+        const int nparts = argparts ? argparts : launch_argmax_part(c, spec, m);
+        {
+            Launch l(c, K_FIELD_ROWS);
+            gk_field_rows<F><<<dim3(rows, m), kRows * 32, sm_rows, c->stream>>>(
+                spec, b.argpart, nparts, b.posspec + g0, b.specval + g0, p.c_aber ? 0 : 1, b.wq, b.I1);
+        }
+        {
+            Launch l(c, K_FIELD_COLS);
+            gk_field_cols<F><<<dim3(cols, m), kCols * 32, sm_cols, c->stream>>>(b.I1, p.c_aber, b.wq, b.phase, b.amp,
+                                                                                b.zph, b.fields + (size_t)g0 * FF);
+        }
+        if (!p.c_aber) continue;
+        const float* unw = b.phase;
+        if (p.deroul) {
+            {
+                Launch l(c, K_VOLKOV_ROWS);
+                gk_volkov_rows<F><<<dim3((F / 2 + kPairs - 1) / kPairs, m), 3 * kPairs * 32, sm_vrows, c->stream>>>(
+                    b.phase, b.zph, b.wq, b.gx);
+            }
+            {
+                Launch l(c, K_VOLKOV_COLS);
+                gk_volkov_cols<F><<<dim3(cols, m), (kCols + kCols / 2) * 32, sm_vcols, c->stream>>>(
+                    b.phase, b.zph, b.gx, b.wq, b.qc);
+            }
+            {
+                Launch l(c, K_VOLKOV_INTEG_ROWS);
+                gk_volkov_integ_rows<F><<<dim3((L / 2 + kRows) / kRows, m), kRows * 32, sm_irows, c->stream>>>(
+                    b.qc, b.wq, b.tq);
+            }
+            {
+                Launch l(c, K_VOLKOV_INTEG_COLS);
+                gk_volkov_integ_cols<F><<<dim3(cols, m), kCols * 32, sm_icols, c->stream>>>(b.tq, b.phase, b.wq,
+                                                                                          b.unwrapped);
+            }
+            unw = b.unwrapped;
+        }
+        launch_aber_fit(c, unw, m);
+        if (form) launch_form(c, unw, g0, m);
+        if (dbg_phase)
+            cudaMemcpyAsync(dbg_phase + (g0 - a0) * FF, b.phase, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+        if (dbg_unwrapped)
+            cudaMemcpyAsync(dbg_unwrapped + (g0 - a0) * FF, unw, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+        if (dbg_amp)
+            cudaMemcpyAsync(dbg_amp + (g0 - a0) * FF, b.amp, m * FF * sizeof(float), cudaMemcpyDefault, c->stream);
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+template <int F>
+int gcap_impl(tdm_ctx* c, int a0, int n, bool form) {
+    Buffers& b = c->b;
+    const size_t sm_rows = warp_arrays(F, kRows), sm_cols = warp_arrays(F, kCols);
+    if (allow_smem(gk_cap_rows<F, false>, sm_rows) || allow_smem(gk_cap_rows<F, true>, sm_rows) ||
+        allow_smem(gk_cap_cols<F>, sm_cols))
+        return TDM_ECUDA;
+    if (form && n > c->chunk) return TDM_EINVAL;  // the chunk buffers hold one chunk
+    const size_t FF = (size_t)F * F;
+    const unsigned rows = (F + kRows - 1) / kRows, cols = (F + kCols - 1) / kCols;
+    for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
+        const int m = a0 + n - g0 < c->chunk ? a0 + n - g0 : c->chunk;
+        {
+            Launch l(c, K_CAP_ROWS);
+            if (form)
+                gk_cap_rows<F, true><<<dim3(rows, m), kRows * 32, sm_rows, c->stream>>>(
+                    nullptr, c->p.deroul ? b.unwrapped : b.phase, b.amp, b.beta, c->p.born, b.tuk_f, c->tuk_f_flat,
+                    b.wq, b.fields + g0 * FF, b.r1);
+            else
+                gk_cap_rows<F, false><<<dim3(rows, m), kRows * 32, sm_rows, c->stream>>>(
+                    b.fields + g0 * FF, nullptr, nullptr, nullptr, 0, b.tuk_f, c->tuk_f_flat, b.wq, nullptr, b.r1);
+        }
+        {
+            Launch l(c, K_CAP_COLS);
+            gk_cap_cols<F><<<dim3(cols, m), kCols * 32, sm_cols, c->stream>>>(b.r1, b.posspec + g0, b.s_tab, b.s_tabf,
+                                                                            c->p, b.wq, b.rec + g0 * FF, b.err);
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
+}
+
+}  // namespace
+
+// 2 NXMAX of the reference's own configuration (NXMAX 125); add a size here
+// (and to generic_field_size) to compile the passes for it.
+bool generic_field_size(int F) { return F == 250; }
+
+int launch_fields_generic(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp,
+                          int argparts, bool form) {
+    switch (c->p.F) {
+        case 250: return gfields_impl<250>(c, a0, n, dbg_phase, dbg_unwrapped, dbg_amp, argparts, form);
+        default: return TDM_EUNSUPPORTED;
+    }
+}
+
+int launch_cap_generic(tdm_ctx* c, int a0, int n, bool form) {
+    switch (c->p.F) {
+        case 250: return gcap_impl<250>(c, a0, n, form);
+        default: return TDM_EUNSUPPORTED;
+    }
+}
+
+}  // namespace tdm

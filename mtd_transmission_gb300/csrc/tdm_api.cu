@@ -78,7 +78,7 @@ int dev_alloc(tdm_ctx* c, T** p, size_t count) {
 
 void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
-    void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.holo_stage, b.inter, b.spectra, b.posspec,
+    void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0], b.rec_buf[1], b.posspec_vol[0],
                     b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
@@ -171,8 +171,8 @@ int check_geom(const tdm_geom* g, std::string& why) {
         return TDM_EUNSUPPORTED;
     }
     const int F = 2 * g->nxmax;
-    if (!is_pow2(F) || F < 64 || F > 512) {
-        why = "2*NXMAX must be a power of two in [64, 512]";
+    if (!((is_pow2(F) && F >= 64 && F <= 512) || generic_field_size(F))) {
+        why = "2*NXMAX must be a power of two in [64, 512] or 250";
         return TDM_EUNSUPPORTED;
     }
     if (!is_pow2(g->dim_final) || g->dim_final < 4 * g->nxmax || g->dim_final > 1024 || g->dim_final < 128) {
@@ -351,6 +351,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.tuk_f, F));
     TRY(dev_alloc(c, &b.s_tab, FF));
     TRY(dev_alloc(c, &b.s_tabf, FF));
+    TRY(dev_alloc(c, &b.wq, 4 * F));
     TRY(dev_alloc(c, &b.holo_stage, 2 * CH * p.H * p.H * 2));
     TRY(dev_alloc(c, &b.inter, CH * p.H * F));
     TRY(dev_alloc(c, &b.spectra, M * FF));
@@ -385,11 +386,17 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     c->tuk_f_flat = tukey_flat(F, 0.1f);
     std::vector<float> thf(th.begin(), th.end()), tff(tf.begin(), tf.end());
     std::vector<float> stabf(stab.begin(), stab.end());
+    std::vector<float2> wq(4 * F);  // exp(-2 pi i k / 4F), for the mixed-radix passes
+    for (int k = 0; k < 4 * F; ++k) {
+        const double ang = -2.0 * M_PI * (double)k / (4.0 * F);
+        wq[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+    }
     if (cudaMemcpy(b.tw, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.tuk_h, thf.data(), p.H * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.tuk_f, tff.data(), F * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tab, stab.data(), FF * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tabf, stabf.data(), FF * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.wq, wq.data(), 4 * F * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(b.err, 0, 4 * sizeof(int)) != cudaSuccess ||
         cudaMemset(b.fit_done, 0, CH * 2 * sizeof(unsigned)) != cudaSuccess)
         TRY(cuda_fail(c, cudaGetLastError(), "table upload"));

@@ -41,6 +41,7 @@ struct Buffers {
     float* tuk_f = nullptr;        // F, field Tukey alpha 0.1 (1D factor)
     double* s_tab = nullptr;       // F*F, sqrt(rayon^2 - fd^2) at [fdy+N][fdx+N]
     float* s_tabf = nullptr;       // float copy
+    float2* wq = nullptr;          // 4F, exp(-2 pi i k / 4F): twiddles of the mixed-radix passes
     uint8_t* holo_stage = nullptr; // host staging: 2 x chunk x H*H*2 bytes
     float2* inter = nullptr;       // chunk x F x H (extraction row pass, kx band column-major)
     float2* spectra = nullptr;     // max_angles x F*F
@@ -185,6 +186,19 @@ int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrap
 // are formed from the chunk's unwrapped phase, amplitude and fits on the fly
 // (and stored in b.fields).
 int launch_cap(tdm_ctx* c, int a0, int n, bool form = false);
+// The same two stages for field sizes that are not powers of two (the
+// mixed-radix engine, fft_generic.cuh; k_generic.cu).
+int launch_fields_generic(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp,
+                          int argparts, bool form);
+int launch_cap_generic(tdm_ctx* c, int a0, int n, bool form);
+// Field sizes the mixed-radix passes are compiled for (2 NXMAX, not powers of two).
+bool generic_field_size(int F);
+// Pieces of the field stage shared by both engines (k_fields.cu): the
+// standalone specular-search partials of m spectra (returns the records per
+// angle), the aberration fits and the field formation of the chunk's m angles.
+int launch_argmax_part(tdm_ctx* c, const float2* spec, int m);
+void launch_aber_fit(tdm_ctx* c, const float* unw, int m);
+void launch_form(tdm_ctx* c, const float* unw, int g0, int m);
 // Outputs of the volume stage: the device buffers the kernels write and, for
 // each caller buffer in host memory, the host destination its device copy is
 // downloaded to on the copy stream as soon as the pass that completes it has

@@ -111,6 +111,15 @@ def workload(name: str) -> tuple[Acquisition, Phantom, int]:
             Ellipsoid((0.01, 0.07, -0.02), (0.14, 0.12, 0.12), 0.01, 0.0, smooth=True),
         ], phase_max=40.0)
         return acq, ph, 1
+    if name == "tomo_config_1024":    # the reference's Tomo_config: 500 x 1024^2, NXMAX 125, CIRCLE 247,777, 512^3
+        acq = Acquisition(ccd_roix=1024, nxmax=125, circle_cx=247, circle_cy=777, dim_final=512, nb_holo=500,
+                          na=1.40, n0=1.515, lambda0=632e-9, f_tube=0.15, f_obj=0.002, tpcam=5.5e-6, rf=0.75,
+                          born=0)
+        ph = Phantom([
+            Ellipsoid((-0.05, 0.02, 0.0), (0.22, 0.17, 0.15), 0.03, 0.003, smooth=True),
+            Ellipsoid((0.06, -0.04, 0.02), (0.16, 0.21, 0.14), 0.05, 0.005, smooth=True),
+        ], phase_max=30.0)
+        return acq, ph, 5
     if name == "large_2048":          # 1000 x 2048^2, NXMAX 256, 1024^3
         acq = Acquisition(ccd_roix=2048, nxmax=256, circle_cx=512, circle_cy=512, dim_final=1024,
                           nb_holo=1000, born=1)

@@ -200,3 +200,25 @@ def test_gather_angle_limit_refused_at_create():
     with pytest.raises(api.TdmError) as e:
         api.Context(g, 40000)
     assert e.value.status == api.STATUS_CODES["TDM_EUNSUPPORTED"]
+
+
+def test_reference_configuration_geometry():
+    """tdm_read_geom on the reference's own Tomo_config gives the committed
+    geometry (tests/golden/tomo_config_geometry.json), and the
+    tomo_config_1024 workload is that geometry."""
+    import json
+    golden_path = os.path.join(os.path.dirname(__file__), "golden", "tomo_config_geometry.json")
+    with open(golden_path) as f:
+        golden = json.load(f)
+    root = "/root/reference"
+    if os.path.isdir(os.path.join(root, "Tomo_config")):
+        sys_path = os.path.join(os.path.dirname(__file__), "golden")
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("mk", os.path.join(sys_path, "make_tomo_config_geometry.py"))
+        mk = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mk)
+        assert mk.parse(root) == golden
+    acq, _, _ = simul.workload("tomo_config_1024")
+    g = Geometry.from_acquisition(acq)
+    for k, v in golden.items():
+        assert getattr(g, k) == v, k
