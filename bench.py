@@ -88,6 +88,12 @@ STAGE_KERNELS = {
 }
 
 
+# Stage of each kernel, for the dominant kernel's roofline: its achieved
+# bandwidth is the stage's per-unit algorithmic bytes (above) times the units
+# its launches process, over its own launch time.
+KERNEL_STAGE = {k: st for st, ks in STAGE_KERNELS.items() for k in ks}
+
+
 def stage_bytes(acq, hits_per_angle):
     H, F, D, M = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final, acq.nb_holo
     return {
@@ -118,21 +124,23 @@ def stage_roofline(acq, hits_per_angle, kern_ms, step_ms, peak):
     return out
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the kernel
-# (profiles/<kernel>_rytov_1024_*.md): the row pass and the Volkov passes on
-# the 64-hologram case (a launch processes 16 angles in every case), the
-# gather on the 600-hologram case; the gather's read traffic grows with the
-# angles (scaled by angles/600), its write traffic (the band planes) does not.
+# DRAM bytes (read + write) per launch from the committed ncu capture of
+# the kernel on this code (the file named in the returned source): the row
+# pass on the 64-hologram case (a launch processes 16 holograms), the gather
+# on the 600-hologram case (its record reads grow with the angles, scaled by
+# angles/600; its band writes do not).  None where no capture of this
+# workload's kernel is committed.
+NCU_TRAFFIC = {
+    "extract_rows": (33.616128e6 + 0.341504e6, 0.0, "profiles/k_extract_rows_rytov_1024_64holos.md"),
+    "gather": (419.033088e6, 648.724224e6, "profiles/k_accumulate_rytov_1024_600holos.md"),
+}
+
+
 def ncu_traffic_per_launch(name, acq):
-    if acq.ccd_roix != 1024 or acq.nxmax != 128 or acq.dim_final != 512:
-        return None
-    if name == "volkov_cols":
-        return 16.83968e6 + 0.001024e6
-    if name == "extract_rows":
-        return 33.616128e6 + 0.341504e6
-    if name == "gather":
-        return 648.724224e6 * acq.nb_holo / 600 + 419.033088e6
-    return None
+    if acq.ccd_roix != 1024 or acq.nxmax != 128 or acq.dim_final != 512 or name not in NCU_TRAFFIC:
+        return None, None
+    fixed, per600, src = NCU_TRAFFIC[name]
+    return fixed + per600 * acq.nb_holo / 600, src
 
 
 def measured_peaks():
@@ -674,18 +682,21 @@ def main():
         roof = None
         if dom:
             t_step_ms, n_launch = kern[dom]
-            if dom in per_angle:
-                bytes_step = per_angle[dom] * M
-            else:
-                bytes_step = per_volume.get(dom, 0)
+            stage = KERNEL_STAGE.get(dom)
+            bytes_step = stage_bytes(acq, hits)[stage] if stage else 0
             achieved = bytes_step / (t_step_ms / 1e3) / 1e9
-            traffic = ncu_traffic_per_launch(dom, acq)
-            roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4),
+            traffic, traffic_src = ncu_traffic_per_launch(dom, acq)
+            roof = {"kernel": dom, "stage": stage, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                    "unit": "GB/s", "frac": round(achieved / peak, 4),
                     "traffic": round(traffic / 1e6, 3) if traffic else None,
                     "traffic_unit": "MB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                    "traffic_source": traffic_src,
+                    "algorithmic_bytes": "the stage's per-unit bytes (extraction: H^2 2 + F^2 8 per hologram; "
+                                         "fields: 2 F^2 8 per angle; cap mapping: F^2 8 + 24 hits per angle; "
+                                         "volume: 32 D^3) times the units of the kernel's launches",
                     "algorithmic_bytes_per_launch_mb": round(bytes_step / max(n_launch, 1) / 1e6, 3),
-                    "peak_source": f"{peak_kind} hbm_gbs",
+                    "peak_source": f"{peak_kind} hbm_gbs (of measured)" if peak_kind == "measured"
+                    else f"{peak_kind} (of fallback)",
                     "launches_per_step": n_launch, "ms_per_step": round(t_step_ms, 4),
                     "algorithmic_bytes_per_step": int(bytes_step)}
         # every kernel with algorithmic bytes: achieved GB/s and fraction of the HBM peak

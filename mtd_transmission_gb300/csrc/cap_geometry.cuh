@@ -24,12 +24,15 @@ __device__ __forceinline__ double cap_fzm0(const Params& p, int2 ps) {
 // fzf = (float)fz, converted once by the caller: FP64 instructions run at a
 // small fraction of the FP32 rate on this GPU, so the per-bin path is FP32
 // and FP64 is used only in the rare rounding-boundary branch.
-__device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, float fzf, int kx, int ky,
-                                         const double* __restrict__ s_tab, const float* __restrict__ s_tabf,
-                                         float* sf, int* __restrict__ err) {
+// The plane of cap pixel fd = (fdx, fdy) (|fd|^2 below the disc threshold)
+// for an angle of height fz (fzf = (float)fz); fz_of() gives fz in FP64, and
+// is called only near a rounding boundary.  -1 (and *err set) when the plane
+// lies outside the cap band.
+template <class FzOf>
+__device__ __forceinline__ int cap_plane_fd(const Params& p, int fdx, int fdy, float fzf, FzOf&& fz_of,
+                                            const double* __restrict__ s_tab, const float* __restrict__ s_tabf,
+                                            float* sf, int* __restrict__ err) {
     const int F = p.F, N = p.N;
-    const int fdx = wrap_f(kx + ps.x, F) - N, fdy = wrap_f(ky + ps.y, F) - N;
-    if (!(fzf >= 0.0f) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;  // fz is sqrt(c) >= 0 or -1
     const int ti = (fdy + N) * F + fdx + N;
     // sqrt(r^2 - fd^2) in float: computed from the exact integer when r^2 < 2^24 (equal to the table)
     *sf = p.r2i ? __fsqrt_rn((float)(p.r2i - fdx * fdx - fdy * fdy)) : s_tabf[ti];
@@ -41,7 +44,7 @@ __device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, fl
     if (fabsf(fr - 0.5f) > 1e-3f) {
         koz = floorf(d + 0.5f);
     } else {
-        koz = (float)round(s_tab[ti] - fz);
+        koz = (float)round(s_tab[ti] - fz_of());
     }
     const int z = (int)koz + p.D / 2;
     if (z < p.zmin || z >= p.zmin + p.band) {
@@ -49,6 +52,15 @@ __device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, fl
         return -1;
     }
     return z;
+}
+
+__device__ __forceinline__ int cap_plane(const Params& p, int2 ps, double fz, float fzf, int kx, int ky,
+                                         const double* __restrict__ s_tab, const float* __restrict__ s_tabf,
+                                         float* sf, int* __restrict__ err) {
+    const int F = p.F, N = p.N;
+    const int fdx = wrap_f(kx + ps.x, F) - N, fdy = wrap_f(ky + ps.y, F) - N;
+    if (!(fzf >= 0.0f) || fdx * fdx + fdy * fdy >= p.disc_thr) return -1;  // fz is sqrt(c) >= 0 or -1
+    return cap_plane_fd(p, fdx, fdy, fzf, [&] { return fz; }, s_tab, s_tabf, sf, err);
 }
 
 // Cap-cell weight (k0/pi)(-2pi) sdz dx^2 (-1)^(kx+ky) of retroPropag_Born

@@ -382,12 +382,12 @@ gk_cap_rows(const float2* __restrict__ fields_in, const float* __restrict__ unwr
     for (int k = lane; k < F; k += 32) r1[row + k] = A[k];
 }
 
-// Column pass: forward FFT along y, then per bin the cap record
-// (contribution, plane) as k_cap_cols writes it.
+// Column pass: forward FFT along y, then per bin the cap value (contribution
+// on the cap cells, 0 elsewhere) as k_cap_cols writes it.
 template <int F>
 __global__ void __launch_bounds__(kCols * 32)
 gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ s_tab,
-            const float* __restrict__ s_tabf, Params p, const float2* __restrict__ wq, float4* __restrict__ rec,
+            const float* __restrict__ s_tabf, Params p, const float2* __restrict__ wq, float2* __restrict__ rec,
             int* __restrict__ err) {
     extern __shared__ float2 sm[];
     __shared__ double s_fz;
@@ -416,7 +416,7 @@ gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, con
             const float Bc = cap_weight(p, sf, ir, kx, ky);
             val = make_float2(-Bc * v.y, Bc * v.x);
         }
-        rec[o] = make_float4(val.x, val.y, __int_as_float(z), 0.f);
+        rec[o] = val;
     }
 }
 

@@ -81,7 +81,7 @@ void free_all(tdm_ctx* c) {
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0], b.rec_buf[1], b.posspec_vol[0],
-                    b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
+                    b.posspec_vol[1], b.cap_fzd, b.cap_fzf, b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
                     b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit, b.ref_inv};
     for (void* p : ptrs)
@@ -375,6 +375,8 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.rec_buf[1], M * FF));
     TRY(dev_alloc(c, &b.posspec_vol[0], M));
     TRY(dev_alloc(c, &b.posspec_vol[1], M));
+    TRY(dev_alloc(c, &b.cap_fzd, M));
+    TRY(dev_alloc(c, &b.cap_fzf, M));
     b.rec = b.rec_buf[0];
     TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
@@ -679,7 +681,7 @@ int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_o
 // first); outputs may be host or device memory.  Host outputs are written to
 // device staging buffers and downloaded while the later passes run.
 static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt,
-                      bool wait = true, cudaStream_t st = nullptr, const float4* rec = nullptr,
+                      bool wait = true, cudaStream_t st = nullptr, const float2* rec = nullptr,
                       const int2* posspec = nullptr, cudaEvent_t ev_gathered = nullptr) {
     const Params& p = c->p;
     const size_t NT = (size_t)p.D * p.D * p.D;
