@@ -337,6 +337,15 @@ int tdm_pgm_info(const char* path, int* width, int* height, int* maxval);
 int tdm_write_tiff_f32(const char* path, const float* vol, int dim_x, int dim_y, int pages, double pixel_size,
                        int orientation);
 
+/* HDF5 file of a complex volume, as the polarisation mode of the reference's
+ * reconstruction writes it (save_complex_volume_hdf5,
+ * Reconstruction/src/IO_functions.cpp:52-82, called at Reconstruction/main.cpp:360-363):
+ * group "/indice_complexe" with float32 datasets "Re" and "Im" of dimensions
+ * (nz, ny, nx), x fastest in re and im.  A minimal writer of the HDF5 format
+ * (superblock version 0, symbol-table groups, contiguous datasets); no
+ * library. */
+int tdm_write_hdf5_complex(const char* path, const float* re, const float* im, int nx, int ny, int nz);
+
 #ifdef __cplusplus
 }
 #endif

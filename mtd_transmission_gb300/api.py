@@ -30,6 +30,7 @@ EXPORTS = (
     "tdm_extract_noalloc", "tdm_pipeline_async", "tdm_cap_planes", "tdm_forward", "tdm_adjoint",
     "tdm_tv_reconstruct", "tdm_batch_create", "tdm_batch_launch", "tdm_batch_destroy", "tdm_autotune",
     "tdm_join", "tdm_set_schedule", "tdm_set_reference_intensity", "tdm_set_wait_limit",
+    "tdm_write_hdf5_complex",
 )
 
 
@@ -128,6 +129,7 @@ def lib():
     L.tdm_read_pgm.argtypes = [ctypes.c_char_p, I, P, ctypes.POINTER(I)]
     L.tdm_pgm_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
     L.tdm_write_tiff_f32.argtypes = [ctypes.c_char_p, P, I, I, I, D, I]
+    L.tdm_write_hdf5_complex.argtypes = [ctypes.c_char_p, P, P, I, I, I]
     L.tdm_extract_noalloc.argtypes = [ctypes.POINTER(Geometry), P, I, I, P, P]
     L.tdm_profile.argtypes = [P, I]
     L.tdm_profile_count.argtypes = []
@@ -417,6 +419,16 @@ def write_tiff(path: str, vol: np.ndarray, pixel_size: float, orientation: int =
         v = v[None]
     pages, hgt, wdt = v.shape
     rc = lib().tdm_write_tiff_f32(path.encode(), ptr(v), wdt, hgt, pages, pixel_size, orientation)
+    if rc != TDM_OK:
+        raise TdmError(rc, f"cannot write {path}")
+
+
+def write_hdf5_complex(path: str, re: np.ndarray, im: np.ndarray):
+    """tdm_write_hdf5_complex: /indice_complexe/{Re,Im} float32 (nz, ny, nx)."""
+    r = np.ascontiguousarray(re, np.float32)
+    i = np.ascontiguousarray(im, np.float32)
+    nz, ny, nx = r.shape
+    rc = lib().tdm_write_hdf5_complex(path.encode(), ptr(r), ptr(i), nx, ny, nz)
     if rc != TDM_OK:
         raise TdmError(rc, f"cannot write {path}")
 

@@ -83,13 +83,17 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
     os.makedirs(BIN, exist_ok=True)
     gxx = shutil.which("g++") or "g++"
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
     for app in APPS:
         src = os.path.join(CSRC, "apps", app + ".cpp")
         exe = os.path.join(BIN, app)
         common = os.path.join(CSRC, "apps", "app_common.h")
         if os.path.exists(src) and (force or _stale(exe, [src, LIB, common])):
+            # tomo_pipeline holds the polarisation states' buffers in device memory (CUDA runtime)
+            cu = ["-I", os.path.join(cuda, "include"), "-L", os.path.join(cuda, "lib64"), "-lcudart"] \
+                if app == "tomo_pipeline" else []
             _run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", src, "-o", exe, "-I", os.path.join(HERE, "..", "include"),
-                  "-L", HERE, "-ltdm", "-Wl,-rpath,$ORIGIN/.."])
+                  "-L", HERE, "-ltdm"] + cu + ["-Wl,-rpath,$ORIGIN/.."])
     return LIB
 
 

@@ -18,39 +18,95 @@
 namespace app {
 
 struct Paths {
-    std::string config, result, acquis;
+    std::string config, result, acquis, racine, mask;
 };
 
-// "-polar" / "-etat S" / "--help" as in pretraitement_hors_axe_CPU/main.cpp:37-61
-// and Reconstruction/main.cpp:63-86.  Polarisation mode is not supported.
-inline int parse_args(int argc, char** argv, const char* prog) {
+// Command line of pretraitement_hors_axe_CPU/main.cpp:37-61 and
+// Reconstruction/main.cpp:63-86: "-polar" (polarisation mode), "-etat S" (one
+// of the four states /LC/polar0/, /LC/polar90/, /RC/polar0/, /RC/polar90/),
+// "--help".  Either option selects $HOME/.config/gui_tomo_polar.conf; as in
+// the reference, any other argument selects gui_tomo.conf again.
+struct Args {
+    bool help = false, polar = false;
+    std::string etat, gui = "gui_tomo.conf";
+    std::vector<std::string> rest;
+};
+
+inline Args parse_args(int argc, char** argv) {
+    Args a;
     for (int i = 1; i < argc; ++i) {
-        std::string a = argv[i];
-        if (a == "--help") {
-            std::printf("%s: GB300 build of %s\n  -polar, -etat S : polarisation mode (not supported)\n", prog, prog);
-            return 1;
-        }
-        if (a == "-polar" || a == "-etat") {
-            std::fprintf(stderr, "%s: polarisation mode (-polar/-etat) is not supported\n", prog);
-            return 2;
+        const std::string s = argv[i];
+        if (s == "--help") {
+            a.help = true;
+        } else if (s == "-polar") {
+            a.polar = true;
+            a.gui = "gui_tomo_polar.conf";
+        } else if (s == "-etat" && i + 1 < argc) {
+            a.etat = argv[++i];
+            a.gui = "gui_tomo_polar.conf";
+        } else {
+            a.gui = "gui_tomo.conf";
+            a.rest.push_back(s);
         }
     }
-    return 0;
+    return a;
 }
 
-// $HOME/.config/gui_tomo.conf -> CHEMIN_CONFIG, CHEMIN_RESULT, CHEMIN_ACQUIS
-// (pretraitement_hors_axe_CPU/manip.cpp:14-29).
-inline bool read_paths(Paths& p) {
+inline void print_help(const char* prog) {
+    std::printf("%s (GB300)\n-polar : mode polar\n-etat : indiquez un des 4 etats :\n/LC/polar0/\n/LC/polar90/\n"
+                "/RC/polar0/\n/RC/polar90/\n", prog);
+}
+
+inline std::string gui_key(const std::string& gui, const char* key) {
+    char buf[4096];
+    return tdm_extract_string(gui.c_str(), key, buf, sizeof buf) == 1 ? std::string(buf) : std::string();
+}
+
+// Paths of the preprocessing (pretraitement_hors_axe_CPU/manip.cpp:14-29,
+// main.cpp:63-80): in polarisation mode the acquisitions are
+// CHEMIN_RACINE/demosaic<etat>, the results <that>/UBorn/ and the mask
+// CHEMIN_RACINE/Image_mask.pgm.
+inline bool read_paths(const Args& a, Paths& p) {
     const char* home = std::getenv("HOME");
     if (!home) return false;
-    std::string gui = std::string(home) + "/.config/gui_tomo.conf";
-    char buf[4096];
-    if (tdm_extract_string(gui.c_str(), "CHEMIN_CONFIG", buf, sizeof buf) != 1) return false;
-    p.config = buf;
-    if (tdm_extract_string(gui.c_str(), "CHEMIN_RESULT", buf, sizeof buf) == 1) p.result = std::string(buf) + "/";
-    if (tdm_extract_string(gui.c_str(), "CHEMIN_ACQUIS", buf, sizeof buf) == 1) p.acquis = std::string(buf) + "/";
+    const std::string gui = std::string(home) + "/.config/" + a.gui;
+    p.config = gui_key(gui, "CHEMIN_CONFIG");
+    if (p.config.empty()) return false;
+    p.result = gui_key(gui, "CHEMIN_RESULT") + "/";
+    p.acquis = gui_key(gui, "CHEMIN_ACQUIS") + "/";
+    p.racine = gui_key(gui, "CHEMIN_RACINE") + "/";
+    if (a.polar) {
+        p.acquis = p.racine + "demosaic" + a.etat + "/";
+        p.result = p.racine + "demosaic" + a.etat + "/UBorn/";
+        p.mask = p.racine + "Image_mask.pgm";
+    } else {
+        p.mask = p.acquis + "Image_mask.pgm";
+    }
     return true;
 }
+
+// Paths of the reconstruction (Reconstruction/src/manip.cpp:10-30): in
+// polarisation mode the configuration files and the results are both in
+// CHEMIN_RACINE/demosaic/<etat>UBorn/.
+inline bool read_paths_recon(const Args& a, Paths& p) {
+    const char* home = std::getenv("HOME");
+    if (!home) return false;
+    const std::string gui = std::string(home) + "/.config/" + a.gui;
+    p.acquis = gui_key(gui, "CHEMIN_ACQUIS");
+    if (a.polar) {
+        p.racine = gui_key(gui, "CHEMIN_RACINE");
+        p.config = p.racine + "/demosaic/" + a.etat + "UBorn/";
+        p.result = p.config;
+    } else {
+        p.result = gui_key(gui, "CHEMIN_RESULT") + "/";
+        p.config = gui_key(gui, "CHEMIN_CONFIG");
+        if (p.config.empty()) return false;
+    }
+    return true;
+}
+
+// The four states of the polarisation set-up (pretraitement_hors_axe_CPU/main.cpp:42-46).
+inline std::vector<std::string> polar_states() { return {"/LC/polar0/", "/LC/polar90/", "/RC/polar0/", "/RC/polar90/"}; }
 
 inline bool file_exists(const std::string& f) {
     struct stat st;

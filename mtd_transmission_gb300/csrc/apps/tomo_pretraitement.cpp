@@ -5,13 +5,19 @@
 //           CHEMIN_CONFIG/recon.txt and config_manip.txt
 //   outputs CHEMIN_RESULT/UBornfinal_{Re,Im}{2N}x{2N}x{M}.raw (FP64, angle-major),
 //           parametres.raw, tab_posSpec.raw, centres.tif, SAV_param_manip.txt
+// -polar -etat S: one state of the polarisation set-up, acquisitions in
+// CHEMIN_RACINE/demosaic<S>, results in <that>/UBorn/ (main.cpp:63-80).
 #include "app_common.h"
 
 int main(int argc, char** argv) {
-    if (int r = app::parse_args(argc, argv, "tomo_pretraitement")) return r == 1 ? 0 : r;
+    const app::Args A = app::parse_args(argc, argv);
+    if (A.help) {
+        app::print_help("tomo_pretraitement");
+        return 0;
+    }
     app::Paths P;
-    if (!app::read_paths(P)) {
-        std::fprintf(stderr, "cannot read $HOME/.config/gui_tomo.conf\n");
+    if (!app::read_paths(A, P)) {
+        std::fprintf(stderr, "cannot read $HOME/.config/%s\n", A.gui.c_str());
         return 1;
     }
     const std::string recon = P.config + "/recon.txt", manip = P.config + "/config_manip.txt";
@@ -33,7 +39,7 @@ int main(int argc, char** argv) {
     }
     tdm_ctx* c = nullptr;
     if (app::check(tdm_create(&g, ok, &c), c, "tdm_create")) return 1;
-    if (app::check(app::load_mask(c, P.acquis + "Image_mask.pgm", F), c, "tdm_set_mask")) return 1;
+    if (app::check(app::load_mask(c, P.mask, F), c, "tdm_set_mask")) return 1;
     std::vector<float> fields((size_t)ok * F * F * 2);
     std::vector<int32_t> pos(2 * (size_t)ok);
     if (app::check(tdm_extract(c, holos.data(), 16, ok, nullptr), c, "tdm_extract")) return 1;

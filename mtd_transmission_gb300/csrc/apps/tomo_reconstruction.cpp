@@ -5,13 +5,20 @@
 //           CHEMIN_CONFIG/recon.txt and config_manip.txt
 //   outputs indice.tif, absorption.tif, OTF3D.tif (EXPORT_OTF), centre_reconstruction.tif,
 //           slice.tiff
+// -polar -etat S: configuration and results in CHEMIN_RACINE/demosaic/<S>UBorn/,
+// the volume as indice_cplx_hdf5.hdf instead of the two TIFF volumes
+// (Reconstruction/src/manip.cpp:18-30, main.cpp:358-367).
 #include "app_common.h"
 
 int main(int argc, char** argv) {
-    if (int r = app::parse_args(argc, argv, "tomo_reconstruction")) return r == 1 ? 0 : r;
+    const app::Args A = app::parse_args(argc, argv);
+    if (A.help) {
+        app::print_help("tomo_reconstruction");
+        return 0;
+    }
     app::Paths P;
-    if (!app::read_paths(P)) {
-        std::fprintf(stderr, "cannot read $HOME/.config/gui_tomo.conf\n");
+    if (!app::read_paths_recon(A, P)) {
+        std::fprintf(stderr, "cannot read $HOME/.config/%s\n", A.gui.c_str());
         return 1;
     }
     const std::string recon = P.config + "/recon.txt", manip = P.config + "/config_manip.txt";
@@ -73,8 +80,15 @@ int main(int argc, char** argv) {
         for (size_t i = 0; i < NT; ++i) of[i] = otf[i];
         tdm_write_tiff_f32((P.result + "OTF3D.tif").c_str(), of.data(), D, D, D, dv.tp_tomo, 4);
     }
-    if (tdm_write_tiff_f32((P.result + "indice.tif").c_str(), vre.data(), D, D, D, dv.tp_tomo, 4) != TDM_OK ||
-        tdm_write_tiff_f32((P.result + "absorption.tif").c_str(), vim.data(), D, D, D, dv.tp_tomo, 4) != TDM_OK) {
+    if (A.polar) {
+        if (tdm_write_hdf5_complex((P.result + "/indice_cplx_hdf5.hdf").c_str(), vre.data(), vim.data(), D, D, D) !=
+            TDM_OK) {
+            std::fprintf(stderr, "cannot write %s/indice_cplx_hdf5.hdf\n", P.result.c_str());
+            return 1;
+        }
+    } else if (tdm_write_tiff_f32((P.result + "indice.tif").c_str(), vre.data(), D, D, D, dv.tp_tomo, 4) != TDM_OK ||
+               tdm_write_tiff_f32((P.result + "absorption.tif").c_str(), vim.data(), D, D, D, dv.tp_tomo, 4) !=
+                   TDM_OK) {
         std::fprintf(stderr, "cannot write the volumes in %s\n", P.result.c_str());
         return 1;
     }

@@ -306,3 +306,198 @@ int tdm_write_tiff_f32(const char* path, const float* vol, int wdt, int hgt, int
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- HDF5
+// A minimal HDF5 file (format specification, superblock version 0) holding
+// the polarisation mode's volume as save_complex_volume_hdf5 writes it
+// (Reconstruction/src/IO_functions.cpp:52-82): group "/indice_complexe" with
+// the float32 datasets "Re" and "Im" of dimensions (Nz, Ny, Nx).  Offsets and
+// lengths are 8 bytes; groups are symbol tables (a version-1 B-tree of group
+// nodes, one symbol table node, a local heap of names); dataset object
+// headers (version 1) carry the dataspace, datatype (IEEE float32, little
+// endian), fill-value (version 2, undefined) and contiguous layout (version 3)
+// messages; the raw data follow the metadata.
+namespace {
+
+constexpr uint64_t kUndef = ~0ull;
+constexpr int kGroupLeafK = 4, kGroupNodeK = 16;
+
+struct H5Buf {
+    std::vector<uint8_t> b;
+    size_t pos() const { return b.size(); }
+    void u8(uint32_t v) { b.push_back((uint8_t)v); }
+    void u16(uint32_t v) { for (int i = 0; i < 2; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void u32(uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void u64(uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void bytes(const char* s, size_t n) { b.insert(b.end(), s, s + n); }
+    void zeros(size_t n) { b.insert(b.end(), n, 0); }
+    void align8() { while (b.size() % 8) b.push_back(0); }
+    void put64(size_t at, uint64_t v) { for (int i = 0; i < 8; ++i) b[at + i] = (uint8_t)(v >> (8 * i)); }
+};
+
+// Version-1 object header with the given messages (type, data); returns its address.
+size_t h5_object_header(H5Buf& f, const std::vector<std::pair<int, std::vector<uint8_t>>>& msgs) {
+    f.align8();
+    const size_t at = f.pos();
+    size_t body = 0;
+    for (const auto& m : msgs) body += 8 + ((m.second.size() + 7) & ~size_t(7));
+    f.u8(1);                        // version
+    f.u8(0);                        // reserved
+    f.u16((uint32_t)msgs.size());   // number of header messages
+    f.u32(1);                       // object reference count
+    f.u32((uint32_t)body);          // object header size
+    f.u32(0);                       // alignment of the messages to 8 bytes
+    for (const auto& m : msgs) {
+        const size_t n = (m.second.size() + 7) & ~size_t(7);
+        f.u16((uint32_t)m.first);
+        f.u16((uint32_t)n);
+        f.u8(0);                    // flags
+        f.zeros(3);
+        f.b.insert(f.b.end(), m.second.begin(), m.second.end());
+        f.zeros(n - m.second.size());
+    }
+    return at;
+}
+
+// Symbol table entry (link name offset, object header address, cache type, scratch).
+void h5_entry(H5Buf& f, uint64_t name_off, uint64_t ohdr, uint32_t cache, uint64_t btree = 0, uint64_t heap = 0) {
+    f.u64(name_off);
+    f.u64(ohdr);
+    f.u32(cache);
+    f.u32(0);
+    f.u64(btree);
+    f.u64(heap);
+}
+
+struct H5Group {
+    size_t heap = 0, btree = 0, snod = 0;
+    std::vector<uint64_t> name_off;  // heap offsets of the members' names, in the order given
+};
+
+// Local heap of the member names ("" at offset 0), the B-tree with one child
+// and the symbol table node; member object header addresses are patched in
+// later through snod_entry_at().  names must be in ascending order.
+H5Group h5_group_tables(H5Buf& f, const std::vector<std::string>& names) {
+    H5Group g;
+    std::vector<uint8_t> data(8, 0);  // offset 0: the empty name
+    for (const auto& n : names) {
+        g.name_off.push_back(data.size());
+        data.insert(data.end(), n.begin(), n.end());
+        data.push_back(0);
+        while (data.size() % 8) data.push_back(0);
+    }
+    f.align8();
+    g.heap = f.pos();
+    f.bytes("HEAP", 4);
+    f.u8(0);
+    f.zeros(3);
+    f.u64(data.size());      // data segment size
+    f.u64(1);                // free list: none (1 ends a free list; the reference HDF5 library writes it for an empty list)
+    f.u64(f.pos() + 8);      // data segment address: right after this field
+    f.b.insert(f.b.end(), data.begin(), data.end());
+    f.align8();
+    g.btree = f.pos();
+    f.bytes("TREE", 4);
+    f.u8(0);                 // group nodes
+    f.u8(0);                 // leaf level
+    f.u16(1);                // entries used
+    f.u64(kUndef);           // left sibling
+    f.u64(kUndef);           // right sibling
+    f.u64(0);                // key 0: the empty name
+    const size_t child = f.pos();
+    f.u64(0);                // child 0: the symbol table node (patched below)
+    f.u64(g.name_off.empty() ? 0 : g.name_off.back());  // key 1: the last name
+    f.zeros((size_t)(2 * kGroupNodeK - 1) * 16);        // unused keys and children of the node
+    f.align8();
+    g.snod = f.pos();
+    f.put64(child, g.snod);
+    f.bytes("SNOD", 4);
+    f.u8(1);
+    f.u8(0);
+    f.u16((uint32_t)names.size());
+    for (size_t i = 0; i < names.size(); ++i) h5_entry(f, g.name_off[i], 0, 0);
+    f.zeros((size_t)(2 * kGroupLeafK - names.size()) * 40);
+    return g;
+}
+
+size_t snod_entry_at(const H5Group& g, size_t i) { return g.snod + 8 + i * 40; }
+
+std::vector<uint8_t> h5_msg_symbol_table(uint64_t btree, uint64_t heap) {
+    H5Buf m;
+    m.u64(btree);
+    m.u64(heap);
+    return m.b;
+}
+
+}  // namespace
+
+extern "C" int tdm_write_hdf5_complex(const char* path, const float* re, const float* im, int nx, int ny, int nz) {
+    if (!path || !re || !im || nx <= 0 || ny <= 0 || nz <= 0) return TDM_EINVAL;
+    const uint64_t n = (uint64_t)nx * ny * nz, bytes = n * 4;
+    H5Buf f;
+    // superblock (version 0), root entry patched below
+    f.bytes("\x89HDF\r\n\x1a\n", 8);
+    f.u8(0); f.u8(0); f.u8(0); f.u8(0);   // superblock, free space, root entry, reserved
+    f.u8(0); f.u8(8); f.u8(8); f.u8(0);   // shared header version, sizeof offsets, sizeof lengths, reserved
+    f.u16(kGroupLeafK);
+    f.u16(kGroupNodeK);
+    f.u32(0);                             // file consistency flags
+    f.u64(0);                             // base address
+    f.u64(kUndef);                        // free-space info
+    const size_t eof_at = f.pos();
+    f.u64(0);                             // end of file address (patched)
+    f.u64(kUndef);                        // driver information block
+    const size_t root_entry = f.pos();
+    h5_entry(f, 0, 0, 1);                 // patched below
+    // root group: one member, "indice_complexe"
+    const H5Group root = h5_group_tables(f, {"indice_complexe"});
+    const size_t root_oh = h5_object_header(f, {{0x0011, h5_msg_symbol_table(root.btree, root.heap)}});
+    // the group "/indice_complexe": members "Im", "Re" (ascending)
+    const H5Group grp = h5_group_tables(f, {"Im", "Re"});
+    const size_t grp_oh = h5_object_header(f, {{0x0011, h5_msg_symbol_table(grp.btree, grp.heap)}});
+    // the two datasets
+    H5Buf space, type, fill;
+    space.u8(1); space.u8(3); space.u8(0); space.u8(0); space.u32(0);  // version 1, rank 3, no max dims
+    space.u64((uint64_t)nz); space.u64((uint64_t)ny); space.u64((uint64_t)nx);
+    type.u8(0x11);                        // version 1, class 1 (floating point)
+    type.u8(0x20); type.u8(31); type.u8(0);  // little endian, implied mantissa msb, sign at bit 31
+    type.u32(4);                          // size
+    type.u16(0); type.u16(32);            // bit offset, precision
+    type.u8(23); type.u8(8); type.u8(0); type.u8(23);  // exponent location and size, mantissa location and size
+    type.u32(127);                        // exponent bias
+    fill.u8(2); fill.u8(1); fill.u8(1); fill.u8(0);  // version 2, early allocation, never written, undefined
+    auto layout = [&](uint64_t addr) {
+        H5Buf l;
+        l.u8(3); l.u8(1);                 // version 3, contiguous
+        l.u64(addr);
+        l.u64(bytes);
+        return l.b;
+    };
+    std::vector<size_t> ds_oh(2), layout_at(2);
+    for (int k = 0; k < 2; ++k) {  // 0: Im, 1: Re
+        ds_oh[k] = h5_object_header(f, {{0x0001, space.b}, {0x0003, type.b}, {0x0005, fill.b}, {0x0008, layout(0)}});
+        // the layout message is the last one: its address field follows 4 header messages
+        layout_at[k] = f.pos() - 24 + 2;
+    }
+    f.align8();
+    const uint64_t data_im = f.pos(), data_re = data_im + bytes, eof = data_re + bytes;
+    f.put64(layout_at[0], data_im);
+    f.put64(layout_at[1], data_re);
+    f.put64(eof_at, eof);
+    // patch the entries: root entry, root member, group members
+    f.put64(root_entry + 8, root_oh);
+    f.put64(root_entry + 24, root.btree);
+    f.put64(root_entry + 32, root.heap);
+    const size_t e0 = snod_entry_at(root, 0);
+    f.put64(e0 + 8, grp_oh);
+    f.b[e0 + 16] = 1;                     // cache type 1: the group's B-tree and heap
+    f.put64(e0 + 24, grp.btree);
+    f.put64(e0 + 32, grp.heap);
+    f.put64(snod_entry_at(grp, 0) + 8, ds_oh[0]);
+    f.put64(snod_entry_at(grp, 1) + 8, ds_oh[1]);
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return TDM_EIO;
+    bool ok = std::fwrite(f.b.data(), 1, f.b.size(), fp) == f.b.size();
+    ok = ok && std::fwrite(im, 4, n, fp) == n && std::fwrite(re, 4, n, fp) == n;
+    return std::fclose(fp) == 0 && ok ? TDM_OK : TDM_EIO;
+}

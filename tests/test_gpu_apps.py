@@ -4,14 +4,16 @@ from __future__ import annotations
 
 import os
 import subprocess
+from dataclasses import replace
 
 import numpy as np
 import pytest
 
 import oracle
 from mtd_transmission_gb300 import build as tdm_build
+from mtd_transmission_gb300 import simul
 from tests.helpers import oracle_cfg, rel_l2, small_case
-from tests.test_host_io import _read_tiff, _write_pgm
+from tests.test_host_io import _read_hdf5, _read_tiff, _write_pgm
 
 pytestmark = pytest.mark.gpu
 BIN = tdm_build.BIN
@@ -87,7 +89,71 @@ def test_pipeline_matches_two_programs(acquisition):
     assert rel_l2(one, two) <= 1e-5
 
 
-def test_polar_mode_is_refused(acquisition):
-    r = subprocess.run([os.path.join(BIN, "tomo_reconstruction"), "-polar"], env=acquisition["env"],
-                       capture_output=True, text=True)
-    assert r.returncode == 2 and "not supported" in r.stderr
+STATES = ("/LC/polar0/", "/LC/polar90/", "/RC/polar0/", "/RC/polar90/")
+
+
+@pytest.fixture(scope="module")
+def polarisation(tmp_path_factory):
+    """A polarisation acquisition: four states of uneven size under
+    CHEMIN_RACINE/demosaic<state>, the mask at CHEMIN_RACINE/Image_mask.pgm,
+    $HOME/.config/gui_tomo_polar.conf (pretraitement_hors_axe_CPU/main.cpp:63-80)."""
+    root = tmp_path_factory.mktemp("polar")
+    home, cfgd, racine = root / "home", root / "config", root / "racine"
+    for d in (home / ".config", cfgd, racine):
+        d.mkdir(parents=True)
+    (home / ".config" / "gui_tomo_polar.conf").write_text(
+        f"CHEMIN_CONFIG {cfgd}\nCHEMIN_RACINE {racine}\nCHEMIN_RESULT {root}\nCHEMIN_ACQUIS {root}\n")
+    acq, ph, _ = small_case("plain_512_born", M=1, ccd_roix=256, nxmax=32, circle_cx=64, circle_cy=64,
+                            dim_final=128)
+    sizes = (5, 7, 4, 6)
+    acq = replace(acq, nb_holo=max(sizes))
+    (cfgd / "recon.txt").write_text(acq.recon_txt())
+    (cfgd / "config_manip.txt").write_text(acq.config_manip_txt())
+    cfg = oracle_cfg(acq)
+    refs, mask = {}, None
+    for k, (state, M) in enumerate(zip(STATES, sizes)):
+        d = simul.holograms(replace(acq, nb_holo=M), ph, M=M, seed=20 + k)
+        holos = d["holos"].numpy()
+        mask = d["mask"].numpy() if mask is None else mask
+        sd = racine / "demosaic" / state.strip("/")
+        (sd / "UBorn").mkdir(parents=True)
+        for a in range(M):
+            _write_pgm(sd / f"i{a:03d}.pgm", holos[a], 4095)
+        # tomo_reconstruction -polar reads its configuration in the state's UBorn folder
+        (sd / "UBorn" / "recon.txt").write_text(acq.recon_txt())
+        (sd / "UBorn" / "config_manip.txt").write_text(acq.config_manip_txt())
+        spec = oracle.extract_stack(holos.astype(np.float64), cfg)
+        fields, pos = oracle.fields(spec, cfg, mask)
+        refs[state] = (sd / "UBorn", oracle.reconstruction(fields, pos, cfg, want_otf=False, want_counts=False))
+    _write_pgm(racine / "Image_mask.pgm", mask, 255)
+    return dict(env=dict(os.environ, HOME=str(home)), refs=refs)
+
+
+def test_polarisation_one_state(polarisation):
+    """tomo_pretraitement -polar -etat S then tomo_reconstruction -polar -etat S:
+    the state's volume in its UBorn folder as HDF5 (/indice_complexe/Re, Im)."""
+    A = polarisation
+    state = STATES[1]
+    _run("tomo_pretraitement", A["env"], "-polar", "-etat", state)
+    _run("tomo_reconstruction", A["env"], "-polar", "-etat", state)
+    res, ref = A["refs"][state]
+    vol = _read_hdf5(res / "indice_cplx_hdf5.hdf")["indice_complexe"]
+    assert rel_l2(vol["Re"], ref["indice"].real) <= 1e-4
+    assert rel_l2(vol["Im"], ref["indice"].imag) <= 1e-4
+
+
+def test_polarisation_four_states_in_one_graph(polarisation):
+    """tomo_pipeline -polar: the four states of uneven size as one CUDA-graph
+    launch, each state's volume against the oracle."""
+    A = polarisation
+    for state in STATES:
+        f = A["refs"][state][0] / "indice_cplx_hdf5.hdf"
+        if f.exists():
+            f.unlink()
+    out = _run("tomo_pipeline", A["env"], "-polar")
+    for state in STATES:
+        assert state in out
+        res, ref = A["refs"][state]
+        vol = _read_hdf5(res / "indice_cplx_hdf5.hdf")["indice_complexe"]
+        assert rel_l2(vol["Re"], ref["indice"].real) <= 1e-4, state
+        assert rel_l2(vol["Im"], ref["indice"].imag) <= 1e-4, state

@@ -118,11 +118,18 @@ def _run(name):
             ph, un, am = (np.zeros((1, F, F), np.float32) for _ in range(3))
             ctx.fields_debug(c64(src[w:w + 1]), phase=ph, unwrapped=un, amp=am)
             dph = np.angle(np.exp(1j * (ph[0] - dbg["phase"][0])))
+            du = un[0] - dbg["unwrap"][0]
+            df = fo[w] - ref_f[w]
+            k = np.unravel_index(int(np.argmax(np.abs(df))), df.shape)
             out["diag"] = {"angle": w, "wrapped_phase_max_abs": float(np.abs(dph).max()),
                            "wrapped_2pi_flips": int((np.abs(ph[0] - dbg["phase"][0]) > np.pi).sum()),
                            "unwrapped_rel_l2": rel_l2(un[0], dbg["unwrap"][0]),
-                           "unwrapped_max_abs": float(np.abs(un[0] - dbg["unwrap"][0]).max()),
-                           "amp_rel_l2": rel_l2(am[0], dbg["amp"][0]), "amp_min": float(dbg["amp"][0].min())}
+                           "unwrapped_l2_piston_removed": float(np.linalg.norm(du - du.mean())),
+                           "amp_rel_l2": rel_l2(am[0], dbg["amp"][0]), "amp_min": float(dbg["amp"][0].min()),
+                           "field_re_l2": float(np.linalg.norm(df.real)), "field_im_l2": float(np.linalg.norm(df.imag)),
+                           "field_norm": float(np.linalg.norm(ref_f[w])), "worst_pixel": [int(k[0]), int(k[1])],
+                           "worst_abs": float(np.abs(df[k])), "amp_there": float(dbg["amp"][0][k]),
+                           "amp_corr_there": float(dbg["amp_corr"][0][k])}
         out.update(pos=pos, fields=fields, re=re, im=im, otf=otf, cnt=cnt, ctx_geom=Geometry.from_acquisition(acq))
         if full:
             out["fields_host"] = fields.cpu().numpy()
@@ -186,7 +193,7 @@ def _stage_checks(out):
     np.testing.assert_array_equal(got, ref)
     err = np.asarray(out["field_err"])
     worst = np.argsort(-err)[:5]
-    assert err.max() <= TOL, ("worst angles", list(zip(worst.tolist(), err[worst].tolist())), out.get("diag"))
+    assert err.max() <= TOL, (out.get("diag"), "worst angles", list(zip(worst.tolist(), err[worst].tolist())))
     _counts_check(out)
 
 

@@ -222,3 +222,82 @@ def test_reference_configuration_geometry():
     g = Geometry.from_acquisition(acq)
     for k, v in golden.items():
         assert getattr(g, k) == v, k
+
+
+def _read_hdf5(path):
+    """A reader of the HDF5 structures the writer uses, after the format
+    specification: superblock 0, the root group's symbol table (local heap,
+    version-1 B-tree of group nodes, symbol table nodes), object headers of
+    version 1 and their dataspace, datatype and layout messages.  Returns
+    {group path: {dataset name: array}}."""
+    buf = open(path, "rb").read()
+    assert buf[:8] == b"\x89HDF\r\n\x1a\n"
+    assert buf[8] == 0 and buf[13] == 8 and buf[14] == 8          # superblock 0, 8-byte offsets and lengths
+    leaf_k, node_k = struct.unpack_from("<HH", buf, 16)
+    eof = struct.unpack_from("<Q", buf, 40)[0]
+    assert eof == len(buf)
+
+    def messages(addr):
+        ver, _, nmsg, _, size, _ = struct.unpack_from("<BBHIII", buf, addr)
+        assert ver == 1
+        out, at = [], addr + 16
+        for _ in range(nmsg):
+            typ, sz, _flags = struct.unpack_from("<HHB", buf, at)
+            out.append((typ, buf[at + 8:at + 8 + sz]))
+            at += 8 + sz
+        assert at == addr + 16 + size
+        return out
+
+    def heap_name(heap, off):
+        assert buf[heap:heap + 4] == b"HEAP"
+        assert struct.unpack_from("<Q", buf, heap + 16)[0] == 1   # no free block
+        data = struct.unpack_from("<Q", buf, heap + 24)[0]
+        end = buf.index(b"\0", data + off)
+        return buf[data + off:end].decode()
+
+    def members(btree, heap):
+        assert buf[btree:btree + 4] == b"TREE" and buf[btree + 4] == 0 and buf[btree + 5] == 0
+        used = struct.unpack_from("<H", buf, btree + 6)[0]
+        out = {}
+        for c in range(used):
+            snod = struct.unpack_from("<Q", buf, btree + 24 + 8 + 16 * c)[0]
+            assert buf[snod:snod + 4] == b"SNOD" and buf[snod + 4] == 1
+            nsym = struct.unpack_from("<H", buf, snod + 6)[0]
+            assert nsym <= 2 * leaf_k
+            for e in range(nsym):
+                name_off, ohdr = struct.unpack_from("<QQ", buf, snod + 8 + 40 * e)
+                out[heap_name(heap, name_off)] = ohdr
+        return out
+
+    def read_object(ohdr):
+        msgs = dict(messages(ohdr))
+        if 0x0011 in msgs:
+            bt, hp = struct.unpack("<QQ", msgs[0x0011])
+            return {n: read_object(a) for n, a in members(bt, hp).items()}
+        sp, ty, lay = msgs[0x0001], msgs[0x0003], msgs[0x0008]
+        assert 0x0005 in msgs
+        rank = sp[1]
+        dims = struct.unpack_from("<" + "Q" * rank, sp, 8)
+        assert ty[0] == 0x11 and struct.unpack_from("<I", ty, 4)[0] == 4   # IEEE float, 4 bytes
+        assert (ty[1] & 1) == 0 and ty[2] == 31                            # little endian, sign bit 31
+        assert lay[0] == 3 and lay[1] == 1                                 # contiguous
+        addr, size = struct.unpack_from("<QQ", lay, 2)
+        assert size == 4 * int(np.prod(dims))
+        return np.frombuffer(buf, "<f4", int(np.prod(dims)), addr).reshape(dims)
+
+    root_ohdr = struct.unpack_from("<Q", buf, 56 + 8)[0]
+    return read_object(root_ohdr)
+
+
+def test_hdf5_complex_volume(tmp_path):
+    """The polarisation mode's output: /indice_complexe/Re and /Im, float32
+    (nz, ny, nx), read back through the format's own structures."""
+    rng = np.random.default_rng(3)
+    re = rng.standard_normal((5, 6, 7)).astype(np.float32)
+    im = rng.standard_normal((5, 6, 7)).astype(np.float32)
+    p = str(tmp_path / "indice_cplx_hdf5.hdf")
+    api.write_hdf5_complex(p, re, im)
+    tree = _read_hdf5(p)
+    assert set(tree) == {"indice_complexe"} and set(tree["indice_complexe"]) == {"Re", "Im"}
+    np.testing.assert_array_equal(tree["indice_complexe"]["Re"], re)
+    np.testing.assert_array_equal(tree["indice_complexe"]["Im"], im)
