@@ -383,12 +383,12 @@ gk_cap_rows(const float2* __restrict__ fields_in, const float* __restrict__ unwr
 }
 
 // Column pass: forward FFT along y, then per bin the cap value (contribution
-// on the cap cells, 0 elsewhere) as k_cap_cols writes it.
+// on the cap cells, 0 elsewhere) and the cell's plane, as k_cap_cols writes them.
 template <int F>
 __global__ void __launch_bounds__(kCols * 32)
 gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ s_tab,
             const float* __restrict__ s_tabf, Params p, const float2* __restrict__ wq, float2* __restrict__ rec,
-            int* __restrict__ err) {
+            int16_t* __restrict__ recz, int* __restrict__ err) {
     extern __shared__ float2 sm[];
     __shared__ double s_fz;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -417,6 +417,7 @@ gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, con
             val = make_float2(-Bc * v.y, Bc * v.x);
         }
         rec[o] = val;
+        recz[o] = (int16_t)z;
     }
 }
 
@@ -513,7 +514,8 @@ int gcap_impl(tdm_ctx* c, int a0, int n, bool form) {
         {
             Launch l(c, K_CAP_COLS);
             gk_cap_cols<F><<<dim3(cols, m), kCols * 32, sm_cols, c->stream>>>(b.r1, b.posspec + g0, b.s_tab, b.s_tabf,
-                                                                            c->p, b.wq, b.rec + g0 * FF, b.err);
+                                                                            c->p, b.wq, b.rec.val + g0 * FF,
+                                                                            b.rec.z + g0 * FF, b.err);
         }
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;

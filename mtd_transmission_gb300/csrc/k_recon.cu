@@ -6,9 +6,9 @@
 //     (-1)^(kx+ky) dx^2 FFT2(field * tukey)[k],
 // so the per-field kernels work on natural FFT bins and store, per bin, the
 // cap contribution -2i k0 sdz value (cteUb2Pot*cteNorm*sdz, fonctions.cpp:902,927),
-// 0 outside the cap cells: an 8-byte cap value.  The gather recomputes each
-// cell's plane from the geometry (cap_plane_fd, the same arithmetic) and reads
-// the values of the cells that hit its column only.
+// 0 outside the cap cells (an 8-byte cap value), and the cell's volume plane z
+// (-1 outside the NA disc) as a 2-byte integer: the gather reads the planes of
+// the bins that fall in its column and the values of the cells that hit it.
 //
 // Mapping (retroPropag_Born, src/fonctions.cpp:875-935) as a gather: voxel
 // column (X, Y) reads bin kx = (X - D/2) mod F for every angle whose cap window
@@ -111,7 +111,7 @@ template <int F>
 __global__ void __launch_bounds__(CapCfg<F>::NT)
 k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, const double* __restrict__ s_tab,
            const float* __restrict__ s_tabf, Params p, const float2* __restrict__ tw, float2* __restrict__ rec,
-           int* __restrict__ err) {
+           int16_t* __restrict__ recz, int* __restrict__ err) {
     using C = CapCfg<F>;
     using W = typename C::W;
     constexpr int B = C::B, NT = C::NT;
@@ -144,6 +144,7 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
             val = make_float2(-Bc * v.y, Bc * v.x);
         }
         rec[o] = val;
+        recz[o] = (int16_t)z;
     }
 }
 
@@ -152,12 +153,12 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 // An angle's cap window is the F x F bins around its specular position, so a
 // column is covered by a fraction of the angles: the CTA first lists, in
 // ascending order, the angles whose window covers row Y and any of its 32
-// columns, with each angle's specular position and cap height.  The lanes
-// then take 32 consecutive listed angles at a time: each lane finds its
-// angle's cell in the column (the window and NA-disc tests and the plane,
-// cap_plane_fd) and loads the cap value of that cell only, the next two
-// groups' values loaded while the current one is added; groups without a
-// hit are skipped.  An angle hits a column at most once, at one plane, and
+// columns.  The lanes then take 32 consecutive listed angles at a time: each
+// lane loads its angle's cell plane in the column (a 2-byte record), and the
+// cap value only when the bin is a cap cell; the planes of the next two groups
+// and the values of the next group are loaded while the current one is
+// added, and groups without a hit are skipped.  An angle hits a column at
+// most once, at one plane, and
 // the column's running sums live in FP64 in shared memory.  When the group's
 // planes are distinct (seen through a plane -> lane ownership table) every
 // lane adds its own hit; otherwise lanes sharing a plane are grouped and the
@@ -169,23 +170,10 @@ constexpr int kGW = 8;  // warps per CTA
 
 size_t gather_smem(int band, int n) { return gather_smem_bytes(band, n); }
 
-// Cap heights of n angles: fzm0 in FP64 and its float value (cap_fzm0).
-__global__ void __launch_bounds__(256)
-k_cap_heights(const int2* __restrict__ posspec, int n, Params p, double* __restrict__ fzd, float* __restrict__ fzf) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a < n) {
-        const double fz = cap_fzm0(p, posspec[a]);
-        fzd[a] = fz;
-        fzf[a] = (float)fz;
-    }
-}
-
 template <int D>
 __global__ void __launch_bounds__(kGW * 32)
-k_accumulate(const float2* __restrict__ rec, const int2* __restrict__ posspec, const double* __restrict__ fzd,
-             const float* __restrict__ fzf, int M, Params p, const double* __restrict__ s_tab,
-             const float* __restrict__ s_tabf, float2* __restrict__ vol, uint32_t* __restrict__ cnt_out,
-             int normalize) {
+k_accumulate(const float2* __restrict__ rec, const int16_t* __restrict__ recz, const int2* __restrict__ posspec,
+             int M, Params p, float2* __restrict__ vol, uint32_t* __restrict__ cnt_out, int normalize) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_wc[kGW];
     __shared__ int s_listed;
@@ -194,7 +182,7 @@ k_accumulate(const float2* __restrict__ rec, const int2* __restrict__ posspec, c
     float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);      // kGW x 32
     uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32);    // kGW x band
     uint8_t* own_all = reinterpret_cast<uint8_t*>(cnt_all + kGW * band);    // kGW x band
-    int4* list = reinterpret_cast<int4*>(own_all + ((kGW * band + 15) & ~15));  // (q.x, q.y, angle, fzf), <= M
+    int2* list = reinterpret_cast<int2*>(own_all + ((kGW * band + 7) & ~7));  // (q.x, angle), <= M
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double2* acc = acc_all + w * band;
     uint16_t* cnt = cnt_all + w * band;
@@ -214,14 +202,14 @@ k_accumulate(const float2* __restrict__ rec, const int2* __restrict__ posspec, c
         bool keep = false;
         if (a < M) {
             q = posspec[a];
-            keep = (unsigned)(by + q.y) < (unsigned)F && bx0 + 31 + q.x >= 0 && bx0 + q.x < F && fzf[a] >= 0.0f;
+            keep = (unsigned)(by + q.y) < (unsigned)F && bx0 + 31 + q.x >= 0 && bx0 + q.x < F;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) s_wc[w] = __popc(bal);
         __syncthreads();
         int off = s_listed;
         for (int k = 0; k < w; ++k) off += s_wc[k];
-        if (keep) list[off + __popc(bal & ((1u << lane) - 1u))] = make_int4(q.x, q.y, a, __float_as_int(fzf[a]));
+        if (keep) list[off + __popc(bal & ((1u << lane) - 1u))] = make_int2(q.x, a);
         __syncthreads();
         if (threadIdx.x == 0) {
             int t = s_listed;
@@ -239,33 +227,29 @@ k_accumulate(const float2* __restrict__ rec, const int2* __restrict__ posspec, c
             acc[e] = make_double2(0.0, 0.0);
             cnt[e] = 0;
         }
-        // (cap value, plane) of listed angle i in this column, or plane -1 when
-        // the angle has no cell in the column
-        const int N = p.N;
-        auto fetch = [&](int i) {
-            float4 r = make_float4(0.f, 0.f, __int_as_float(-1), 0.f);
+        // plane of listed angle i's cell in this column, or -1 when the angle's
+        // window misses the column or the bin is outside its cap; the cap
+        // value of a cell with plane z
+        auto fetch_z = [&](int i) {
+            int z = -1;
             if (i < listed) {
-                const int4 q = list[i];
-                const int fdx = bx + q.x - N, fdy = by + q.y - N;
-                if ((unsigned)(fdx + N) < (unsigned)F && fdx * fdx + fdy * fdy < p.disc_thr) {
-                    float sf;
-                    const int z = cap_plane_fd(p, fdx, fdy, __int_as_float(q.w), [&] { return fzd[q.z]; }, s_tab,
-                                               s_tabf, &sf, nullptr);
-                    if (z >= 0) {
-                        const float2 v = __ldg(&rec[(size_t)q.z * FF + koff]);
-                        r = make_float4(v.x, v.y, __int_as_float(z), 0.f);
-                    }
-                }
+                const int2 q = list[i];
+                if ((unsigned)(bx + q.x) < (unsigned)F) z = __ldg(&recz[(size_t)q.y * FF + koff]);
             }
-            return r;
+            return z;
         };
-        float4 nxt = fetch(lane), nxt2 = fetch(32 + lane);
+        auto fetch_v = [&](int i, int z) {
+            return z >= 0 ? __ldg(&rec[(size_t)list[i].y * FF + koff]) : make_float2(0.f, 0.f);
+        };
+        int z_nxt = fetch_z(lane), z_nxt2 = fetch_z(32 + lane);
+        float2 v_nxt = fetch_v(lane, z_nxt);
         __syncwarp();
         for (int g0 = 0; g0 < listed; g0 += 32) {
-            const float4 r = nxt;
-            nxt = nxt2;
-            nxt2 = fetch(g0 + 64 + lane);
-            const int z = __float_as_int(r.z);
+            const int z = z_nxt;
+            const float2 r = v_nxt;
+            z_nxt = z_nxt2;
+            v_nxt = fetch_v(g0 + 32 + lane, z_nxt);
+            z_nxt2 = fetch_z(g0 + 64 + lane);
             const int e = z >= 0 ? z - zmin : -1;
             if (!__any_sync(0xffffffffu, e >= 0)) continue;
             if (e >= 0) own[e] = (uint8_t)lane;
@@ -503,7 +487,8 @@ k_fzpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int 
 __global__ void __launch_bounds__(256)
 k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, Params p,
              const double* __restrict__ s_tab, const float* __restrict__ s_tabf, const float2* __restrict__ data,
-             float2* __restrict__ caps, float2* __restrict__ res, double* __restrict__ misfit, int* __restrict__ err) {
+             float2* __restrict__ caps, float2* __restrict__ res, int16_t* __restrict__ resz, double* __restrict__ misfit,
+             int* __restrict__ err) {
     const int a = blockIdx.y, F = p.F, D = p.D;
     const int2 ps = posspec[a];
     __shared__ double s_fz;
@@ -527,7 +512,10 @@ k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, P
             m2 += (double)v.x * v.x + (double)v.y * v.y;
         }
         if (caps) caps[o] = v;
-        if (res) res[o] = v;
+        if (res) {
+            res[o] = v;
+            resz[o] = (int16_t)z;
+        }
     }
     if (misfit) {
 #pragma unroll
@@ -546,7 +534,7 @@ k_cap_sample(const float2* __restrict__ vol, const int2* __restrict__ posspec, P
 __global__ void __launch_bounds__(256)
 k_cap_pack(const float2* __restrict__ caps, const int2* __restrict__ posspec, Params p,
            const double* __restrict__ s_tab, const float* __restrict__ s_tabf, float2* __restrict__ rec,
-           int* __restrict__ err) {
+           int16_t* __restrict__ recz, int* __restrict__ err) {
     const int a = blockIdx.y, F = p.F;
     const int2 ps = posspec[a];
     __shared__ double s_fz;
@@ -560,6 +548,7 @@ k_cap_pack(const float2* __restrict__ caps, const int2* __restrict__ posspec, Pa
         const int z = cap_plane(p, ps, fz, fzf, i % F, i / F, s_tab, s_tabf, &sf, err);
         const float2 v = z >= 0 ? caps[o] : make_float2(0.f, 0.f);
         rec[o] = v;
+        recz[o] = (int16_t)z;
     }
 }
 
@@ -630,7 +619,7 @@ int cap_impl(tdm_ctx* c, int a0, int n, bool form) {
         {
             Launch l(c, K_CAP_COLS);
             k_cap_cols<F><<<dim3(F / C::B, m), C::NT, C::SMEM, c->stream>>>(
-                b.r1, b.posspec + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec + g0 * FF, b.err);
+                b.r1, b.posspec + g0, b.s_tab, b.s_tabf, c->p, b.tw, b.rec.val + g0 * FF, b.rec.z + g0 * FF, b.err);
         }
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
@@ -647,7 +636,7 @@ static cudaError_t download_after(tdm_ctx* c, cudaStream_t st, cudaEvent_t ev, v
 }
 
 template <int D>
-int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float2* rec, const int2* posspec,
+int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, CapRecs rec, const int2* posspec,
                 cudaEvent_t ev_gathered) {
     float* re = out.re;
     float* im = out.im;
@@ -674,13 +663,8 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
     }
     cudaEventRecord(c->ev_stage[4], st);
     {
-        Launch l(c, K_POSSPEC, st);
-        k_cap_heights<<<(n + 255) / 256, 256, 0, st>>>(posspec, n, p, b.cap_fzd, b.cap_fzf);
-    }
-    {
         Launch l(c, K_GATHER, st);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, st>>>(rec, posspec, b.cap_fzd, b.cap_fzf, n, p, b.s_tab,
-                                                                  b.s_tabf, b.vol, cnt, 1);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, st>>>(rec.val, rec.z, posspec, n, p, b.vol, cnt, 1);
     }
     cudaEventRecord(c->ev_stage[5], st);
     if (ev_gathered && cudaEventRecord(ev_gathered, st)) return TDM_ECUDA;
@@ -731,7 +715,7 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const 
 }
 
 template <int D>
-int forward_impl(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float2* data, float2* res,
+int forward_impl(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float2* data, CapRecs res,
                  double* misfit) {
     using P = PassCfg<D>;
     Buffers& b = c->b;
@@ -756,13 +740,13 @@ int forward_impl(tdm_ctx* c, const float* xn, const float* xk, int n, float2* ca
         Launch l(c, K_CAP_COLS);
         const int per = (p.F * p.F + 255) / 256;
         k_cap_sample<<<dim3(per < 16 ? per : 16, n), 256, 0, c->stream>>>(b.vol, b.posspec, p, b.s_tab, b.s_tabf, data,
-                                                                          caps, res, misfit, b.err);
+                                                                          caps, res.val, res.z, misfit, b.err);
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }
 
 template <int D>
-int adjoint_impl(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, bool normalize) {
+int adjoint_impl(tdm_ctx* c, CapRecs recs, int n, float* xn, float* xk, bool normalize) {
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
@@ -773,14 +757,9 @@ int adjoint_impl(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, bo
         allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
     {
-        Launch l(c, K_POSSPEC);
-        k_cap_heights<<<(n + 255) / 256, 256, 0, c->stream>>>(b.posspec, n, p, b.cap_fzd, b.cap_fzf);
-    }
-    {
         Launch l(c, K_GATHER);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(recs, b.posspec, b.cap_fzd, b.cap_fzf, n, p,
-                                                                         b.s_tab, b.s_tabf, b.vol, nullptr,
-                                                                         normalize ? 1 : 0);
+        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(recs.val, recs.z, b.posspec, n, p, b.vol,
+                                                                         nullptr, normalize ? 1 : 0);
     }
     {
         Launch l(c, K_ZPASS);
@@ -804,7 +783,7 @@ int adjoint_impl(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, bo
 // owners plus a 32-lane staging row, and the CTA's list of n angles at most.
 size_t gather_smem_bytes(int band, int n) {
     return (size_t)kGW * band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 15) & ~15) + (size_t)n * sizeof(int4);
+           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 7) & ~7) + (size_t)n * sizeof(int2);
 }
 
 int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
@@ -818,7 +797,7 @@ int launch_cap(tdm_ctx* c, int a0, int n, bool form) {
     }
 }
 
-int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float2* rec, const int2* posspec,
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, CapRecs rec, const int2* posspec,
                   cudaEvent_t ev_gathered) {
     switch (c->p.D) {
         case 128: return volume_impl<128>(c, n, out, st, rec, posspec, ev_gathered);
@@ -830,7 +809,7 @@ int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, cons
 }
 
 int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float2* data,
-                   float2* res, double* misfit) {
+                   CapRecs res, double* misfit) {
     switch (c->p.D) {
         case 128: return forward_impl<128>(c, xn, xk, n, caps, data, res, misfit);
         case 256: return forward_impl<256>(c, xn, xk, n, caps, data, res, misfit);
@@ -840,7 +819,7 @@ int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* 
     }
 }
 
-int launch_adjoint(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, bool normalize) {
+int launch_adjoint(tdm_ctx* c, CapRecs recs, int n, float* xn, float* xk, bool normalize) {
     switch (c->p.D) {
         case 128: return adjoint_impl<128>(c, recs, n, xn, xk, normalize);
         case 256: return adjoint_impl<256>(c, recs, n, xn, xk, normalize);
@@ -850,12 +829,12 @@ int launch_adjoint(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, 
     }
 }
 
-int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float2* recs) {
+int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, CapRecs recs) {
     const int per = (c->p.F * c->p.F + 255) / 256;
     {
         Launch l(c, K_CAP_COLS);
         k_cap_pack<<<dim3(per < 16 ? per : 16, n), 256, 0, c->stream>>>(caps, c->b.posspec, c->p, c->b.s_tab,
-                                                                        c->b.s_tabf, recs, c->b.err);
+                                                                        c->b.s_tabf, recs.val, recs.z, c->b.err);
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }

@@ -80,10 +80,10 @@ void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
-                    b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0], b.rec_buf[1], b.posspec_vol[0],
-                    b.posspec_vol[1], b.cap_fzd, b.cap_fzf, b.vol, b.out_re, b.out_im, b.out_otf,
+                    b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0].val, b.rec_buf[0].z, b.rec_buf[1].val,
+                    b.rec_buf[1].z, b.posspec_vol[0], b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
-                    b.xv[4], b.xv[5], b.caps, b.rec2, b.misfit, b.ref_inv};
+                    b.xv[4], b.xv[5], b.caps, b.rec2.val, b.rec2.z, b.misfit, b.ref_inv};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = Buffers{};
@@ -371,12 +371,12 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.fit_done, CH * 2));
     TRY(dev_alloc(c, &b.fields, M * FF));
     TRY(dev_alloc(c, &b.r1, CH * FF));
-    TRY(dev_alloc(c, &b.rec_buf[0], M * FF));
-    TRY(dev_alloc(c, &b.rec_buf[1], M * FF));
+    for (auto& r : b.rec_buf) {
+        TRY(dev_alloc(c, &r.val, M * FF));
+        TRY(dev_alloc(c, &r.z, M * FF));
+    }
     TRY(dev_alloc(c, &b.posspec_vol[0], M));
     TRY(dev_alloc(c, &b.posspec_vol[1], M));
-    TRY(dev_alloc(c, &b.cap_fzd, M));
-    TRY(dev_alloc(c, &b.cap_fzf, M));
     b.rec = b.rec_buf[0];
     TRY(dev_alloc(c, &b.vol, (size_t)D * D * D));
     TRY(dev_alloc(c, &b.rinv, kNC * kNC));
@@ -681,7 +681,7 @@ int tdm_fields_debug(tdm_ctx* c, const float* spectra_in, int n, float* fields_o
 // first); outputs may be host or device memory.  Host outputs are written to
 // device staging buffers and downloaded while the later passes run.
 static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t* otf, uint32_t* cnt,
-                      bool wait = true, cudaStream_t st = nullptr, const float2* rec = nullptr,
+                      bool wait = true, cudaStream_t st = nullptr, const CapRecs* rec = nullptr,
                       const int2* posspec = nullptr, cudaEvent_t ev_gathered = nullptr) {
     const Params& p = c->p;
     const size_t NT = (size_t)p.D * p.D * p.D;
@@ -707,7 +707,7 @@ static int run_volume(tdm_ctx* c, int n, bool cap, float* re, float* im, uint8_t
     if (im && out.im != im) out.host_im = im;
     if (otf && out.otf != otf) out.host_otf = otf;
     if (cnt && out.cnt != cnt) out.host_cnt = cnt;
-    if (int rc = launch_volume(c, n, out, st ? st : c->stream, rec ? rec : b.rec, posspec ? posspec : b.posspec,
+    if (int rc = launch_volume(c, n, out, st ? st : c->stream, rec ? *rec : b.rec, posspec ? posspec : b.posspec,
                                ev_gathered))
         return fail(c, rc, "volume launch failed");
     const bool host = out.host_re || out.host_im || out.host_otf || out.host_cnt;
@@ -875,7 +875,7 @@ static int pipeline(tdm_ctx* c, const void* holos, int bits, int n, float* indic
     TDM_CU(cudaEventRecord(c->ev_angles, c->stream));
     TDM_CU(cudaStreamWaitEvent(c->vol_stream, c->ev_angles, 0));
     int rc = run_volume(c, n, false, indice_out, absorption_out, otf_out, counts_out, wait, c->vol_stream,
-                        c->b.rec_buf[par], c->b.posspec_vol[par], c->ev_rec_free[par]);
+                        &c->b.rec_buf[par], c->b.posspec_vol[par], c->ev_rec_free[par]);
     if (rc) return rc;
     TDM_CU(cudaEventRecord(c->ev_vol_last, c->vol_stream));
     c->rec_parity ^= 1;
@@ -909,7 +909,7 @@ static int ensure_operator_buffers(tdm_ctx* c) {
     for (auto& v : c->b.xv)
         if (!v && dev_alloc(c, &v, NT)) return TDM_ENOMEM;
     if (!c->b.caps && dev_alloc(c, &c->b.caps, MF)) return TDM_ENOMEM;
-    if (!c->b.rec2 && dev_alloc(c, &c->b.rec2, MF)) return TDM_ENOMEM;
+    if (!c->b.rec2.val && (dev_alloc(c, &c->b.rec2.val, MF) || dev_alloc(c, &c->b.rec2.z, MF))) return TDM_ENOMEM;
     if (!c->b.misfit && dev_alloc(c, &c->b.misfit, 1)) return TDM_ENOMEM;
     return TDM_OK;
 }
@@ -945,7 +945,7 @@ int tdm_forward(tdm_ctx* c, const float* index, const float* absorption, int n, 
     }
     const bool host_out = !is_device_ptr(caps_out);
     float2* caps = host_out ? c->b.caps : reinterpret_cast<float2*>(caps_out);
-    if (int rc = launch_forward(c, xn, xk, n, caps, nullptr, nullptr, nullptr))
+    if (int rc = launch_forward(c, xn, xk, n, caps, nullptr, CapRecs{}, nullptr))
         return fail(c, rc, "tdm_forward: launch failed");
     if (host_out)
         TDM_CU(cudaMemcpyAsync(caps_out, caps, n * FF * sizeof(float2), cudaMemcpyDeviceToHost, c->stream));
@@ -1018,7 +1018,7 @@ int tdm_tv_reconstruct(tdm_ctx* c, const float* caps, int n, const int32_t* poss
     double first = -1, last = -1;
     for (int it = 0; it < o->iterations; ++it) {
         TDM_CU(cudaMemsetAsync(b.misfit, 0, sizeof(double), c->stream));
-        if (int rc = launch_forward(c, xn, xk, n, nullptr, b.rec, b.rec2, b.misfit))
+        if (int rc = launch_forward(c, xn, xk, n, nullptr, b.rec.val, b.rec2, b.misfit))
             return fail(c, rc, "tdm_tv_reconstruct: launch failed");
         if (it == 0 || it == o->iterations - 1) {
             double m = 0;

@@ -19,6 +19,14 @@ constexpr int kMaxLanes = 8;    // chunks of the per-angle stages in flight at o
 constexpr int kStageSlots = 16; // hologram upload slots of one chunk each
 constexpr int kChunkCapMax = 128;  // angles of per-chunk scratch (all lanes together), at most
 
+// Cap records of a stack: per angle and FFT bin ([angle][ky][kx]) the cap
+// value (the cell's contribution, 0 outside the cap cells) and the cell's
+// volume plane (-1 outside the cells).
+struct CapRecs {
+    float2* val = nullptr;
+    int16_t* z = nullptr;
+};
+
 // Device-side parameters of one volume, fixed at context creation.
 struct Params {
     int H, N, F, L, D;
@@ -61,10 +69,8 @@ struct Buffers {
     unsigned* fit_done = nullptr;  // chunk x 2 finished-slice counters (zero between launches)
     float2* fields = nullptr;      // max_angles x F*F
     float2* r1 = nullptr;          // chunk x F*F
-    float2* rec = nullptr;         // max_angles x F*F cap values (contribution on the cap cells, 0 elsewhere): rec_buf[i]
-    float2* rec_buf[2] = {};       // the two cap-value buffers of consecutive pipeline calls
-    double* cap_fzd = nullptr;     // max_angles cap heights fzm0 (FP64) of the angles being gathered
-    float* cap_fzf = nullptr;      // max_angles the same in float
+    CapRecs rec;                   // max_angles x F*F cap records: rec_buf[i]
+    CapRecs rec_buf[2];            // the two cap-record buffers of consecutive pipeline calls
     int2* posspec_vol[2] = {};     // max_angles: specular positions read by the volume stage of those calls
     float2* vol = nullptr;         // D^3 complex, [y][x][z] layout
     float* out_re = nullptr;       // D^3 staging when the caller's output is in host memory
@@ -78,7 +84,7 @@ struct Buffers {
     // forward operator / adjoint / regularised reconstruction (allocated on first use)
     float* xv[6] = {};             // D^3 each: iterate index/absorption (x2, double buffered), gradient index/absorption
     float2* caps = nullptr;        // max_angles x F*F cap values staged for host callers
-    float2* rec2 = nullptr;        // max_angles x F*F residual / adjoint-input cap values
+    CapRecs rec2;                  // max_angles x F*F residual / adjoint-input cap records
     double* misfit = nullptr;      // data misfit accumulator
 };
 
@@ -220,13 +226,13 @@ struct VolumeOut {
 // cap cells; with data (cap records), res = spectrum - data on the data's
 // cells and *misfit += sum |res|^2.  Uses b.vol.
 int launch_forward(tdm_ctx* c, const float* xn, const float* xk, int n, float2* caps, const float2* data,
-                   float2* res, double* misfit);
+                   CapRecs res, double* misfit);
 // Adjoint of the forward operator applied to cap records (unnormalised
 // scatter, z/y/x passes); with normalize, the hit-count-normalised scatter and
 // the reconstruction's own scale (the single-pass reconstruction of recs).
-int launch_adjoint(tdm_ctx* c, const float2* recs, int n, float* xn, float* xk, bool normalize);
+int launch_adjoint(tdm_ctx* c, CapRecs recs, int n, float* xn, float* xk, bool normalize);
 // Cap records (value, cell plane) of cap values in FFT-bin order.
-int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, float2* recs);
+int launch_cap_pack(tdm_ctx* c, const float2* caps, int n, CapRecs recs);
 // One projected-gradient step with the TV gradient (steps tv_n, tv_k) and box constraints.
 int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn, const float* gk, float step,
                    float tv_n, float tv_k, float eps, float nlo, float nhi, float klo, float khi, float* xn_out,
@@ -237,6 +243,6 @@ int launch_tv_step(tdm_ctx* c, const float* xn, const float* xk, const float* gn
 // rewritten only after the previous volume's download of that part is done
 // (c->ev_dl).  ev_gathered (may be null) is recorded on st once the gather
 // has read rec.
-int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, const float2* rec, const int2* posspec,
+int launch_volume(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, CapRecs rec, const int2* posspec,
                   cudaEvent_t ev_gathered);
 }  // namespace tdm

@@ -193,6 +193,8 @@ def _stage_checks(out):
     np.testing.assert_array_equal(got, ref)
     err = np.asarray(out["field_err"])
     worst = np.argsort(-err)[:5]
+    if out.get("diag"):
+        print("field error diagnostics:", out["diag"])
     assert err.max() <= TOL, (out.get("diag"), "worst angles", list(zip(worst.tolist(), err[worst].tolist())))
     _counts_check(out)
 
