@@ -80,8 +80,8 @@ typedef struct {
 
 /* Creates a context on the current CUDA device for stacks of up to
  * max_angles holograms (TDM_EUNSUPPORTED above 65535, or above what the cap
- * gather's per-CTA angle list allows for the geometry: about 12,000 angles
- * at NXMAX 128, DIM_FINAL 512; the message gives the limit).  A context is
+ * gather's per-CTA angle list allows for the geometry: 24,620 angles at
+ * NXMAX 128, DIM_FINAL 512; the limit is printed on stderr).  A context is
  * used by one host thread at a time.  Replaces the FFTW plan set-up of both programs
  * (pretraitement_hors_axe_CPU/main.cpp:91-105,180-189; Reconstruction/main.cpp:131,185,318). */
 int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out);

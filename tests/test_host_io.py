@@ -194,7 +194,7 @@ def test_noalloc_wrapper_checks_buffers():
 def test_gather_angle_limit_refused_at_create():
     """The cap gather keeps each CTA's list of angles in shared memory: a
     context whose angle count cannot fit is refused at creation (before any
-    device work), with the limit in the message, instead of failing later."""
+    device work), with the limit printed on stderr, instead of failing later."""
     acq, _, _ = simul.workload("rytov_1024")
     g = Geometry.from_acquisition(acq)
     with pytest.raises(api.TdmError) as e:
