@@ -61,8 +61,8 @@ def algorithmic_bytes(name, acq, hits_per_angle, band):
         "cap_cols": F * F * 8 + F * F * 10,
     }
     per_volume = {
-        "gather": hits_per_angle * acq.nb_holo * 10 + band * D * D * 8,
-        "zpass": band * D * D * 8 + D ** 3 * 8 + D ** 3,
+        # the gather with the z pass: cap cells in, the z-transformed spectrum and the OTF out
+        "gather": hits_per_angle * acq.nb_holo * 10 + D ** 3 * 8 + D ** 3,
         "ypass": 2 * D ** 3 * 8,
         "xpass": D ** 3 * 8 + 2 * D ** 3 * 4,
     }
@@ -84,7 +84,7 @@ STAGE_KERNELS = {
     "fields": ("field_rows", "field_cols", "volkov_rows", "volkov_cols", "volkov_integ_rows",
                "volkov_integ_cols", "aber_fit", "form"),
     "cap_mapping": ("cap_rows", "cap_cols"),
-    "volume": ("gather", "zpass", "ypass", "xpass"),
+    "volume": ("gather", "ypass", "xpass"),
 }
 
 
@@ -125,14 +125,12 @@ def stage_roofline(acq, hits_per_angle, kern_ms, step_ms, peak):
 
 
 # DRAM bytes (read + write) per launch from the committed ncu capture of
-# the kernel on this code (the file named in the returned source): the row
-# pass on the 64-hologram case (a launch processes 16 holograms), the gather
-# on the 600-hologram case (its record reads grow with the angles, scaled by
-# angles/600; its band writes do not).  None where no capture of this
-# workload's kernel is committed.
+# the kernel on this code (the file named in the returned source), as
+# (bytes that do not depend on the angle count, bytes per 600 angles): the
+# row pass on the 64-hologram case (a launch processes 16 holograms).  None
+# where no capture of this workload's kernel is committed.
 NCU_TRAFFIC = {
     "extract_rows": (33.616128e6 + 0.341504e6, 0.0, "profiles/k_extract_rows_rytov_1024_64holos.md"),
-    "gather": (419.033088e6, 648.724224e6, "profiles/k_accumulate_rytov_1024_600holos.md"),
 }
 
 
@@ -504,9 +502,10 @@ def cufft_reference(acq, kern):
                 "hologram_rows_16": round(ours("extract_rows") / n_chunks, 4),
                 "hologram_cols_16": round(ours("extract_cols") / n_chunks, 4),
                 "fields_2d_16": round(ours("field_rows", "field_cols") / n_chunks, 4),
-                "volume_3d": ours("zpass", "ypass", "xpass")},
+                "volume_3d": ours("gather", "ypass", "xpass")},
             "note": "the hand-written passes include their fused work (Tukey window, row packing and band "
-                    "separation, crop, recentring, atan2/phasor, shifts, scaling and the index/absorption split); "
+                    "separation, crop, recentring, atan2/phasor, shifts, scaling and the index/absorption split; "
+                    "the volume's z pass runs inside the cap gather, so volume_3d includes the gather); "
                     "the cuFFT calls are bare transforms"}
 
 
@@ -597,8 +596,10 @@ def main():
     barrier()
     s_first = sampler.mark()
     ev0.record(stream)
+    t_enq = time.perf_counter()
     for _ in range(args.steps):
         ctx.pipeline(holos, indice=re, absorption=im, otf=otf)
+    t_enq = time.perf_counter() - t_enq  # host time to enqueue the K steps
     ctx.join()  # the last volume stages run on the context's second stream
     ev1.record(stream)
     ctx.synchronize()
@@ -643,6 +644,7 @@ def main():
     # E2E_TRIALS trials of e2e_steps volumes and the median trial is reported
     # (every trial is listed in the line).
     e2e_trials_s = []
+    e2e_enqueue_s = []
     e2e_sync_s = 0.0
     if args.e2e_steps > 0:
         h_re, h_im, h_otf = h_outs[0]
@@ -662,6 +664,7 @@ def main():
             for k in range(args.e2e_steps):
                 h_re, h_im, h_otf = h_outs[k % 2]
                 ctx.pipeline_async(h_holos, indice=h_re, absorption=h_im, otf=h_otf)
+            e2e_enqueue_s.append(time.perf_counter() - t0)
             ctx.synchronize()
             e2e_trials_s.append(time.perf_counter() - t0)
     t_e = max_over_ranks(e2e_trials_s + [e2e_sync_s], world, "cuda")
@@ -736,9 +739,13 @@ def main():
                             "volumes out, alternating output sets), one tdm_synchronize at the end; median of "
                             f"{E2E_TRIALS} trials of {args.e2e_steps} volumes",
                     "trials": [round(v, 3) for v in e2e_trials],
+                    # host time spent inside the pipeline_async calls of each trial, per volume
+                    "enqueue_ms_per_step": [round(1e3 * s / args.e2e_steps, 3) for s in e2e_enqueue_s],
                     "sync_value": round(e2e_sync, 3) if e2e_sync else None,
                     "sync_mode": "tdm_pipeline per step, each call returns with the volume in host memory"},
             "gpu_launches": int(launches),
+            # host time spent inside the K pipeline calls, per step (the calls queue work and return)
+            "enqueue_ms_per_step": round(1e3 * t_enq / args.steps, 3),
             "roofline": roof,
             "roofline_all": roof_all,
             "roofline_stages": stage_roofline(acq, hits, {k: v[0] for k, v in kern.items()}, ms_max / args.steps,

@@ -43,9 +43,26 @@ struct ExtractCfg {
     static dim3 grid_cols(int F, int m) { return dim3((F + C - 1) / C, m); }
 };
 
-// Row pass.  tuk is the 1D hologram window, exactly 1 on [flat.x, flat.y]
-// (not read there); ref_inv (may be null) is the H x H reciprocal of the
-// reference amplitude, applied to every pixel first (main.cpp:147).  BULK: each warp's 2G rows (its G row pairs, consecutive in
+// Lanes' elements n1 whose pixels x = j + T n1 can fall in the hologram
+// window's tapers: the first and the last win_edge of the E.  The window
+// (Tukey, alpha 0.05) is exactly 1 on the others; window_edge_ok checks that
+// on the host before a launch.
+template <int H>
+constexpr int win_edge() { return H >= 2048 ? 2 : 1; }
+inline bool window_edge_ok(int H, int2 flat, int edge) {
+    const int T = H / warp_fft_e(H);
+    return flat.x <= T * edge && flat.y >= H - T * edge - 1;
+}
+
+// Row pass.  win[x] = ((-1)^x w(x), -2^23 (-1)^x w(x)) is the hologram window
+// with the sign modulation of the first fftshift (hologram_window): a pixel p
+// is read as the float m = 2^23 + p (its bits OR 0x4B000000) and fma(m, ws,
+// cs) is p (-1)^x w(x) rounded once, with no integer-to-float conversion.  On
+// the window's flat middle (-1)^x = (-1)^j, so the lane's own (+-1, -+2^23)
+// stands for the table there.  The rows' factors (-1)^y w(y) are applied when
+// the two packed rows are separated.  ref_inv (may be null) is the H x H
+// reciprocal of the reference amplitude, applied to every pixel
+// (main.cpp:147).  BULK: each warp's 2G rows (its G row pairs, consecutive in
 // memory) are staged in shared memory by one bulk copy and read from there;
 // requires a 16-byte aligned stack.  Otherwise the lanes load the pixels
 // directly.  A bulk copy that does not complete within wait_polls polls sets
@@ -54,41 +71,38 @@ struct ExtractCfg {
 // shared memory of a finished CTA.
 template <int H, bool BULK>
 __global__ void __launch_bounds__(ExtractCfg<H>::NT, ExtractCfg<H>::ROWS_CTAS)
-k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict__ tuk, int2 flat,
+k_extract_rows(const void* __restrict__ holos, int bits, const float2* __restrict__ win,
                const float* __restrict__ ref_inv, const float2* __restrict__ tw, float2* __restrict__ inter, int F,
                int x0, int* __restrict__ err, uint32_t wait_polls) {
     using Cf = ExtractCfg<H>;
     using W = typename Cf::W;
-    constexpr int T = W::T, E = W::E, P = Cf::P;
+    constexpr int T = W::T, E = W::E, P = Cf::P, K = win_edge<H>();
     extern __shared__ __align__(16) float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y;
     const int ya = 2 * (blockIdx.x * P + tr), yb = ya + 1;
     float2* s = sm + tr * W::STRIDE;
-    const float wa = tuk[ya], wb = tuk[yb];
-    const float sx = (j & 1) ? -1.0f : 1.0f;  // (-1)^x for x = j + T n1, T even; ya even, yb odd
+    const float ha = 0.5f * __ldg(&win[ya]).x, hb = 0.5f * __ldg(&win[yb]).x;  // (-1)^y w(y) / 2
+    const float2 flat = (j & 1) ? make_float2(-1.0f, 8388608.0f) : make_float2(1.0f, -8388608.0f);
     const size_t bpp = bits == 16 ? 2 : 1;
     float2 x[E];
-    // windowed pixels of rows ya (real part) and yb (imaginary part, negated)
+    // windowed pixels of rows ya (real part) and yb (imaginary part)
+    auto put = [&](int n1, uint32_t pa, uint32_t pb) {
+        const float2 wc = (n1 < K || n1 >= E - K) ? __ldg(&win[j + n1 * T]) : flat;
+        x[n1] = make_float2(fmaf(__uint_as_float(0x4B000000u | pa), wc.x, wc.y),
+                            fmaf(__uint_as_float(0x4B000000u | pb), wc.x, wc.y));
+    };
     auto load = [&](const char* row) {
         if (bits == 16) {
             const uint16_t* ra = reinterpret_cast<const uint16_t*>(row);
 #pragma unroll
-            for (int n1 = 0; n1 < E; ++n1) {
-                const int xx = j + n1 * T;
-                const float w = sx * ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx]));  // window is 1 on [flat]
-                x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
-            }
+            for (int n1 = 0; n1 < E; ++n1) put(n1, ra[j + n1 * T], ra[H + j + n1 * T]);
         } else {
             const uint8_t* ra = reinterpret_cast<const uint8_t*>(row);
 #pragma unroll
-            for (int n1 = 0; n1 < E; ++n1) {
-                const int xx = j + n1 * T;
-                const float w = sx * ((xx >= flat.x && xx <= flat.y) ? 1.0f : __ldg(&tuk[xx]));
-                x[n1] = make_float2((float)ra[xx] * (w * wa), -(float)ra[H + xx] * (w * wb));
-            }
+            for (int n1 = 0; n1 < E; ++n1) put(n1, ra[j + n1 * T], ra[H + j + n1 * T]);
         }
-        if (ref_inv) {  // pixel / reference amplitude, before the window (it scales each product)
+        if (ref_inv) {  // pixel / reference amplitude (it scales each product)
             const float* qa = ref_inv + (size_t)ya * H;
 #pragma unroll
             for (int n1 = 0; n1 < E; ++n1) {
@@ -133,7 +147,8 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
         for (int k2 = 0; k2 < T; ++k2) s[warp_out_pos<H>(j, q, k2)] = x[q * T + k2];
     }
     __syncwarp();
-    // separate the two real rows on the kx band: Xa = (Z(k) + conj Z(-k))/2, Xb = (Z(k) - conj Z(-k))/(2i);
+    // separate the two real rows on the kx band: Xa = (Z(k) + conj Z(-k))/2, Xb = (Z(k) - conj Z(-k))/(2i),
+    // times the rows' window factors;
     // rows ya (even) and yb = ya + 1 of column c are adjacent in inter (one
     // 16-byte word), and the CTA's P row pairs are one 16P-byte segment of
     // each column.  The words go through the tile, CB columns at a time, so
@@ -146,8 +161,8 @@ k_extract_rows(const void* __restrict__ holos, int bits, const float* __restrict
         for (int c = j; c < nc; c += T) {
             const int k = x0 + cb + c, km = (H - k) & (H - 1);
             const float2 z = s[W::pad(k)], zm = s[W::pad(km)];
-            tile[c * (P + 1) + tr] = make_float4(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y), 0.5f * (z.y + zm.y),
-                                                 -0.5f * (z.x - zm.x));
+            tile[c * (P + 1) + tr] = make_float4(ha * (z.x + zm.x), ha * (z.y - zm.y), hb * (z.y + zm.y),
+                                                 -hb * (z.x - zm.x));
         }
         __syncthreads();
         for (int i = threadIdx.x; i < nc * P; i += Cf::NT) {

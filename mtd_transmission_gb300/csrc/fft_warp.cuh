@@ -224,6 +224,32 @@ __device__ __forceinline__ void fft_warp_regs(float2 (&x)[WarpFFT<N>::E], float2
     for (int q = 0; q < E / T; ++q) dft<T, DIR>(&x[q * T]);
 }
 
+// fft_warp_regs with a smaller exchange buffer: the E/T output blocks are
+// exchanged one at a time (block q reads the rows k1 in [qT, qT + T), which
+// come from the same registers x[qT .. qT + T) of every lane), so s needs
+// T (T + 1) slots instead of N + E (WarpFFT<N>::LEN).  Same values, in the
+// same registers, as fft_warp_regs; one more __syncwarp pair per block.
+template <int N, int DIR>
+__device__ __forceinline__ void fft_warp_regs_lean(float2 (&x)[WarpFFT<N>::E], float2* s, int j,
+                                                   const float2* __restrict__ tw) {
+    using W = WarpFFT<N>;
+    constexpr int E = W::E, T = W::T;
+    const float2* twr = tw + twr_offset(N);
+    dft<E, DIR>(x);
+    twiddle_lane<N, DIR>(x, twr, j);
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) {
+        __syncwarp();  // earlier readers of s are done
+#pragma unroll
+        for (int kk = 0; kk < T; ++kk) s[kk * (T + 1) + j] = x[q * T + kk];
+        __syncwarp();
+#pragma unroll
+        for (int n2 = 0; n2 < T; ++n2) x[q * T + n2] = s[j * (T + 1) + n2];
+    }
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) dft<T, DIR>(&x[q * T]);
+}
+
 // The same transform run from the other end: on entry x[q T + k2] holds
 // element (j + q T) + E k2 (the order fft_warp_regs produces); on return x[n1]
 // holds element j + T n1 of its DIR transform.  With k = k1 + E k2 and

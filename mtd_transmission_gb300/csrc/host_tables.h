@@ -50,6 +50,20 @@ inline std::vector<double> tukey_factor(int n, float alpha) {
     return t;
 }
 
+// Row-pass table of the hologram window (Tukey, alpha 0.05, main.cpp:105):
+// ((-1)^x w(x), -2^23 (-1)^x w(x)) for x in [0, H).  (-1)^x is the first
+// fftshift; the second member lets a kernel turn a pixel read as 2^23 + p into
+// p (-1)^x w(x) with one FMA.
+inline std::vector<float2> hologram_window(int H) {
+    const std::vector<double> t = tukey_factor(H, 0.05f);
+    std::vector<float2> w(H);
+    for (int x = 0; x < H; ++x) {
+        const float ws = (x & 1) ? -(float)t[x] : (float)t[x];
+        w[x] = make_float2(ws, -8388608.0f * ws);
+    }
+    return w;
+}
+
 // Indices [x, y] where tukey_factor(n, alpha) is exactly 1 (its flat middle,
 // same bounds as above): kernels skip the table there.
 inline int2 tukey_flat(int n, float alpha) {

@@ -27,6 +27,7 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
     using C = ExtractCfg<H>;
     const Params& p = c->p;
     const size_t sm_rows = C::smem_rows(p.F), sm_cols = C::smem_cols(p.F);
+    if (!window_edge_ok(H, c->tuk_h_flat, win_edge<H>())) return TDM_EUNSUPPORTED;
     if (allow_smem(k_extract_rows<H, true>, sm_rows) != cudaSuccess) return TDM_ECUDA;
     if (allow_smem(k_extract_rows<H, false>, sm_rows) != cudaSuccess) return TDM_ECUDA;
     if (allow_smem(k_extract_cols<H>, sm_cols) != cudaSuccess) return TDM_ECUDA;
@@ -39,10 +40,9 @@ int extract_impl(tdm_ctx* c, const void* holos, int bits, int n, int a0, bool ar
         const char* src = static_cast<const char*>(holos) + (size_t)h0 * bytes_per;
         {
             Launch l(c, K_EXTRACT_ROWS);
-            rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.tuk_h, c->tuk_h_flat,
+            rows<<<C::grid_rows(m), C::NT, sm_rows, c->stream>>>(src, bits, c->b.win_h,
                                                                 c->use_ref ? c->b.ref_inv : nullptr, c->b.tw,
-                                                                c->b.inter, p.F,
-                                                                p.x0, c->b.err, c->wait_polls);
+                                                                c->b.inter, p.F, p.x0, c->b.err, c->wait_polls);
         }
         {
             Launch l(c, K_EXTRACT_COLS);

@@ -13,12 +13,13 @@
 // Mapping (retroPropag_Born, src/fonctions.cpp:875-935) as a gather: voxel
 // column (X, Y) reads bin kx = (X - D/2) mod F for every angle whose cap window
 // covers it; each angle hits a column at most once, so the column's sums are
-// formed without atomics, in a fixed order; hit counts are exact (k_accumulate).
+// formed without atomics, in a fixed order; hit counts are exact (k_gather_z).
 //
 // Volume: fftshift3D, backward 3D FFT x Delta_f^3, fftshift3D, x -1/(2 n0 kv^2)
 // (main.cpp:282-352).  For even D the two shifts are sign modulations:
 //     out[m] = (-1)^(mx+my+mz+3D/2) IFFT3((-1)^(kx+ky+kz) V)[m].
-// A z pass, a y pass and an x pass that writes the index and absorption volumes.
+// The z pass runs inside the gather (k_gather_z); then a y pass, and an x pass
+// that writes the index and absorption volumes.
 #include "tdm_internal.cuh"
 #include "fft_warp.cuh"
 #include "form.cuh"
@@ -166,37 +167,17 @@ k_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, cons
 // most 32 terms) before adding the sum.  The sums are deterministic, the hit
 // counts exact.  Widening the FP32 hits and narrowing the sums are done on
 // the integer pipe (fp_bits.cuh), so the FP64 pipe only adds.
-constexpr int kGW = 8;  // warps per CTA
 
-size_t gather_smem(int band, int n) { return gather_smem_bytes(band, n); }
-
-template <int D>
-__global__ void __launch_bounds__(kGW * 32)
-k_accumulate(const float2* __restrict__ rec, const int16_t* __restrict__ recz, const int2* __restrict__ posspec,
-             int M, Params p, float2* __restrict__ vol, uint32_t* __restrict__ cnt_out, int normalize) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ int s_wc[kGW];
-    __shared__ int s_listed;
-    const int band = p.band;
-    double2* acc_all = reinterpret_cast<double2*>(smraw);                   // kGW x band
-    float2* stg_all = reinterpret_cast<float2*>(acc_all + kGW * band);      // kGW x 32
-    uint16_t* cnt_all = reinterpret_cast<uint16_t*>(stg_all + kGW * 32);    // kGW x band
-    uint8_t* own_all = reinterpret_cast<uint8_t*>(cnt_all + kGW * band);    // kGW x band
-    int2* list = reinterpret_cast<int2*>(own_all + ((kGW * band + 7) & ~7));  // (q.x, angle), <= M
+// Lists, in ascending order, the angles whose window covers row Y (by = Y -
+// D/2) and one of the columns bx0 .. bx0 + 31 of the CTA: list[i] = (posSpec
+// x, angle).  Returns the count; all NW warps of the CTA call it together.
+template <int NW>
+__device__ __forceinline__ int list_angles(const int2* __restrict__ posspec, int M, int F, int by, int bx0, int2* list,
+                                           int* s_wc, int* s_listed) {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double2* acc = acc_all + w * band;
-    uint16_t* cnt = cnt_all + w * band;
-    uint8_t* own = own_all + w * band;
-    float2* stg = stg_all + w * 32;
-    const int F = p.F, h = D / 2, zmin = p.zmin;
-    const size_t FF = (size_t)F * F;
-    const int Y = blockIdx.y;
-    const int by = Y - h;
-    const int bx0 = blockIdx.x * 32 - h;
-    // the angles whose window covers row Y and one of the columns bx0 .. bx0 + 31
-    if (threadIdx.x == 0) s_listed = 0;
+    if (threadIdx.x == 0) *s_listed = 0;
     __syncthreads();
-    for (int a0 = 0; a0 < M; a0 += kGW * 32) {
+    for (int a0 = 0; a0 < M; a0 += NW * 32) {
         const int a = a0 + threadIdx.x;
         int2 q = make_int2(0, 0);
         bool keep = false;
@@ -207,98 +188,235 @@ k_accumulate(const float2* __restrict__ rec, const int16_t* __restrict__ recz, c
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) s_wc[w] = __popc(bal);
         __syncthreads();
-        int off = s_listed;
+        int off = *s_listed;
         for (int k = 0; k < w; ++k) off += s_wc[k];
         if (keep) list[off + __popc(bal & ((1u << lane) - 1u))] = make_int2(q.x, a);
         __syncthreads();
         if (threadIdx.x == 0) {
-            int t = s_listed;
-            for (int k = 0; k < kGW; ++k) t += s_wc[k];
-            s_listed = t;
+            int t = *s_listed;
+            for (int k = 0; k < NW; ++k) t += s_wc[k];
+            *s_listed = t;
         }
         __syncthreads();
     }
-    const int listed = s_listed;
-    for (int cx = 0; cx < 32; cx += kGW) {
-        const int X = blockIdx.x * 32 + cx + w;
-        const int bx = X - h;  // fd + N = X - D/2 + posSpec
-        const size_t koff = (size_t)(((by % F) + F) % F) * F + ((bx % F) + F) % F;  // bins of this column
-        for (int e = lane; e < band; e += 32) {
-            acc[e] = make_double2(0.0, 0.0);
-            cnt[e] = 0;
+    return *s_listed;
+}
+
+// One warp sums column (bx, by) of the listed angles into acc / cnt (band
+// entries, zeroed here): the cells' planes and values are read from the cap
+// records at koff, the bin of the column in each angle's F x F window.
+__device__ __forceinline__ void gather_column(const float2* __restrict__ rec, const int16_t* __restrict__ recz,
+                                              const int2* list, int listed, size_t FF, size_t koff, int bx, int F,
+                                              int zmin, int band, double2* acc, uint16_t* cnt, uint8_t* own,
+                                              float2* stg, int lane) {
+    for (int e = lane; e < band; e += 32) {
+        acc[e] = make_double2(0.0, 0.0);
+        cnt[e] = 0;
+    }
+    // plane of listed angle i's cell in this column, or -1 when the angle's
+    // window misses the column or the bin is outside its cap; the cap
+    // value of a cell with plane z
+    auto fetch_z = [&](int i) {
+        int z = -1;
+        if (i < listed) {
+            const int2 q = list[i];
+            if ((unsigned)(bx + q.x) < (unsigned)F) z = __ldg(&recz[(size_t)q.y * FF + koff]);
         }
-        // plane of listed angle i's cell in this column, or -1 when the angle's
-        // window misses the column or the bin is outside its cap; the cap
-        // value of a cell with plane z
-        auto fetch_z = [&](int i) {
-            int z = -1;
-            if (i < listed) {
-                const int2 q = list[i];
-                if ((unsigned)(bx + q.x) < (unsigned)F) z = __ldg(&recz[(size_t)q.y * FF + koff]);
-            }
-            return z;
-        };
-        auto fetch_v = [&](int i, int z) {
-            return z >= 0 ? __ldg(&rec[(size_t)list[i].y * FF + koff]) : make_float2(0.f, 0.f);
-        };
-        int z_nxt = fetch_z(lane), z_nxt2 = fetch_z(32 + lane);
-        float2 v_nxt = fetch_v(lane, z_nxt);
+        return z;
+    };
+    auto fetch_v = [&](int i, int z) {
+        return z >= 0 ? __ldg(&rec[(size_t)list[i].y * FF + koff]) : make_float2(0.f, 0.f);
+    };
+    int z_nxt = fetch_z(lane), z_nxt2 = fetch_z(32 + lane);
+    float2 v_nxt = fetch_v(lane, z_nxt);
+    __syncwarp();
+    for (int g0 = 0; g0 < listed; g0 += 32) {
+        const int z = z_nxt;
+        const float2 r = v_nxt;
+        z_nxt = z_nxt2;
+        v_nxt = fetch_v(g0 + 32 + lane, z_nxt);
+        z_nxt2 = fetch_z(g0 + 64 + lane);
+        const int e = z >= 0 ? z - zmin : -1;
+        if (!__any_sync(0xffffffffu, e >= 0)) continue;
+        if (e >= 0) own[e] = (uint8_t)lane;
         __syncwarp();
-        for (int g0 = 0; g0 < listed; g0 += 32) {
-            const int z = z_nxt;
-            const float2 r = v_nxt;
-            z_nxt = z_nxt2;
-            v_nxt = fetch_v(g0 + 32 + lane, z_nxt);
-            z_nxt2 = fetch_z(g0 + 64 + lane);
-            const int e = z >= 0 ? z - zmin : -1;
-            if (!__any_sync(0xffffffffu, e >= 0)) continue;
-            if (e >= 0) own[e] = (uint8_t)lane;
+        const bool shared_plane = e >= 0 && own[e] != lane;
+        if (!__any_sync(0xffffffffu, shared_plane)) {
+            if (e >= 0) {
+                double2 t = acc[e];
+                t.x += widen(r.x);
+                t.y += widen(r.y);
+                acc[e] = t;
+                cnt[e]++;
+            }
+        } else {
+            const unsigned grp = __match_any_sync(0xffffffffu, e >= 0 ? e : -1 - lane);
+            stg[lane] = make_float2(r.x, r.y);
             __syncwarp();
-            const bool shared_plane = e >= 0 && own[e] != lane;
-            if (!__any_sync(0xffffffffu, shared_plane)) {
-                if (e >= 0) {
-                    double2 t = acc[e];
-                    t.x += widen(r.x);
-                    t.y += widen(r.y);
-                    acc[e] = t;
-                    cnt[e]++;
+            if (e >= 0 && (grp & ((1u << lane) - 1)) == 0) {  // lowest lane of its plane group
+                float sx = 0.0f, sy = 0.0f;
+                for (unsigned g = grp; g; g &= g - 1) {
+                    const float2 u = stg[__ffs(g) - 1];
+                    sx += u.x;
+                    sy += u.y;
                 }
-            } else {
-                const unsigned grp = __match_any_sync(0xffffffffu, e >= 0 ? e : -1 - lane);
-                stg[lane] = make_float2(r.x, r.y);
+                double2 t = acc[e];
+                t.x += widen(sx);
+                t.y += widen(sy);
+                acc[e] = t;
+                cnt[e] += (uint16_t)__popc(grp);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Cell (X, Y, zmin + e) of the normalised spectrum from its sums (main.cpp:243-249;
+// not normalised for the adjoint scatter); (-1)^(X+Y+Z) stands for the first
+// fftshift3D.
+__device__ __forceinline__ float2 gather_cell(const double2* acc, const uint16_t* cnt, int e, int X, int Y, int zmin,
+                                              int normalize, unsigned& n) {
+    n = cnt[e];
+    float2 val = make_float2(0.0f, 0.0f);
+    if (n) {
+        const double2 t = acc[e];
+        const float dn = normalize ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
+        val = make_float2(narrow(t.x) / dn, narrow(t.y) / dn);
+    }
+    if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
+    return val;
+}
+
+// ---------------------------------------------------------------- gather fused with the z pass
+// k_gather_z: the cap gather and the inverse FFT along z (the first axis of
+// the 3D inverse FFT) in one kernel, so that the cap band (the planes of the
+// spectrum that caps reach) is neither written to HBM nor read back.  A CTA
+// of kGZ warps covers 32 consecutive columns (X) at one Y; a warp takes its
+// columns G = WarpFFT<D>::G at a time (the lanes of one column transform),
+// sums each with gather_column into its own FP64 sums, loads the G
+// normalised columns into registers (zero outside the band) and
+// inverse-transforms them along z together.  The transform's exchange
+// buffers (T (T + 1) slots per transform, fft_warp_regs_lean) overlay the
+// sums, which are in registers by then.  Each lane stores its outputs
+// directly (lane-minor order is contiguous in z) into the [y][x][z] volume.
+// The OTF mask (Re != 0 after normalisation, main.cpp:262-267) of the CTA's
+// 32 columns is collected as one bit per column and plane in shared memory
+// and stored as 32-byte rows; planes outside the band are cleared by the
+// host.
+constexpr int kGZ = 4;  // warps per CTA
+
+template <int D>
+struct GatherZ {
+    using W = WarpFFT<D>;
+    static constexpr int G = W::G, T = W::T, E = W::E;
+    static constexpr int COLS = 32 / kGZ;  // columns per warp
+    static_assert(COLS % G == 0, "a warp's columns split into groups of G");
+    // per-warp region: G sums (double2) and G counts (uint16) of the band, or,
+    // once the sums are in registers, the G exchange buffers
+    __host__ __device__ static size_t region(int band) {
+        const size_t sums = (size_t)G * band * (sizeof(double2) + sizeof(uint16_t));
+        const size_t xch = (size_t)G * T * (T + 1) * sizeof(float2);
+        return ((sums > xch ? sums : xch) + 15) & ~size_t(15);
+    }
+    __host__ __device__ static size_t own_bytes(int band) { return (size_t)((band + 15) & ~15); }
+    static size_t smem(int band, int n) {
+        return kGZ * (region(band) + 32 * sizeof(float2) + own_bytes(band)) + (((size_t)band * 4 + 7) & ~size_t(7)) +
+               (size_t)n * sizeof(int2);
+    }
+};
+
+template <int D>
+__global__ void __launch_bounds__(kGZ * 32, 5)
+k_gather_z(const float2* __restrict__ rec, const int16_t* __restrict__ recz, const int2* __restrict__ posspec, int M,
+           Params p, const float2* __restrict__ tw, float2* __restrict__ vol, uint32_t* __restrict__ cnt_out,
+           uint8_t* __restrict__ otf, int normalize) {
+    using Z = GatherZ<D>;
+    constexpr int G = Z::G, T = Z::T, E = Z::E;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ int s_wc[kGZ];
+    __shared__ int s_listed;
+    const int band = p.band;
+    const size_t reg = Z::region(band), ownb = Z::own_bytes(band);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* region = smraw + w * reg;
+    double2* acc0 = reinterpret_cast<double2*>(region);                  // G x band
+    uint16_t* cnt0 = reinterpret_cast<uint16_t*>(acc0 + G * band);      // G x band
+    float2* stg = reinterpret_cast<float2*>(smraw + kGZ * reg) + w * 32;
+    uint8_t* own = smraw + kGZ * (reg + 32 * sizeof(float2)) + w * ownb;
+    uint32_t* bits = reinterpret_cast<uint32_t*>(smraw + kGZ * (reg + 32 * sizeof(float2) + ownb));  // band
+    int2* list = reinterpret_cast<int2*>(reinterpret_cast<unsigned char*>(bits) + (((size_t)band * 4 + 7) & ~size_t(7)));
+    const int F = p.F, h = D / 2, zmin = p.zmin;
+    const size_t FF = (size_t)F * F;
+    const int Y = blockIdx.y, by = Y - h, X0 = blockIdx.x * 32;
+    if (otf)
+        for (int e = threadIdx.x; e < band; e += kGZ * 32) bits[e] = 0;  // ordered by list_angles' barriers
+    const int listed = list_angles<kGZ>(posspec, M, F, by, X0 - h, list, s_wc, &s_listed);
+    const int g = lane / T, j = lane % T;  // this lane's transform of the group, and its lane in it
+    for (int r = 0; r < Z::COLS / G; ++r) {
+#pragma unroll 1
+        for (int gg = 0; gg < G; ++gg) {
+            const int X = X0 + w + kGZ * (r * G + gg);
+            const int bx = X - h;
+            const size_t koff = (size_t)(((by % F) + F) % F) * F + ((bx % F) + F) % F;
+            double2* acc = acc0 + gg * band;
+            const uint16_t* cnt = cnt0 + gg * band;
+            gather_column(rec, recz, list, listed, FF, koff, bx, F, zmin, band, acc, cnt0 + gg * band, own, stg,
+                          lane);
+            // normalised cells, in place: cell e's float2 goes to bytes [8e, 8e + 8), over sums of cells
+            // below the current 32, which have been read (a rolled loop keeps the kernel's code small)
+            float2* cell = reinterpret_cast<float2*>(acc);
+            for (int e0 = 0; e0 < band; e0 += 32) {
+                const int e = e0 + lane;
+                float2 v = make_float2(0.f, 0.f);
+                if (e < band) {
+                    unsigned n;
+                    v = gather_cell(acc, cnt, e, X, Y, zmin, normalize, n);
+                    if (cnt_out) cnt_out[((size_t)(zmin + e) * D + Y) * D + X] = n;
+                    if (otf && v.x != 0.0f) atomicOr(&bits[e], 1u << (X - X0));
+                }
                 __syncwarp();
-                if (e >= 0 && (grp & ((1u << lane) - 1)) == 0) {  // lowest lane of its plane group
-                    float sx = 0.0f, sy = 0.0f;
-                    for (unsigned g = grp; g; g &= g - 1) {
-                        const float2 u = stg[__ffs(g) - 1];
-                        sx += u.x;
-                        sy += u.y;
-                    }
-                    double2 t = acc[e];
-                    t.x += widen(sx);
-                    t.y += widen(sy);
-                    acc[e] = t;
-                    cnt[e] += (uint16_t)__popc(grp);
-                }
+                if (e < band) cell[e] = v;
             }
-            __syncwarp();
-        }
-        // normalise (main.cpp:243-249; not for the adjoint scatter); (-1)^(X+Y+Z)
-        // stands for the first fftshift3D
-        float2* col = vol + ((size_t)Y * D + X) * D + zmin;
-        for (int e = lane; e < band; e += 32) {
-            const unsigned n = cnt[e];
-            float2 val = make_float2(0.0f, 0.0f);
-            if (n) {
-                const double2 t = acc[e];
-                const float dn = normalize ? (float)n : 1.0f;  // FP32 division: FP64 division is a long sequence here
-                val = make_float2(narrow(t.x) / dn, narrow(t.y) / dn);
-            }
-            if ((X + Y + zmin + e) & 1) val = make_float2(-val.x, -val.y);
-            col[e] = val;
-            if (cnt_out) cnt_out[((size_t)(zmin + e) * D + Y) * D + X] = n;
         }
         __syncwarp();
+        const int X = X0 + w + kGZ * (r * G + g);
+        const float2* cell = reinterpret_cast<const float2*>(acc0 + g * band);
+        float2 x[E];
+#pragma unroll
+        for (int n1 = 0; n1 < E; ++n1) {
+            const int e = j + n1 * T - zmin;
+            x[n1] = (unsigned)e < (unsigned)band ? cell[e] : make_float2(0.f, 0.f);
+        }
+        // the exchange buffers overlay the sums: every lane has read its column (the transform's first __syncwarp)
+        fft_warp_regs_lean<D, +1>(x, reinterpret_cast<float2*>(region) + g * T * (T + 1), j, tw);
+        float2* col = vol + ((size_t)Y * D + X) * D;
+#pragma unroll
+        for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+            for (int k2 = 0; k2 < T; ++k2) col[j + q * T + E * k2] = x[q * T + k2];
+        }
+        __syncwarp();  // the next group's sums overlay the exchange buffers
+    }
+    if (otf) {
+        __syncthreads();
+        uint8_t* o = otf + (size_t)Y * D + X0;
+        const size_t plane = (size_t)D * D;
+        if ((reinterpret_cast<uintptr_t>(otf) & 15) == 0) {
+            for (int i = threadIdx.x; i < 2 * band; i += kGZ * 32) {  // 16 columns' flags per store
+                const uint32_t b = bits[i >> 1] >> (16 * (i & 1));
+                uint32_t v[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const uint32_t nib = (b >> (4 * t)) & 0xFu;
+                    v[t] = (nib & 1u) | ((nib & 2u) << 7) | ((nib & 4u) << 14) | ((nib & 8u) << 21);
+                }
+                *reinterpret_cast<uint4*>(o + (size_t)(zmin + (i >> 1)) * plane + 16 * (i & 1)) =
+                    make_uint4(v[0], v[1], v[2], v[3]);
+            }
+        } else {
+            for (int i = threadIdx.x; i < 32 * band; i += kGZ * 32)
+                o[(size_t)(zmin + i / 32) * plane + i % 32] = (uint8_t)((bits[i / 32] >> (i % 32)) & 1u);
+        }
     }
 }
 
@@ -309,49 +427,6 @@ struct PassCfg {
     static constexpr int NT = B * W::T;    // threads per CTA
     static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
-
-// Inverse FFT along z (contiguous) for B consecutive columns of the [y][x][z]
-// volume; planes outside the cap band are zero and are not read.  Each lane
-// loads and stores its elements directly (lane-minor order is contiguous in
-// z).  The OTF mask (Re != 0 after normalisation, main.cpp:262-267) is taken
-// from the spectrum values loaded here: B consecutive columns are B
-// consecutive x at one y, written as one 16-byte row per plane.
-template <int D>
-__global__ void __launch_bounds__(PassCfg<D>::NT)
-k_zpass(float2* __restrict__ vol, const float2* __restrict__ tw, int zmin, int band, uint8_t* __restrict__ otf) {
-    using C = PassCfg<D>;
-    using W = typename C::W;
-    constexpr int B = C::B, T = W::T, E = W::E;
-    extern __shared__ float2 sm[];
-    uint8_t* flags = reinterpret_cast<uint8_t*>(sm + B * W::STRIDE);  // D x B
-    const int t = threadIdx.x / T, j = threadIdx.x % T;
-    const size_t c0 = (size_t)blockIdx.x * B;
-    float2* col = vol + (c0 + t) * D;
-    float2 x[E];
-#pragma unroll
-    for (int n1 = 0; n1 < E; ++n1) {
-        const int Z = j + n1 * T;
-        x[n1] = (Z >= zmin && Z < zmin + band) ? col[Z] : make_float2(0.f, 0.f);
-        if (otf) flags[Z * B + t] = x[n1].x != 0.0f ? 1 : 0;
-    }
-    fft_warp_regs<D, +1>(x, sm + t * W::STRIDE, j, tw);
-#pragma unroll
-    for (int q = 0; q < E / T; ++q) {
-#pragma unroll
-        for (int k2 = 0; k2 < T; ++k2) col[j + q * T + E * k2] = x[q * T + k2];
-    }
-    if (otf) {
-        __syncthreads();
-        uint8_t* o = otf + c0;
-        const size_t plane = (size_t)D * D;
-        if ((reinterpret_cast<uintptr_t>(otf) & 15) == 0) {
-            for (int Z = threadIdx.x; Z < D; Z += C::NT)
-                *reinterpret_cast<uint4*>(o + Z * plane) = *reinterpret_cast<const uint4*>(flags + Z * B);
-        } else {
-            for (int i = threadIdx.x; i < D * B; i += C::NT) o[(i / B) * plane + i % B] = flags[i];
-        }
-    }
-}
 
 // Inverse FFT along y, in place, for B consecutive z at fixed x.
 template <int D, int DIR>
@@ -417,8 +492,8 @@ k_xpass(const float2* __restrict__ vol, const float2* __restrict__ tw, float sca
 // is A = S G with G = T^-1 = M_in FFT3(M_out x) / (s D^3) and S the sampling
 // of each angle's cap cells (the cells the gather fills, same geometry); its
 // adjoint is A^H = G^H S^H, G^H = M_out IFFT3(M_in .) / (s D^3) and S^H the
-// unnormalised scatter, i.e. k_accumulate without the division by the hit
-// count followed by the z, y and x passes with scale 1 / (s D^3).
+// unnormalised scatter, i.e. k_gather_z without the division by the hit
+// count, followed by the y and x passes with scale 1 / (s D^3).
 
 // Forward x pass: FFT along x of B consecutive z rows at fixed y of the
 // index/absorption volumes (x M_out x scale), into the [y][x][z] spectrum.
@@ -645,39 +720,40 @@ int volume_impl(tdm_ctx* c, int n, const VolumeOut& out, cudaStream_t st, CapRec
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    const size_t sm_a = gather_smem(p.band, n);
-    const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
+    const size_t sm_a = GatherZ<D>::smem(p.band, n);
+    const size_t sm_p = P::SMEM;
     if (sm_a > kMaxSmemPerCta) return TDM_EUNSUPPORTED;
-    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
-        allow_smem(k_xpass<D>, sm_p))
+    if (allow_smem(k_gather_z<D>, sm_a) || allow_smem(k_ypass<D, 1>, sm_p) || allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
     // A staged output part may still be downloading from the previous volume:
     // each part's writer waits for that part's download (ev_dl) just before it runs.
     auto staged_free = [&](int part) { return cudaStreamWaitEvent(st, c->ev_dl[part], 0); };
     auto downloaded = [&](int part) { return cudaEventRecord(c->ev_dl[part], c->dl_stream); };
     if (out.host_cnt && staged_free(kOutSlabs)) return TDM_ECUDA;
-    if (cnt) {  // planes outside the cap band carry no hits
-        const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
+    if (out.host_otf && staged_free(kOutSlabs + 1)) return TDM_ECUDA;
+    // planes outside the cap band carry no hits and no OTF support
+    const size_t plane = (size_t)D * D, lo = (size_t)p.zmin * plane, hi = (size_t)(p.zmin + p.band) * plane;
+    const size_t NT = (size_t)D * D * D;
+    if (cnt) {
         cudaMemsetAsync(cnt, 0, lo * sizeof(uint32_t), st);
-        cudaMemsetAsync(cnt + hi, 0, ((size_t)D * plane - hi) * sizeof(uint32_t), st);
+        cudaMemsetAsync(cnt + hi, 0, (NT - hi) * sizeof(uint32_t), st);
+    }
+    if (otf) {
+        cudaMemsetAsync(otf, 0, lo, st);
+        cudaMemsetAsync(otf + hi, 0, NT - hi, st);
     }
     cudaEventRecord(c->ev_stage[4], st);
     {
         Launch l(c, K_GATHER, st);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, st>>>(rec.val, rec.z, posspec, n, p, b.vol, cnt, 1);
+        k_gather_z<D><<<dim3(D / 32, D), kGZ * 32, sm_a, st>>>(rec.val, rec.z, posspec, n, p, b.tw, b.vol, cnt, otf,
+                                                                 1);
     }
     cudaEventRecord(c->ev_stage[5], st);
     if (ev_gathered && cudaEventRecord(ev_gathered, st)) return TDM_ECUDA;
-    const size_t NT = (size_t)D * D * D;
     if (out.host_cnt) {
         if (download_after(c, st, c->ev_out[kOutSlabs], out.host_cnt, cnt, NT * sizeof(uint32_t)) ||
             downloaded(kOutSlabs))
             return TDM_ECUDA;
-    }
-    if (out.host_otf && staged_free(kOutSlabs + 1)) return TDM_ECUDA;
-    {
-        Launch l(c, K_ZPASS, st);
-        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, st>>>(b.vol, b.tw, p.zmin, p.band, otf);
     }
     if (out.host_otf) {
         if (download_after(c, st, c->ev_out[kOutSlabs + 1], out.host_otf, otf, NT) || downloaded(kOutSlabs + 1))
@@ -750,20 +826,15 @@ int adjoint_impl(tdm_ctx* c, CapRecs recs, int n, float* xn, float* xk, bool nor
     using P = PassCfg<D>;
     Buffers& b = c->b;
     const Params& p = c->p;
-    const size_t sm_a = gather_smem(p.band, n);
-    const size_t sm_p = P::SMEM, sm_z = P::SMEM + (size_t)D * P::B;
+    const size_t sm_a = GatherZ<D>::smem(p.band, n);
+    const size_t sm_p = P::SMEM;
     if (sm_a > kMaxSmemPerCta) return TDM_EUNSUPPORTED;
-    if (allow_smem(k_accumulate<D>, sm_a) || allow_smem(k_zpass<D>, sm_z) || allow_smem(k_ypass<D, 1>, sm_p) ||
-        allow_smem(k_xpass<D>, sm_p))
+    if (allow_smem(k_gather_z<D>, sm_a) || allow_smem(k_ypass<D, 1>, sm_p) || allow_smem(k_xpass<D>, sm_p))
         return TDM_ECUDA;
     {
         Launch l(c, K_GATHER);
-        k_accumulate<D><<<dim3(D / 32, D), kGW * 32, sm_a, c->stream>>>(recs.val, recs.z, b.posspec, n, p, b.vol,
-                                                                         nullptr, normalize ? 1 : 0);
-    }
-    {
-        Launch l(c, K_ZPASS);
-        k_zpass<D><<<dim3(D * D / P::B), P::NT, sm_z, c->stream>>>(b.vol, b.tw, p.zmin, p.band, nullptr);
+        k_gather_z<D><<<dim3(D / 32, D), kGZ * 32, sm_a, c->stream>>>(recs.val, recs.z, b.posspec, n, p, b.tw, b.vol,
+                                                                        nullptr, nullptr, normalize ? 1 : 0);
     }
     {
         Launch l(c, K_YPASS);
@@ -779,11 +850,16 @@ int adjoint_impl(tdm_ctx* c, CapRecs recs, int n, float* xn, float* xk, bool nor
 
 }  // namespace
 
-// Dynamic shared memory of k_accumulate: per warp the band's sums, counts and
-// owners plus a 32-lane staging row, and the CTA's list of n angles at most.
-size_t gather_smem_bytes(int band, int n) {
-    return (size_t)kGW * band * sizeof(double2) + (size_t)kGW * 32 * sizeof(float2) +
-           (size_t)kGW * band * sizeof(uint16_t) + (size_t)((kGW * band + 7) & ~7) + (size_t)n * sizeof(int2);
+// Dynamic shared memory of k_gather_z: per warp the sums and counts of its
+// column group (or their exchange buffers), its plane owners and a 32-lane
+// staging row; the CTA's OTF bits and its list of n angles at most.
+size_t gather_smem_bytes(int D, int band, int n) {
+    switch (D) {
+        case 128: return GatherZ<128>::smem(band, n);
+        case 256: return GatherZ<256>::smem(band, n);
+        case 512: return GatherZ<512>::smem(band, n);
+        default: return GatherZ<1024>::smem(band, n);
+    }
 }
 
 int launch_cap(tdm_ctx* c, int a0, int n, bool form) {

@@ -78,7 +78,7 @@ int dev_alloc(tdm_ctx* c, T** p, size_t count) {
 
 void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
-    void* ptrs[] = {b.tw, b.tuk_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
+    void* ptrs[] = {b.tw, b.win_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
                     b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0].val, b.rec_buf[0].z, b.rec_buf[1].val,
                     b.rec_buf[1].z, b.posspec_vol[0], b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
@@ -286,10 +286,10 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         fprintf(stderr, "tdm_create: Ewald caps exceed the DIM_FINAL volume along z\n");
         return TDM_EUNSUPPORTED;
     }
-    if (gather_smem_bytes(p.band, max_angles) > kMaxSmemPerCta) {
+    if (gather_smem_bytes(D, p.band, max_angles) > kMaxSmemPerCta) {
         // the gather keeps each CTA's list of angles in shared memory
         int most = 0;
-        while (gather_smem_bytes(p.band, most + 1) <= kMaxSmemPerCta) ++most;
+        while (gather_smem_bytes(D, p.band, most + 1) <= kMaxSmemPerCta) ++most;
         delete c;
         fprintf(stderr, "tdm_create: at most %d angles for this geometry (the cap gather's angle list of a "
                         "%d-plane cap band must fit one CTA's shared memory)\n", most, p.band);
@@ -347,7 +347,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F, M = max_angles, CH = c->chunk_cap, L = p.L;
     TRY(dev_alloc(c, &b.tw, kTwTotal));
-    TRY(dev_alloc(c, &b.tuk_h, p.H));
+    TRY(dev_alloc(c, &b.win_h, p.H));
     TRY(dev_alloc(c, &b.tuk_f, F));
     TRY(dev_alloc(c, &b.s_tab, FF));
     TRY(dev_alloc(c, &b.s_tabf, FF));
@@ -383,10 +383,11 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.err, 4));
     // tables
     const std::vector<float2> tw = twiddle_table();
-    std::vector<double> th = tukey_factor(p.H, 0.05f), tf = tukey_factor(F, 0.1f);
+    const std::vector<float2> wh = hologram_window(p.H);
+    std::vector<double> tf = tukey_factor(F, 0.1f);
     c->tuk_h_flat = tukey_flat(p.H, 0.05f);
     c->tuk_f_flat = tukey_flat(F, 0.1f);
-    std::vector<float> thf(th.begin(), th.end()), tff(tf.begin(), tf.end());
+    std::vector<float> tff(tf.begin(), tf.end());
     std::vector<float> stabf(stab.begin(), stab.end());
     std::vector<float2> wq(4 * F);  // exp(-2 pi i k / 4F), for the mixed-radix passes
     for (int k = 0; k < 4 * F; ++k) {
@@ -394,7 +395,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         wq[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
     if (cudaMemcpy(b.tw, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b.tuk_h, thf.data(), p.H * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b.win_h, wh.data(), p.H * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.tuk_f, tff.data(), F * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tab, stab.data(), FF * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b.s_tabf, stabf.data(), FF * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||

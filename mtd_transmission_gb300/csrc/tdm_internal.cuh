@@ -44,7 +44,7 @@ struct Params {
 // Device buffers (all owned by the context).
 struct Buffers {
     float2* tw = nullptr;          // kTwTotal twiddles (twiddle_table)
-    float* tuk_h = nullptr;        // H, hologram Tukey alpha 0.05 (1D factor)
+    float2* win_h = nullptr;       // H, hologram window with sign (hologram_window)
     float* ref_inv = nullptr;      // H*H, 1 / reference amplitude (tdm_set_reference_intensity), on first use
     float* tuk_f = nullptr;        // F, field Tukey alpha 0.1 (1D factor)
     double* s_tab = nullptr;       // F*F, sqrt(rayon^2 - fd^2) at [fdy+N][fdx+N]
@@ -156,7 +156,7 @@ struct tdm_ctx {
 namespace tdm {
 // Dynamic shared memory of the cap gather for a cap band of `band` planes and
 // n angles (the CTA keeps its list of angles in shared memory).
-size_t gather_smem_bytes(int band, int n);
+size_t gather_smem_bytes(int D, int band, int n);
 constexpr size_t kMaxSmemPerCta = 227 * 1024;
 // Scope around one kernel launch on c->stream: counts the launch and, when
 // profiling is on, brackets it with a pair of CUDA events.

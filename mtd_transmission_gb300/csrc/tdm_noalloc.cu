@@ -9,6 +9,7 @@
 // scratch (the row-pass intermediate) in a fixed array compiled into this
 // library.  Every GPU that loads the library holds that array until the
 // process exits.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -24,13 +25,13 @@ using namespace tdm::extract;
 
 constexpr size_t kScratchBytes = size_t(4) << 20;  // 4 MiB: one 2048 x 256 band, or two 1024 x 256
 constexpr int kMaxH = 2048;
-constexpr int kTukeyLen = 256 + 512 + 1024 + 2048;  // one table per supported CCD_ROIX
+constexpr int kWindowLen = 256 + 512 + 1024 + 2048;  // one window table per supported CCD_ROIX
 
 static __device__ __align__(256) float2 g_scratch[kScratchBytes / sizeof(float2)];
 static __device__ __align__(256) float2 g_twiddle[kTwTotal];
-static __device__ __align__(256) float g_tukey[kTukeyLen];
+static __device__ __align__(256) float2 g_window[kWindowLen];
 
-int tukey_offset(int H) { return H - 256; }  // 256 -> 0, 512 -> 256, 1024 -> 768, 2048 -> 1792
+int window_offset(int H) { return H - 256; }  // 256 -> 0, 512 -> 256, 1024 -> 768, 2048 -> 1792
 
 // Device addresses of the arrays above.  In host code the array names are
 // host-side stand-ins, not device addresses, so they are looked up once per
@@ -39,7 +40,7 @@ struct Symbols {
     bool ready = false;
     float2* scratch = nullptr;
     float2* twiddle = nullptr;
-    float* tukey = nullptr;
+    float2* window = nullptr;
 };
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -52,21 +53,21 @@ int device_symbols(int dev, Symbols& out) {
     if (!s.ready) {
         if (cudaGetSymbolAddress(reinterpret_cast<void**>(&s.scratch), g_scratch) != cudaSuccess ||
             cudaGetSymbolAddress(reinterpret_cast<void**>(&s.twiddle), g_twiddle) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void**>(&s.tukey), g_tukey) != cudaSuccess) {
+            cudaGetSymbolAddress(reinterpret_cast<void**>(&s.window), g_window) != cudaSuccess) {
             cudaGetLastError();
             return TDM_ECUDA;
         }
         const std::vector<float2> tw = twiddle_table();
-        std::vector<float> tk(kTukeyLen);
+        std::vector<float2> wt(kWindowLen);
         for (int H = 256; H <= kMaxH; H *= 2) {
-            const std::vector<double> t = tukey_factor(H, 0.05f);  // hologram window, main.cpp:105
-            for (int i = 0; i < H; ++i) tk[tukey_offset(H) + i] = (float)t[i];
+            const std::vector<float2> t = hologram_window(H);  // hologram window, main.cpp:105
+            std::copy(t.begin(), t.end(), wt.begin() + window_offset(H));
         }
         // A copy from pageable host memory may return before the data has
         // reached the device; the tables must be complete before any kernel
         // on any stream (or another thread that sees ready) reads them.
         if (cudaMemcpy(s.twiddle, tw.data(), kTwTotal * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(s.tukey, tk.data(), kTukeyLen * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s.window, wt.data(), kWindowLen * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaDeviceSynchronize() != cudaSuccess) {
             cudaGetLastError();
             return TDM_ECUDA;
@@ -92,6 +93,7 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
         cudaStream_t st) {
     using C = ExtractCfg<H>;
     const size_t sm_rows = C::smem_rows(F), sm_cols = C::smem_cols(F);
+    if (!window_edge_ok(H, tukey_flat(H, 0.05f), win_edge<H>())) return TDM_EUNSUPPORTED;
     if (sm_rows > 48 * 1024 &&
         cudaFuncSetAttribute(k_extract_rows<H, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows))
         return TDM_ECUDA;
@@ -104,9 +106,8 @@ int run(const Symbols& s, const void* holos, int bits, int n, float2* out, int F
     for (int h0 = 0; h0 < n; h0 += chunk) {
         const int m = n - h0 < chunk ? n - h0 : chunk;
         k_extract_rows<H, false><<<C::grid_rows(m), C::NT, sm_rows, st>>>(
-            static_cast<const char*>(holos) + h0 * in_bytes, bits, s.tukey + tukey_offset(H), tukey_flat(H, 0.05f),
-            nullptr, s.twiddle, s.scratch, F,
-            x0, nullptr, 0u);
+            static_cast<const char*>(holos) + h0 * in_bytes, bits, s.window + window_offset(H), nullptr, s.twiddle,
+            s.scratch, F, x0, nullptr, 0u);
         k_extract_cols<H><<<C::grid_cols(F, m), C::NT, sm_cols, st>>>(
             s.scratch, s.twiddle, out + (size_t)h0 * F * F, F, x0, y0, nullptr);
     }

@@ -39,7 +39,7 @@ def test_stage_roofline_arithmetic():
     acq, _, _ = simul.workload("rytov_1024")
     hits = _hits(acq.nxmax)
     kern = {"extract_rows": 1.0, "extract_cols": 0.5, "field_rows": 0.25, "volkov_cols": 0.75,
-            "cap_rows": 0.5, "cap_cols": 0.5, "gather": 0.5, "zpass": 0.25, "ypass": 0.5, "xpass": 0.5}
+            "cap_rows": 0.5, "cap_cols": 0.5, "gather": 0.75, "ypass": 0.5, "xpass": 0.5}
     r = bench.stage_roofline(acq, hits, kern, 5.0, 6787.6)
     b = bench.stage_bytes(acq, hits)
     for st, t in (("extraction", 1.5), ("fields", 1.0), ("cap_mapping", 1.0), ("volume", 1.75)):

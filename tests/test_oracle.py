@@ -52,6 +52,19 @@ def test_tukey_float_semantics(n, alpha):
     np.testing.assert_array_equal(oracle.tukey2d(n, alpha), _tukey_numpy(n, alpha))
 
 
+@pytest.mark.parametrize("n", [256, 512, 1024, 2048])
+def test_hologram_window_flat_where_the_row_pass_skips_it(n):
+    """The extraction's row pass reads the hologram window only for the first
+    and last K of each lane's E elements (x = j + T n1, T = n / E; K = 2 at
+    2048 points, else 1) and takes it as exactly 1 elsewhere; the window of
+    tukey2D (alpha 0.05) is exactly 1 on that whole middle."""
+    e = 64 if n >= 2048 else 32 if n >= 512 else 16
+    t_lanes, k = n // e, (2 if n >= 2048 else 1)
+    t = _tukey_numpy(n, 0.05)[n // 2]
+    assert np.all(t[t_lanes * k:n - t_lanes * k] == 1.0)
+    assert t[0] != 1.0 and t[-1] != 1.0
+
+
 def test_coord_spec_quirk():
     F = 16
     s = np.zeros((F, F), np.complex128)
