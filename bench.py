@@ -127,10 +127,13 @@ def stage_roofline(acq, hits_per_angle, kern_ms, step_ms, peak):
 # DRAM bytes (read + write) per launch from the committed ncu capture of
 # the kernel on this code (the file named in the returned source), as
 # (bytes that do not depend on the angle count, bytes per 600 angles): the
-# row pass on the 64-hologram case (a launch processes 16 holograms).  None
-# where no capture of this workload's kernel is committed.
+# row pass on the 64-hologram case (a launch processes 16 holograms), the
+# gather on the 600-angle workload (its record reads grow with the angles;
+# its volume and OTF writes do not).  None where no capture of this
+# workload's kernel is committed.
 NCU_TRAFFIC = {
     "extract_rows": (33.616128e6 + 0.341504e6, 0.0, "profiles/k_extract_rows_rytov_1024_64holos.md"),
+    "gather": (1083.210e6, 393.620e6, "profiles/k_gather_z_rytov_1024.md"),
 }
 
 

@@ -251,7 +251,8 @@ int tdm_batch_destroy(tdm_batch* batch);
 int tdm_extract_noalloc(const tdm_geom* geom, const void* holos, int bits, int n, float* spectra_out, void* stream);
 
 /* Planes of the D^3 spectrum that the Ewald caps can reach, [zmin, zmin +
- * band): the gather writes only these and the z pass reads only these.
+ * band): the gather sums only these, and its z transform takes the other
+ * planes as zero.
  * Diagnostic; no counterpart in the reference. */
 int tdm_cap_planes(const tdm_ctx* ctx, int* zmin, int* band);
 
