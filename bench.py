@@ -248,7 +248,7 @@ def cpu_baseline(acq, ph, seed, sample_angles: int, threads: int):
     import numpy as np
 
     import oracle
-    from mtd_transmission_gb300 import simul
+    from tests import simul
     from tests.helpers import oracle_cfg
     oracle.set_threads(threads)
     cfg = oracle_cfg(acq)
@@ -305,7 +305,6 @@ def fft_check(acq, threads: int):
 def run_reference(args, acq, ph, seed):
     threads = os.cpu_count() or 1
     import oracle
-    from mtd_transmission_gb300 import simul  # noqa: F401
     oracle.build()
     S = args.ref_sample
     # warm-up steps include the one-off volume stage measurement
@@ -346,7 +345,8 @@ def tv_form(iterations: int = 50, segment: int = 5):
     import numpy as np
     import torch
 
-    from mtd_transmission_gb300 import Context, Geometry, simul
+    from mtd_transmission_gb300 import Context, Geometry
+    from tests import simul
     acq, _, _ = simul.workload("plain_512_born")
     M = 400
     acq = replace(acq, nb_holo=M)
@@ -405,7 +405,8 @@ def batched_form(count: int = 8, seed: int = 2, rounds: int = 3):
     import numpy as np
     import torch
 
-    from mtd_transmission_gb300 import Batch, Context, Geometry, simul
+    from mtd_transmission_gb300 import Batch, Context, Geometry
+    from tests import simul
     rng = np.random.default_rng(seed)
     specs, stacks, ctxs = [], [], []
     for i in range(count):
@@ -542,7 +543,7 @@ def main():
 
     from dataclasses import replace
 
-    from mtd_transmission_gb300 import simul
+    from tests import simul
     acq, ph, seed = simul.workload(args.workload)
     if args.holograms:
         acq = replace(acq, nb_holo=args.holograms)

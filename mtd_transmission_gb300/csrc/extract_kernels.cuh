@@ -15,9 +15,8 @@ namespace extract {
 // keeps the crop's kx band, written column-major (inter[a][c][y]): the two
 // rows' values of one column are one 16-byte word, and the CTA's row pairs
 // fill one segment of each column, stored whole from a shared-memory tile
-// (16-byte pieces of distinct lines, one per lane, cost the L1 a wavefront
-// each and L2 a partial-sector write; the tile took both passes from 1.83 to
-// 1.80 ms per 600 holograms and the step from 5.32 to 5.26 ms).  The column pass
+// (16-byte pieces of distinct lines, one per lane, would cost the L1 a
+// wavefront each and L2 a partial-sector write).  The column pass
 // then reads whole columns contiguously and writes the crop rows through a
 // shared-memory tile (and, on request, the crop's partial specular-peak
 // winners, one record per warp).

@@ -6,7 +6,7 @@ from dataclasses import replace
 import numpy as np
 
 import oracle
-from mtd_transmission_gb300 import simul
+from tests import simul
 
 ORACLE_KEYS = ("ccd_roix", "nxmax", "circle_cx", "circle_cy", "dim_final", "na", "n0", "lambda0", "f_tube", "f_obj",
                "tpcam", "rf", "born", "c_aber", "deroul", "volkov", "coef_na_obj_limit")

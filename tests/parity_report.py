@@ -74,7 +74,7 @@ def run(name, workload, over, M=8):
 
 def run_full(workload):
     import torch
-    from mtd_transmission_gb300 import simul
+    from tests import simul
     from tests.test_gpu_full_size import _dot_product
     acq, ph, seed = simul.workload(workload)
     data = simul.holograms(acq, ph, seed=seed, device="cuda")

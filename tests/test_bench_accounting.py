@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import bench
-from mtd_transmission_gb300 import simul
+from tests import simul
 
 
 def _hits(nxmax):

@@ -17,7 +17,8 @@ import math
 import numpy as np
 import pytest
 
-from mtd_transmission_gb300 import Geometry, api, simul
+from mtd_transmission_gb300 import Geometry, api
+from tests import simul
 
 
 def _round_away(x):

@@ -16,7 +16,8 @@ import numpy as np
 import pytest
 
 import oracle
-from mtd_transmission_gb300 import Context, Geometry, simul
+from mtd_transmission_gb300 import Context, Geometry
+from tests import simul
 from tests.helpers import oracle_cfg, rel_l2
 
 pytestmark = pytest.mark.gpu

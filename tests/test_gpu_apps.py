@@ -11,7 +11,7 @@ import pytest
 
 import oracle
 from mtd_transmission_gb300 import build as tdm_build
-from mtd_transmission_gb300 import simul
+from tests import simul
 from tests.helpers import oracle_cfg, rel_l2, small_case
 from tests.test_host_io import _read_hdf5, _read_tiff, _write_pgm
 

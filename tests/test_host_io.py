@@ -17,7 +17,8 @@ import numpy as np
 import pytest
 
 import oracle
-from mtd_transmission_gb300 import api, simul
+from mtd_transmission_gb300 import api
+from tests import simul
 from mtd_transmission_gb300.api import Geometry
 from tests.helpers import oracle_cfg
 

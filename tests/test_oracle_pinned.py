@@ -101,7 +101,7 @@ def test_volkov_unwrap_up_to_the_zero_frequency_piston(case, request):
 
 
 def test_reconstruction_parameters():
-    from mtd_transmission_gb300 import simul
+    from tests import simul
     for name in ("plain_512_born", "rytov_1024", "large_2048"):
         acq, _, _ = simul.workload(name)
         cfg = oracle_cfg(acq)
