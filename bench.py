@@ -744,11 +744,13 @@ def main():
                             f"{E2E_TRIALS} trials of {args.e2e_steps} volumes",
                     "trials": [round(v, 3) for v in e2e_trials],
                     # host time spent inside the pipeline_async calls of each trial, per volume
+                    # (including time blocked on full launch queues while the GPU catches up)
                     "enqueue_ms_per_step": [round(1e3 * s / args.e2e_steps, 3) for s in e2e_enqueue_s],
                     "sync_value": round(e2e_sync, 3) if e2e_sync else None,
                     "sync_mode": "tdm_pipeline per step, each call returns with the volume in host memory"},
             "gpu_launches": int(launches),
-            # host time spent inside the K pipeline calls, per step (the calls queue work and return)
+            # host time spent inside the K pipeline calls, per step: the calls queue work and return,
+            # but block while launch queues are full, so this is an upper bound on the host cost
             "enqueue_ms_per_step": round(1e3 * t_enq / args.steps, 3),
             "roofline": roof,
             "roofline_all": roof_all,

@@ -278,8 +278,8 @@ int tdm_set_schedule(tdm_ctx* ctx, int chunk, int lanes);
 
 /* Project autotuner (no counterpart in the reference): times tdm_pipeline on
  * the given stack (device holograms) with the schedules (chunk, lanes) = (16, 4),
- * (16, 2), (8, 4), (12, 4), (32, 2) and (16, 6) that fit the context's scratch
- * and keeps the fastest; *chunk_out receives its chunk. */
+ * (16, 2), (8, 4), (12, 4), (32, 2), (16, 6) and (32, 4) that fit the context's
+ * scratch and keeps the fastest; *chunk_out receives its chunk. */
 int tdm_autotune(tdm_ctx* ctx, const void* holos, int bits, int n, int* chunk_out);
 
 /* Stream-ordered execution helpers.  tdm_pipeline queues each volume's stage

@@ -1139,7 +1139,7 @@ int tdm_autotune(tdm_ctx* c, const void* holos, int bits, int n, int* chunk_out)
         return fail(c, TDM_EINVAL, "tdm_autotune: invalid argument (device holograms required)");
     cudaSetDevice(c->device);
     if (int rc = tdm_synchronize(c)) return rc;
-    const int cands[][2] = {{16, 4}, {16, 2}, {8, 4}, {12, 4}, {32, 2}, {16, 6}};
+    const int cands[][2] = {{16, 4}, {16, 2}, {8, 4}, {12, 4}, {32, 2}, {16, 6}, {32, 4}};
     int best = c->chunk, best_lanes = c->lanes;
     float best_ms = 0;
     cudaEvent_t t0 = prof_event(c), t1 = prof_event(c);
