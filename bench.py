@@ -228,6 +228,46 @@ def max_over_ranks(values, world: int, device):
     return t.tolist()
 
 
+def host_link_probe(h_in, d_in, pairs_out, reps: int = 3, chunk: int = 32 << 20):
+    """Copy throughput of the host link with the step's own pinned buffers:
+    h_in -> d_in alone, the (device, host) pairs_out device -> host alone, and
+    both at once on two streams; 32 MB copies, as the pipeline's uploads are,
+    best of reps.  GB/s (1e9 bytes/s)."""
+    import torch
+    src = h_in.view(-1).view(torch.uint8)
+    dst = d_in.view(-1).view(torch.uint8)
+    outs = [(d.view(-1).view(torch.uint8), h.view(-1).view(torch.uint8)) for d, h in pairs_out]
+    n_in = src.numel()
+    n_out = sum(d.numel() for d, _ in outs)
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def up():
+        with torch.cuda.stream(s_in):
+            for o in range(0, n_in, chunk):
+                dst[o:o + chunk].copy_(src[o:o + chunk], non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(s_out):
+            for d, h in outs:
+                for o in range(0, d.numel(), chunk):
+                    h[o:o + chunk].copy_(d[o:o + chunk], non_blocking=True)
+
+    def best(*fns):
+        t_best = 1e9
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for f in fns:
+                f()
+            torch.cuda.synchronize()
+            t_best = min(t_best, time.perf_counter() - t)
+        return t_best
+
+    t_up, t_down, t_both = best(up), best(down), best(up, down)
+    return {"h2d_gbs": round(n_in / t_up / 1e9, 1), "d2h_gbs": round(n_out / t_down / 1e9, 1),
+            "both_gbs": round((n_in + n_out) / t_both / 1e9, 1), "both_ms": round(1e3 * t_both, 3)}
+
+
 def whole_job_rate(world: int, steps: int, seconds: float) -> float:
     """Units per second of the whole job: each of the `world` replicas
     processed `steps` units in at most `seconds`."""
@@ -677,6 +717,12 @@ def main():
     e2e_sync = whole_job_rate(world, args.e2e_steps, t_e[-1]) if args.e2e_steps > 0 else None
     h2d = int(h_holos.numel() * h_holos.element_size())
     d2h = int(2 * D ** 3 * 4 + D ** 3)
+    # the host link on this machine with these buffers: one step's upload and
+    # download at once bound the end-to-end rate
+    link = None
+    if args.e2e_steps > 0:
+        link = host_link_probe(h_holos, holos, [(re, h_outs[0][0]), (im, h_outs[0][1]), (otf, h_outs[0][2])])
+        link["bound_per_s"] = round(1e3 / link["both_ms"], 3)
 
     if rank == 0:
         # roofline of the dominant kernel
@@ -747,6 +793,9 @@ def main():
                     # (including time blocked on full launch queues while the GPU catches up)
                     "enqueue_ms_per_step": [round(1e3 * s / args.e2e_steps, 3) for s in e2e_enqueue_s],
                     "sync_value": round(e2e_sync, 3) if e2e_sync else None,
+                    # copy throughput of the host link measured after the trials with the same pinned
+                    # buffers (one step's upload and download), and the rate it bounds
+                    "link": link,
                     "sync_mode": "tdm_pipeline per step, each call returns with the volume in host memory"},
             "gpu_launches": int(launches),
             # host time spent inside the K pipeline calls, per step: the calls queue work and return,
