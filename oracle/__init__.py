@@ -59,6 +59,8 @@ def lib():
         L.orc_coord_spec.argtypes = [P, ctypes.c_int]
         L.orc_calc_uborn2.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
         L.orc_volkov.argtypes = [P, ctypes.c_int, P]
+        L.orc_herraez.argtypes = [P, ctypes.c_int, ctypes.c_int, P, P]
+        L.orc_crand.argtypes = [ctypes.c_longlong, ctypes.c_int, P]
         L.orc_aber_surface.argtypes = [P, ctypes.c_int, P, P]
         L.orc_fields.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OrcCfg), P, P, P, P, P, P, P, P]
         L.orc_reconstruction.argtypes = [P, P, ctypes.c_int, ctypes.POINTER(OrcCfg), P, P, P, P, P]
@@ -177,6 +179,23 @@ def volkov(phase: np.ndarray) -> np.ndarray:
     p = np.ascontiguousarray(phase, np.float64)
     out = np.empty_like(p)
     lib().orc_volkov(_p(p), p.shape[0], _p(out))
+    return out
+
+
+def herraez(phase: np.ndarray, angle: int = 0):
+    """Herraez unwrapping of a square wrapped phase as the angle of index
+    `angle` of the stack: (unwrapped phase, 2 pi count per pixel)."""
+    p = np.ascontiguousarray(phase, np.float64)
+    out = np.empty_like(p)
+    inc = np.empty(p.shape, np.int32)
+    lib().orc_herraez(_p(p), p.shape[0], angle, _p(out), _p(inc))
+    return out, inc
+
+
+def crand(skip: int, n: int) -> np.ndarray:
+    """n outputs of the C library's rand() after `skip` draws (oracle's restatement)."""
+    out = np.empty(n, np.int32)
+    lib().orc_crand(skip, n, _p(out))
     return out
 
 

@@ -28,7 +28,7 @@ LIBS = {
         "dir": "Tomo_prog/pretraitement_hors_axe_CPU",
         "includes": [".", "include"],
         "sources": ["fonctions.cpp", "FFT_fonctions.cpp", "src/deroulement_volkov4.cpp", "src/FFTW_init.cpp",
-                    "src/vecteur.cpp"],
+                    "src/vecteur.cpp", "deroulement_herraez.cpp"],
         "driver": "ref_pretraitement.cpp",
     },
     "libref_reconstruction.so": {

@@ -1,18 +1,21 @@
 // Driver of the reference's own preprocessing functions (test infrastructure
 // only): compiled with Tomo_prog/pretraitement_hors_axe_CPU/{fonctions.cpp,
 // FFT_fonctions.cpp, src/deroulement_volkov4.cpp, src/FFTW_init.cpp,
-// src/vecteur.cpp} into oracle/_ref/libref_pretraitement.so.  Each entry point
+// src/vecteur.cpp, deroulement_herraez.cpp} into
+// oracle/_ref/libref_pretraitement.so.  Each entry point
 // sets up its arguments as tomo_pretraitement's main does
 // (pretraitement_hors_axe_CPU/main.cpp, lines cited) and calls the
 // reference function; nothing here recomputes what the reference computes.
 #include <malloc.h>
 
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
 #include "FFTW_init.h"
 #include "FFT_fonctions.h"
+#include "deroulement_herraez.h"
 #include "deroulement_volkov4.h"
 #include "fonctions.h"
 
@@ -84,6 +87,18 @@ void ref_pre_volkov(const double* phase, int F, double* out) {
     std::vector<vecteur> kv = init_kvect_shift(Var2D{2 * F, 2 * F});
     deroul_volkov4_total_sym_paire(ph, un, kv, param_c2c_double);
     std::memcpy(out, un.data(), un.size() * sizeof(double));
+}
+
+// phaseUnwrapping_Mat (deroulement_herraez.cpp:32-74) as main.cpp:263 calls
+// it for the angle of index `angle` in tomo_pretraitement's loop: every
+// earlier angle drew F^2 rand() values in initialisePIXELs (:348), so the C
+// library's generator is reset (srand(1) is its initial state) and advanced
+// by angle F^2 draws first.
+void ref_pre_herraez(const double* phase, int F, int angle, double* out) {
+    srand(1);
+    for (long long i = 0; i < (long long)angle * F * F; ++i) rand();
+    const std::vector<double> ph(phase, phase + (size_t)F * F);
+    phaseUnwrapping_Mat(Var2D{F, F}, ph, out);
 }
 
 }  // extern "C"

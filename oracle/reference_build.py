@@ -44,6 +44,7 @@ def _libs():
         _pre.ref_pre_coord_spec.argtypes = [P, I]
         _pre.ref_pre_field.argtypes = [P, I, I, I, P, P]
         _pre.ref_pre_volkov.argtypes = [P, I, P]
+        _pre.ref_pre_herraez.argtypes = [P, I, I, P]
         _rec = ctypes.CDLL(os.path.join(_DIR, "libref_reconstruction.so"))
         _rec.ref_rec_manip.argtypes = [ctypes.c_char_p, P]
         _rec.ref_rec_volume.argtypes = [ctypes.c_char_p, P, P, I, P, P, P]
@@ -86,6 +87,13 @@ def volkov(phase: np.ndarray) -> np.ndarray:
     p = np.ascontiguousarray(phase, np.float64)
     out = np.empty_like(p)
     _libs()[0].ref_pre_volkov(_p(p), p.shape[0], _p(out))
+    return out
+
+
+def herraez(phase: np.ndarray, angle: int = 0) -> np.ndarray:
+    p = np.ascontiguousarray(phase, np.float64)
+    out = np.empty_like(p)
+    _libs()[0].ref_pre_herraez(_p(p), p.shape[0], angle, _p(out))
     return out
 
 

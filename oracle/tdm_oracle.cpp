@@ -485,6 +485,140 @@ std::vector<double> aber_surface(const Aber& A, const std::vector<double>& img) 
     return surf;
 }
 
+// ---------------------------------------------------------------------------
+// Herraez unwrapping (pretraitement_hors_axe_CPU/deroulement_herraez.cpp)
+// ---------------------------------------------------------------------------
+// The C library's rand() as the reference's build draws it: glibc's random()
+// with its default TYPE_3 state, i.e. the additive feedback generator
+//   r[0] = 1, r[i] = 16807 r[i-1] mod (2^31 - 1) (0 < i < 31),
+//   r[i] = r[i-31] (31 <= i < 34), r[i] = r[i-3] + r[i-31] mod 2^32 (i >= 34),
+// whose k-th output is r[k + 344] >> 1.
+struct CRand {
+    uint32_t ring[34];
+    int pos = 0;  // index of r[i-34] in the ring, i the next index
+    CRand() {
+        int64_t r[34];
+        r[0] = 1;
+        for (int i = 1; i < 31; ++i) r[i] = (16807 * r[i - 1]) % 2147483647;
+        for (int i = 31; i < 34; ++i) r[i] = r[i - 31];
+        for (int i = 0; i < 34; ++i) ring[i] = (uint32_t)r[i];
+        for (int i = 34; i < 344; ++i) step();
+    }
+    uint32_t step() {  // r[i] = r[i-3] + r[i-31]
+        const uint32_t v = ring[(pos + 31) % 34] + ring[(pos + 3) % 34];
+        ring[pos] = v;
+        pos = (pos + 1) % 34;
+        return v;
+    }
+    int next() { return (int)(step() >> 1); }
+};
+
+// Float constants and helpers of the file (:9-10, :357-380).
+constexpr float kHzPi = 3.141592654f, kHzTwoPi = 6.283185307f;
+float hz_wrap(float v) { return v > kHzPi ? v - kHzTwoPi : (v < -kHzPi ? v + kHzTwoPi : v); }
+int hz_find_wrap(float l, float r) {
+    const float d = l - r;
+    return d > kHzPi ? -1 : (d < -kHzPi ? 1 : 0);
+}
+
+// sort (:163-180) and Mix (:113-159): a merge sort on edge indices that
+// halves with size/2, so the last index of an odd-sized run is left where it
+// is; stable merges, ties taken from the first run.
+void hz_sort(const std::vector<float>& key, int* idx, int size, std::vector<int>& tmp) {
+    if (size == 2) {
+        if (key[idx[0]] > key[idx[1]]) std::swap(idx[0], idx[1]);
+    } else if (size > 2) {
+        const int h = size / 2;
+        hz_sort(key, idx, h, tmp);
+        hz_sort(key, idx + h, h, tmp);
+        int a = 0, b = 0, o = 0;
+        while (a < h && b < h) tmp[o++] = key[idx[a]] <= key[idx[h + b]] ? idx[a++] : idx[h + b++];
+        while (a < h) tmp[o++] = idx[a++];
+        while (b < h) tmp[o++] = idx[h + b++];
+        std::copy(tmp.begin(), tmp.begin() + 2 * h, idx);
+    }
+}
+
+// phaseUnwrapping_Mat (:32-74) on a W x W wrapped phase, as the angle of
+// index `angle` in tomo_pretraitement's loop: every earlier angle drew W^2
+// rand() values (initialisePIXELs, :348).  Writes the unwrapped phase and
+// each pixel's number of 2 pi.
+void herraez(const double* phase, int W, int angle, double* out, int32_t* inc_out) {
+    const int n = W * W;
+    CRand g;
+    for (long long i = 0; i < (long long)angle * n; ++i) g.step();
+    std::vector<float> value(n), rel(n);
+    for (int p = 0; p < n; ++p) {  // initialisePIXELs (:333-355): 9999999 + rand() in int, wrapping past INT_MAX
+        value[p] = (float)phase[p];
+        rel[p] = (float)(int32_t)(9999999u + (uint32_t)g.next());
+    }
+    for (int i = 1; i < W - 1; ++i)  // calculate_reliability (:385-413), in float
+        for (int j = 1; j < W - 1; ++j) {
+            const int p = i * W + j;
+            auto d2 = [&](int o) { return hz_wrap((float)(phase[p - o] - phase[p])) - hz_wrap((float)(phase[p] - phase[p + o])); };
+            const float H = d2(1), V = d2(W), D1 = d2(W + 1), D2 = d2(W - 1);
+            rel[p] = H * H + V * V + D1 * D1 + D2 * D2;
+        }
+    // horizentalEDGEs (:415-437) then verticalEDGEs (:439-459)
+    const int ne = W * (W - 1) * 2;
+    std::vector<int> p1(ne), p2(ne), einc(ne);
+    std::vector<float> key(ne);
+    int e = 0;
+    for (int i = 0; i < W; ++i)
+        for (int j = 0; j < W - 1; ++j, ++e) p1[e] = i * W + j, p2[e] = i * W + j + 1;
+    for (int i = 0; i < W - 1; ++i)
+        for (int j = 0; j < W; ++j, ++e) p1[e] = i * W + j, p2[e] = (i + 1) * W + j;
+    for (e = 0; e < ne; ++e) {
+        key[e] = rel[p1[e]] + rel[p2[e]];
+        einc[e] = hz_find_wrap(value[p1[e]], value[p2[e]]);
+    }
+    std::vector<int> idx(ne), tmp(ne);  // quick_sort (:193-213)
+    for (e = 0; e < ne; ++e) idx[e] = e;
+    hz_sort(key, idx.data(), ne, tmp);
+    // gatherPIXELs (:461-561): groups as linked lists from their head
+    std::vector<int> head(n), last(n), next(n, -1), count(n, 1), inc(n, 0);
+    for (int p = 0; p < n; ++p) head[p] = last[p] = p;
+    for (int k = 0; k < ne; ++k) {
+        const int q = idx[k], P1 = p1[q], P2 = p2[q], ei = einc[q];
+        if (head[P2] == head[P1]) continue;
+        if (next[P2] < 0 && head[P2] == P2) {  // PIXEL 2 alone: it joins PIXEL 1's group
+            const int h1 = head[P1];
+            next[last[h1]] = P2;
+            last[h1] = P2;
+            ++count[h1];
+            head[P2] = h1;
+            inc[P2] = inc[P1] - ei;
+        } else if (next[P1] < 0 && head[P1] == P1) {  // PIXEL 1 alone: it joins PIXEL 2's group
+            const int h2 = head[P2];
+            next[last[h2]] = P1;
+            last[h2] = P1;
+            ++count[h2];
+            head[P1] = h2;
+            inc[P1] = inc[P2] + ei;
+        } else {
+            int g1 = head[P1], g2 = head[P2];
+            if (count[g1] > count[g2]) {  // group 2 into group 1
+                next[last[g1]] = g2;
+                last[g1] = last[g2];
+                count[g1] += count[g2];
+                const int d = inc[P1] - ei - inc[P2];
+                for (int r = g2; r >= 0; r = next[r]) head[r] = g1, inc[r] += d;
+            } else {  // group 1 into group 2
+                next[last[g2]] = g1;
+                last[g2] = last[g1];
+                count[g2] += count[g1];
+                const int d = inc[P2] + ei - inc[P1];
+                for (int r = g1; r >= 0; r = next[r]) head[r] = g2, inc[r] += d;
+            }
+        }
+    }
+    for (int p = 0; p < n; ++p) {  // unwrapImage (:564-575), returnImage (:580-594)
+        const float v = value[p] + kHzTwoPi * (float)inc[p];
+        out[p] = v;
+        if (inc_out) inc_out[p] = inc[p];
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -513,6 +647,21 @@ void orc_derive(const orc_cfg* c, orc_derived* d) {
     d->delta_f = 1 / (d->tp_uborn * 2 * (double)c->nxmax);
     d->tp_tomo = d->tp_uborn * (double)(2 * (size_t)c->nxmax) / (double)c->dim_final;
     d->rayon = std::round((double)(size_t)c->nxmax * c->n0 / c->na);
+}
+
+// phaseUnwrapping_Mat (pretraitement_hors_axe_CPU/deroulement_herraez.cpp:32-74)
+// for the angle of index `angle` of the stack (rand() draws of the earlier
+// angles skipped); inc_out (may be null) receives each pixel's 2 pi count.
+void orc_herraez(const double* phase, int F, int angle, double* out, int32_t* inc_out) {
+    herraez(phase, F, angle, out, inc_out);
+}
+
+// The first n outputs of the C library's rand() generator (glibc, default
+// seed) after `skip` draws, as the oracle restates it.
+void orc_crand(long long skip, int n, int32_t* out) {
+    CRand g;
+    for (long long i = 0; i < skip; ++i) g.step();
+    for (int i = 0; i < n; ++i) out[i] = g.next();
 }
 
 void orc_tukey2d(int n, float alpha, double* out) {

@@ -65,6 +65,23 @@ def test_hologram_window_flat_where_the_row_pass_skips_it(n):
     assert t[0] != 1.0 and t[-1] != 1.0
 
 
+def test_crand_is_the_c_library_generator():
+    """The oracle's restatement of the C library's rand() (glibc's default
+    generator), which Herraez unwrapping draws its border reliabilities from,
+    against the C library itself, from the start and after 102,000 draws."""
+    import ctypes
+    try:
+        libc = ctypes.CDLL("libc.so.6")
+    except OSError:
+        pytest.skip("no glibc")
+    libc.srand(1)
+    first = np.array([libc.rand() for _ in range(2000)], np.int32)
+    np.testing.assert_array_equal(oracle.crand(0, 2000), first)
+    for _ in range(100000):
+        libc.rand()
+    np.testing.assert_array_equal(oracle.crand(102000, 100), np.array([libc.rand() for _ in range(100)], np.int32))
+
+
 def test_coord_spec_quirk():
     F = 16
     s = np.zeros((F, F), np.complex128)

@@ -100,6 +100,28 @@ def test_volkov_unwrap_up_to_the_zero_frequency_piston(case, request):
         assert np.abs(diff - diff.mean()).max() <= 1e-10, a
 
 
+def _herraez_phase(F, sigma, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:F, 0:F] / F
+    true = 25 * np.exp(-((x - .5) ** 2 + (y - .45) ** 2) / 0.04) - 6 * y
+    return np.angle(np.exp(1j * (true + rng.normal(0, sigma, (F, F)))))
+
+
+@pytest.mark.parametrize("F", [64, 250, 256])
+@pytest.mark.parametrize("sigma", [0.0, 1.2])
+@pytest.mark.parametrize("angle", [0, 3])
+def test_herraez_unwrap_bit_exact(F, sigma, angle):
+    """phaseUnwrapping_Mat (deroulement_herraez.cpp:32-74): the restatement
+    gives the reference's unwrapped phase bit for bit, on smooth phases and on
+    noisy ones whose residues make the result depend on the edge order, for
+    the first angle of a stack and a later one (the border pixels'
+    reliabilities come from rand(), whose earlier draws are skipped)."""
+    wrapped = _herraez_phase(F, sigma, seed=F + int(10 * sigma))
+    got, inc = oracle.herraez(wrapped, angle)
+    np.testing.assert_array_equal(got, rb.herraez(wrapped, angle))
+    assert inc.min() < 0 or inc.max() > 0
+
+
 def test_reconstruction_parameters():
     from tests import simul
     for name in ("plain_512_born", "rytov_1024", "large_2048"):
