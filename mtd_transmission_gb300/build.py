@@ -21,7 +21,8 @@ LIB = os.path.join(HERE, "libtdm.so")
 BIN = os.path.join(HERE, "bin")
 APPS = ("tomo_pretraitement", "tomo_reconstruction", "tomo_pipeline")
 
-CU_SOURCES = ("tdm_api.cu", "k_extract.cu", "k_fields.cu", "k_recon.cu", "k_generic.cu", "tdm_noalloc.cu")
+CU_SOURCES = ("tdm_api.cu", "k_extract.cu", "k_fields.cu", "k_recon.cu", "k_generic.cu", "k_herraez.cu",
+              "tdm_noalloc.cu")
 CPP_SOURCES = ("host_io.cpp",)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstdint>
 #include <vector>
 
 #include "fft_core.cuh"
@@ -62,6 +63,52 @@ inline std::vector<float2> hologram_window(int H) {
         w[x] = make_float2(ws, -8388608.0f * ws);
     }
     return w;
+}
+
+// The C library's rand() as the reference's build draws it: glibc's random()
+// with its default state, the additive feedback generator r[0] = 1,
+// r[i] = 16807 r[i-1] mod (2^31 - 1) (0 < i < 31), r[i] = r[i-31]
+// (31 <= i < 34), r[i] = r[i-3] + r[i-31] mod 2^32 (i >= 34), whose k-th
+// output is r[k + 344] >> 1.
+class CRand {
+    uint32_t ring_[34];
+    int pos_ = 0;  // ring slot of r[i-34], i the next index
+
+public:
+    CRand() {
+        int64_t r[34];
+        r[0] = 1;
+        for (int i = 1; i < 31; ++i) r[i] = (16807 * r[i - 1]) % 2147483647;
+        for (int i = 31; i < 34; ++i) r[i] = r[i - 31];
+        for (int i = 0; i < 34; ++i) ring_[i] = (uint32_t)r[i];
+        for (int i = 34; i < 344; ++i) step();
+    }
+    uint32_t step() {
+        const uint32_t v = ring_[(pos_ + 31) % 34] + ring_[(pos_ + 3) % 34];
+        ring_[pos_] = v;
+        pos_ = pos_ + 1 == 34 ? 0 : pos_ + 1;
+        return v;
+    }
+    int next() { return (int)(step() >> 1); }
+};
+
+// Herraez unwrapping's border reliabilities (VOLKOV 0).  initialisePIXELs
+// (pretraitement_hors_axe_CPU/deroulement_herraez.cpp:348) draws one rand()
+// per pixel, row by row, F^2 per angle in the order tomo_pretraitement
+// unwraps them; calculate_reliability then overwrites the interior's.  Per
+// angle, the draws of the border pixels: row 0, then columns 0 and F - 1 of
+// rows 1 .. F - 2, then row F - 1 (4F - 4 values).
+inline std::vector<int> crand_border_table(int F, int angles) {
+    std::vector<int> t((size_t)angles * (4 * F - 4));
+    CRand g;
+    size_t o = 0;
+    for (int a = 0; a < angles; ++a)
+        for (int i = 0; i < F; ++i)
+            for (int j = 0; j < F; ++j) {
+                const int v = g.next();
+                if (i == 0 || i == F - 1 || j == 0 || j == F - 1) t[o++] = v;
+            }
+    return t;
 }
 
 // Indices [x, y] where tukey_factor(n, alpha) is exactly 1 (its flat middle,

@@ -657,7 +657,10 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         }
         if (!p.c_aber) continue;
         const float* unw = b.phase;
-        if (p.deroul) {
+        if (p.deroul && !p.volkov) {
+            if (int rc = launch_herraez(c, g0, m)) return rc;
+            unw = b.unwrapped;
+        } else if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
                 k_volkov_rows<L><<<dim3(F / (2 * RC::P), m), RC::NT, sm_vrows, c->stream>>>(b.phase, b.zph, b.tw,

@@ -454,7 +454,10 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
         }
         if (!p.c_aber) continue;
         const float* unw = b.phase;
-        if (p.deroul) {
+        if (p.deroul && !p.volkov) {
+            if (int rc = launch_herraez(c, g0, m)) return rc;
+            unw = b.unwrapped;
+        } else if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
                 gk_volkov_rows<F><<<dim3((F / 2 + kPairs - 1) / kPairs, m), 3 * kPairs * 32, sm_vrows, c->stream>>>(

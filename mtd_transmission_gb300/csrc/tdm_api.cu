@@ -16,7 +16,7 @@ namespace tdm {
 const char* const kKernelNames[K_COUNT] = {
     "extract_rows", "extract_cols", "argmax", "field_rows", "field_cols", "volkov_rows", "volkov_cols",
     "volkov_integ_rows", "volkov_integ_cols", "aber_fit", "form", "cap_rows", "cap_cols", "gather",
-    "ypass", "xpass", "posspec", "zpass"};
+    "ypass", "xpass", "posspec", "zpass", "herraez"};
 
 cudaEvent_t prof_event(tdm_ctx* c) {
     if (!c->ev_pool.empty()) {
@@ -83,7 +83,7 @@ void free_all(tdm_ctx* c) {
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0].val, b.rec_buf[0].z, b.rec_buf[1].val,
                     b.rec_buf[1].z, b.posspec_vol[0], b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
-                    b.xv[4], b.xv[5], b.caps, b.rec2.val, b.rec2.z, b.misfit, b.ref_inv};
+                    b.xv[4], b.xv[5], b.caps, b.rec2.val, b.rec2.z, b.misfit, b.ref_inv, b.hz_rand};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = Buffers{};
@@ -184,8 +184,8 @@ int check_geom(const tdm_geom* g, std::string& why) {
         why = "crop window (CIRCLE_CX/CY +- NXMAX) outside the hologram spectrum";
         return TDM_EINVAL;
     }
-    if (g->c_aber && g->deroul && !g->volkov) {
-        why = "VOLKOV 0 (Herraez unwrapping) is not supported";
+    if (g->c_aber && g->deroul && !g->volkov && F > 256) {
+        why = "VOLKOV 0 (Herraez unwrapping) needs 2*NXMAX <= 256 (its pixel groups live in one CTA's shared memory)";
         return TDM_EUNSUPPORTED;
     }
     if (!(g->na > 0) || !(g->n0 > 0) || !(g->lambda0 > 0) || !(g->f_obj > 0) || !(g->rf > 0) || !(g->f_tube > 0) ||
@@ -242,6 +242,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     p.born = geom->born ? 1 : 0;
     p.c_aber = geom->c_aber ? 1 : 0;
     p.deroul = geom->deroul ? 1 : 0;
+    p.volkov = geom->volkov ? 1 : 0;
     p.rayon = c->dv.rayon;
     p.inv_rayon = 1.0 / c->dv.rayon;
     const int N = p.N, F = p.F, D = p.D;
@@ -403,6 +404,12 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaMemset(b.err, 0, 4 * sizeof(int)) != cudaSuccess ||
         cudaMemset(b.fit_done, 0, CH * 2 * sizeof(unsigned)) != cudaSuccess)
         TRY(cuda_fail(c, cudaGetLastError(), "table upload"));
+    if (p.c_aber && p.deroul && !p.volkov) {  // Herraez unwrapping's border reliabilities
+        const std::vector<int> br = crand_border_table(F, max_angles);
+        TRY(dev_alloc(c, &b.hz_rand, br.size()));
+        if (cudaMemcpy(b.hz_rand, br.data(), br.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+            TRY(cuda_fail(c, cudaGetLastError(), "table upload"));
+    }
     if (p.c_aber) TRY(build_aberration(c, nullptr));
 #undef TRY
     *out = c;
@@ -522,6 +529,7 @@ int tdm_synchronize(tdm_ctx* c) {
     if (err) {
         cudaMemset(c->b.err, 0, sizeof(int));
         if (err & 2) return fail(c, TDM_ECUDA, "a bulk copy of hologram rows did not complete");
+        if (err & 8) return fail(c, TDM_EDATA, "Herraez unwrapping: a 2 pi offset between merged groups beyond +-127");
         return fail(c, TDM_EDATA, "an Ewald-cap voxel fell outside the DIM_FINAL volume");
     }
     return TDM_OK;

@@ -32,6 +32,7 @@ struct Params {
     int H, N, F, L, D;
     int x0, y0;              // crop corner in the fftshifted hologram spectrum
     int born, c_aber, deroul;
+    int volkov;              // VOLKOV: 1 Volkov unwrapping, 0 Herraez
     int disc_thr;            // fd^2 < disc_thr  <=>  fd^2 < COEF_NA_OBJ_LIMIT * N^2
     int zmin, band;          // cap planes z in [zmin, zmin + band)
     int r2i;                 // rayon^2 when below 2^24 (cap heights as float sqrt of exact integers), else 0
@@ -64,6 +65,7 @@ struct Buffers {
     float2* qc = nullptr;          // chunk x L*F (FFT along y of Q, columns X >= F)
     float2* tq = nullptr;          // chunk x L*F
     float* unwrapped = nullptr;    // chunk x F*F
+    int* hz_rand = nullptr;        // VOLKOV 0: max_angles x (4F - 4) border rand() draws (crand_border_table)
     double* beta = nullptr;        // chunk x 2 x kNC
     float* fit_part = nullptr;     // chunk x 2 x 8 x kNC slice sums of the fits
     unsigned* fit_done = nullptr;  // chunk x 2 finished-slice counters (zero between launches)
@@ -92,7 +94,7 @@ struct Buffers {
 enum KernelId {
     K_EXTRACT_ROWS, K_EXTRACT_COLS, K_ARGMAX, K_FIELD_ROWS, K_FIELD_COLS, K_VOLKOV_ROWS, K_VOLKOV_COLS,
     K_VOLKOV_INTEG_ROWS, K_VOLKOV_INTEG_COLS, K_ABER_FIT, K_FORM, K_CAP_ROWS, K_CAP_COLS, K_GATHER,
-    K_YPASS, K_XPASS, K_POSSPEC, K_ZPASS, K_COUNT
+    K_YPASS, K_XPASS, K_POSSPEC, K_ZPASS, K_HERRAEZ, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 
@@ -187,6 +189,10 @@ int launch_extract(tdm_ctx* c, const void* holos_dev, int bits, int n, int a0, b
 // Per-angle field formation for spectra [a0, a0 + n).  argparts > 0: the
 // extraction left that many partial winners per angle (one chunk only);
 // form = false (C_ABER pipeline): the fields are formed by the cap row pass.
+// Herraez unwrapping (VOLKOV 0) of the chunk's m wrapped phases (b.phase ->
+// b.unwrapped), stack angles a0 .. a0 + m - 1; F <= 256.
+int launch_herraez(tdm_ctx* c, int a0, int m);
+size_t herraez_gather_smem(int F);
 int launch_fields(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp,
                   int argparts = 0, bool form = true);
 // Per-field spectra and cap contributions for fields [a0, a0 + n); with

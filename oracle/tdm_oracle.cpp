@@ -753,7 +753,9 @@ int orc_aber_surface(const uint8_t* mask, int F, const double* img, double* surf
 // (UBornFinal, M*F*F complex) and tabPosSpec (x values then y values).
 // Optional per-angle intermediates (may be NULL): wrapped phase, unwrapped
 // phase, amplitude, corrected phase, corrected amplitude (M*F*F doubles each).
-// Returns 0, -1 (aberration fit undefined), -3 (Herraez unwrap requested).
+// Returns 0 or -1 (aberration fit undefined).  VOLKOV 0 unwraps with Herraez's
+// method, the stack's angle a drawing its border reliabilities as the
+// reference's loop would for its a-th angle (main.cpp:262-266).
 int orc_fields(const double* spectra, int M, int nxmax, const orc_cfg* cfg, const uint8_t* mask,
                double* fields_out, double* posspec_out, double* dbg_phase, double* dbg_unwrap,
                double* dbg_amp, double* dbg_phase_corr, double* dbg_amp_corr) {
@@ -761,7 +763,6 @@ int orc_fields(const double* spectra, int M, int nxmax, const orc_cfg* cfg, cons
     const size_t P = (size_t)F * F;
     Aber A;
     if (cfg->c_aber && !aber_init(A, mask, F)) return -1;
-    if (cfg->c_aber && cfg->deroul && !cfg->volkov) return -3;
     for (int a = 0; a < M; ++a) {
         const cd* tf = reinterpret_cast<const cd*>(spectra) + (size_t)a * P;
         int cpt_max = orc_coord_spec(reinterpret_cast<const double*>(tf), F);
@@ -776,8 +777,14 @@ int orc_fields(const double* spectra, int M, int nxmax, const orc_cfg* cfg, cons
             orc_calc_uborn2(reinterpret_cast<const double*>(tf), F, kxmi, kymi, reinterpret_cast<double*>(ub.data()));
             std::vector<double> ph(P), unw;
             for (size_t c = 0; c < P; ++c) ph[c] = std::atan2(ub[c].imag(), ub[c].real());
-            if (cfg->deroul) unw = volkov_unwrap(ph, F);
-            else unw = ph;
+            if (cfg->deroul && cfg->volkov) {
+                unw = volkov_unwrap(ph, F);
+            } else if (cfg->deroul) {
+                unw.resize(P);
+                herraez(ph.data(), F, a, unw.data(), nullptr);
+            } else {
+                unw = ph;
+            }
             std::vector<double> sph = aber_surface(A, unw);
             std::vector<double> amp(P);
             for (size_t c = 0; c < P; ++c) amp[c] = std::abs(ub[c]);
