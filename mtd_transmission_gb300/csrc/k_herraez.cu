@@ -62,6 +62,13 @@ __device__ __forceinline__ void hz_edge(int e, int F, int& p1, int& p2) {
     }
 }
 
+// An edge's payload through the sort: its first pixel, whether it is
+// vertical, and its 2 pi jump + 1: (p1 << 3) | (vertical << 2) | (jump + 1).
+__device__ __forceinline__ void hz_payload_pixels(uint32_t pl, int F, int& p1, int& p2) {
+    p1 = (int)(pl >> 3);
+    p2 = p1 + ((pl & 4u) ? F : 1);
+}
+
 __global__ void __launch_bounds__(kHzThreads)
 k_hz_reliability(const float* __restrict__ phase, const int* __restrict__ border_rand, int a0, int F,
                  float* __restrict__ rel) {
@@ -94,7 +101,7 @@ struct SortBuf {
     uint32_t* pay;
 };
 
-// Per edge: key = its reliability, payload = (edge index << 2) | (2 pi jump + 1).
+// Per edge: key = its reliability, and its payload (hz_payload_pixels).
 // The chunk's angle i keeps its arrays at offset i * stride.
 __global__ void __launch_bounds__(kHzThreads)
 k_hz_edges(const float* __restrict__ phase, const float* __restrict__ rel, int F, size_t stride, SortBuf out) {
@@ -109,7 +116,7 @@ k_hz_edges(const float* __restrict__ phase, const float* __restrict__ rel, int F
     const int jump = d > kHzPi ? -1 : (d < -kHzPi ? 1 : 0);
     const size_t o = a * stride + e;
     out.eff[o] = __fadd_rn(rl[p1], rl[p2]);  // a run of one
-    out.pay[o] = ((uint32_t)e << 2) | (uint32_t)(jump + 1);
+    out.pay[o] = ((uint32_t)p1 << 3) | (p2 - p1 == 1 ? 0u : 4u) | (uint32_t)(jump + 1);
 }
 
 struct SortLevel {
@@ -163,7 +170,7 @@ k_hz_sort_level(SortBuf in, SortBuf out, size_t stride, const float* __restrict_
         }
     } else if (inside && h >= 1 && (n & 1)) {  // the odd node's leftover joins the node's run at its end
         int p1, p2;
-        hz_edge((int)(pl >> 2), F, p1, p2);
+        hz_payload_pixels(pl, F, p1, p2);
         const float* rl = rel + (size_t)blockIdx.y * F * F;
         x = fmaxf(fmaxf(k[s + h - 1], k[s + 2 * h - 1]), __fadd_rn(rl[p1], rl[p2]));
     }
@@ -208,9 +215,9 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
                 const int cnt = min(32, ne - k0);
                 for (int t = 0; t < cnt; ++t) {
                     const uint32_t pl = batch[t];
-                    const int e = (int)(pl >> 2), jump = (int)(pl & 3u) - 1;
+                    const int jump = (int)(pl & 3u) - 1;
                     int p1, p2;
-                    hz_edge(e, F, p1, p2);
+                    hz_payload_pixels(pl, F, p1, p2);
                     // root of each pixel and the pixel's 2 pi count relative to it (path halving)
                     auto find = [&](int p, int& acc) {
                         acc = 0;

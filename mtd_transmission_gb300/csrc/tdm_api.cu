@@ -405,6 +405,8 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
         cudaMemset(b.fit_done, 0, CH * 2 * sizeof(unsigned)) != cudaSuccess)
         TRY(cuda_fail(c, cudaGetLastError(), "table upload"));
     if (p.c_aber && p.deroul && !p.volkov) {  // Herraez unwrapping's border reliabilities
+        // its merging runs one CTA per angle: twice as many angles in flight
+        if (32 * c->lanes <= c->chunk_cap) c->chunk = c->holo_chunk = 32;
         const std::vector<int> br = crand_border_table(F, max_angles);
         TRY(dev_alloc(c, &b.hz_rand, br.size()));
         if (cudaMemcpy(b.hz_rand, br.data(), br.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
