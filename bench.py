@@ -556,11 +556,12 @@ def cufft_reference(acq, kern):
 def workload_config(acq, args):
     return {"workload": f"{args.workload}: {acq.nb_holo} x {acq.ccd_roix}^2 uint16 12-bit holograms, "
                         f"NXMAX {acq.nxmax} ({2 * acq.nxmax}^2 fields), {'Born' if acq.born else 'Rytov'}, "
-                        f"Volkov + aberration correction, {acq.dim_final}^3 volume",
+                        f"{'Volkov' if acq.volkov else 'Herraez'} + aberration correction, {acq.dim_final}^3 volume",
             "holograms": acq.nb_holo, "hologram_px": acq.ccd_roix, "field_px": 2 * acq.nxmax,
             "volume": acq.dim_final, "parallelism": f"replicas x{args.gpus}",
             "schedule": {"chunk": schedule_for(acq.nb_holo)[0], "lanes": schedule_for(acq.nb_holo)[1]},
-            "l2": "inputs larger than L2: 1.26 GB of holograms per step (no flush needed)"}
+            "l2": f"inputs larger than L2: {acq.nb_holo * acq.ccd_roix ** 2 * 2 / 1e9:.2f} GB of holograms per step "
+                  "(no flush needed)"}
 
 
 def main():
@@ -577,6 +578,7 @@ def main():
     ap.add_argument("--profile-out", default=None)
     ap.add_argument("--no-profile-pass", action="store_true", help="skip the per-kernel event pass")
     ap.add_argument("--holograms", type=int, default=None, help="override the workload's hologram count")
+    ap.add_argument("--herraez", action="store_true", help="unwrap with Herraez's method (VOLKOV 0) instead of Volkov's")
     ap.add_argument("--no-forms", action="store_true", help="skip the regularised-reconstruction form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -587,6 +589,8 @@ def main():
     acq, ph, seed = simul.workload(args.workload)
     if args.holograms:
         acq = replace(acq, nb_holo=args.holograms)
+    if args.herraez:
+        acq = replace(acq, volkov=0)
     world, rank, local = dist_setup()
 
     if args.impl == "reference":
