@@ -30,7 +30,9 @@
 //                    The reference keeps each group as a linked list and adds
 //                    the merged group's 2 pi offset to every member; here the
 //                    groups are a union-find forest in shared memory whose
-//                    links carry the 2 pi offset to the parent, and which
+//                    links carry the 2 pi offset to the parent (int8; -128
+//                    marks a root, whose parent slot holds the group's size),
+//                    and which
 //                    takes the same decisions (a lone pixel 2 joins pixel 1's
 //                    group, else a lone pixel 1 joins pixel 2's, else the
 //                    larger group absorbs the other, ties to group 2), so each
@@ -180,10 +182,11 @@ k_hz_sort_level(SortBuf in, SortBuf out, size_t stride, const float* __restrict_
 
 // Shared memory of k_hz_gather for F x F pixels: per pixel the parent (or,
 // at a root, the group's size - 1) as uint16 and the 2 pi offset to the
-// parent as int8, and one root bit per pixel.
+// parent as int8, kHzRoot marking a root.
+constexpr int kHzRoot = -128;
 size_t hz_gather_smem(int F) {
     const size_t n = (size_t)F * F;
-    return n * 2 + ((n + 3) & ~size_t(3)) + ((n + 31) / 32) * 4;
+    return n * 3;
 }
 
 __global__ void __launch_bounds__(kHzThreads)
@@ -193,20 +196,42 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
     const int a = blockIdx.x, n = F * F, ne = 2 * F * (F - 1);
     uint16_t* up = reinterpret_cast<uint16_t*>(smraw);
     int8_t* pot = reinterpret_cast<int8_t*>(up + n);
-    uint32_t* rootbit = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(pot) + ((n + 3) & ~3));
     __shared__ uint32_t batch[32];
     for (int p = threadIdx.x; p < n; p += kHzThreads) {
-        up[p] = 0;  // every pixel its own group of size 1
-        pot[p] = 0;
+        up[p] = 0;  // every pixel the root of its own group of size 1
+        pot[p] = (int8_t)kHzRoot;
     }
-    for (int w = threadIdx.x; w < (n + 31) / 32; w += kHzThreads) rootbit[w] = 0xffffffffu;
     __syncthreads();
-    auto is_root = [&](int p) { return (rootbit[p >> 5] >> (p & 31)) & 1u; };
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         const uint32_t* ps = pays + a * stride;
         uint32_t nxt = lane < ne ? ps[lane] : 0u;
         int bad = 0;
+        // root of pixel p and p's 2 pi count relative to it, halving the path
+        // (each visited pixel is relinked to its grandparent)
+        auto find = [&](int p, int& acc) {
+            acc = 0;
+            int pp = pot[p];
+            if (pp == kHzRoot) return p;
+            int q = up[p];
+            while (true) {
+                const int pq = pot[q];
+                if (pq == kHzRoot) {
+                    acc += pp;
+                    return q;
+                }
+                const int g = up[q];
+                const int v = pp + pq;  // p's offset to g
+                bad |= v < -127 || v > 127;
+                pot[p] = (int8_t)v;
+                up[p] = (uint16_t)g;
+                acc += v;
+                p = g;
+                pp = pot[g];
+                if (pp == kHzRoot) return g;
+                q = up[g];
+            }
+        };
         for (int k0 = 0; k0 < ne; k0 += 32) {
             batch[lane] = nxt;
             nxt = k0 + 32 + lane < ne ? ps[k0 + 32 + lane] : 0u;  // the next batch, in flight meanwhile
@@ -218,30 +243,13 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
                     const int jump = (int)(pl & 3u) - 1;
                     int p1, p2;
                     hz_payload_pixels(pl, F, p1, p2);
-                    // root of each pixel and the pixel's 2 pi count relative to it (path halving)
-                    auto find = [&](int p, int& acc) {
-                        acc = 0;
-                        while (!is_root(p)) {
-                            const int q = up[p];
-                            if (!is_root(q)) {
-                                const int v = pot[p] + pot[q];
-                                bad |= v < -128 || v > 127;
-                                pot[p] = (int8_t)v;
-                                up[p] = up[q];
-                            }
-                            acc += pot[p];
-                            p = up[p];
-                        }
-                        return p;
-                    };
                     int a1, a2;
                     const int r1 = find(p1, a1), r2 = find(p2, a2);
                     if (r1 == r2) continue;
                     const int s1 = up[r1] + 1, s2 = up[r2] + 1;
                     // child root c joins parent root r with 2 pi offset v; the group has `size` pixels
                     auto link = [&](int c, int r, int v, int size) {
-                        bad |= v < -128 || v > 127;
-                        rootbit[c >> 5] &= ~(1u << (c & 31));
+                        bad |= v < -127 || v > 127;
                         up[c] = (uint16_t)r;
                         pot[c] = (int8_t)v;
                         up[r] = (uint16_t)(size - 1);
@@ -261,7 +269,7 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
     float* out = unwrapped + (size_t)a * n;
     for (int p = threadIdx.x; p < n; p += kHzThreads) {
         int acc = 0;
-        for (int q = p; !is_root(q); q = up[q]) acc += pot[q];
+        for (int q = p; pot[q] != kHzRoot; q = up[q]) acc += pot[q];
         out[p] = __fadd_rn(ph[p], __fmul_rn(kHzTwoPi, __int2float_rn(acc)));
     }
 }
