@@ -57,7 +57,7 @@ typedef struct {
     int born;           /* BORN: 1 Born, 0 Rytov */
     int c_aber;         /* C_ABER: aberration correction (and unwrapping) on/off */
     int deroul;         /* DEROUL: phase unwrapping on/off (only with C_ABER) */
-    int volkov;         /* VOLKOV: 1 Volkov; 0 Herraez (2*NXMAX <= 256) */
+    int volkov;         /* VOLKOV: 1 Volkov; 0 Herraez */
     double na;          /* NA */
     double n0;          /* N0 */
     double lambda0;     /* LAMBDA (m) */

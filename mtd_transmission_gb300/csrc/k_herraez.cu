@@ -180,21 +180,28 @@ k_hz_sort_level(SortBuf in, SortBuf out, size_t stride, const float* __restrict_
     out.pay[base + dst] = pl;
 }
 
-// Shared memory of k_hz_gather for F x F pixels: per pixel the parent (or,
-// at a root, the group's size - 1) as uint16 and the 2 pi offset to the
-// parent as int8, kHzRoot marking a root.
+// The forest of k_hz_gather for F x F pixels: per pixel the parent (or, at a
+// root, the group's size - 1) and the 2 pi offset to the parent as int8,
+// kHzRoot marking a root.  In shared memory (uint16 parents) up to 256^2
+// pixels: 3 bytes a pixel.
 constexpr int kHzRoot = -128;
 size_t hz_gather_smem(int F) {
     const size_t n = (size_t)F * F;
     return n * 3;
 }
 
+// One CTA per angle.  Idx is the parent's type: uint16_t with the forest in
+// shared memory (up to 256^2 pixels), uint32_t with it in global memory
+// (forest, up to n parents then n offsets, one per angle at a stride).
+template <class Idx, bool SHARED>
 __global__ void __launch_bounds__(kHzThreads)
 k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __restrict__ phase, int F,
-            float* __restrict__ unwrapped, int* __restrict__ err) {
+            float* __restrict__ unwrapped, int* __restrict__ err, unsigned char* __restrict__ forest,
+            size_t forest_stride) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int a = blockIdx.x, n = F * F, ne = 2 * F * (F - 1);
-    uint16_t* up = reinterpret_cast<uint16_t*>(smraw);
+    unsigned char* base = SHARED ? smraw : forest + a * forest_stride;
+    Idx* up = reinterpret_cast<Idx*>(base);
     int8_t* pot = reinterpret_cast<int8_t*>(up + n);
     __shared__ uint32_t batch[32];
     for (int p = threadIdx.x; p < n; p += kHzThreads) {
@@ -213,23 +220,23 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
             acc = 0;
             int pp = pot[p];
             if (pp == kHzRoot) return p;
-            int q = up[p];
+            int q = (int)up[p];
             while (true) {
                 const int pq = pot[q];
                 if (pq == kHzRoot) {
                     acc += pp;
                     return q;
                 }
-                const int g = up[q];
+                const int g = (int)up[q];
                 const int v = pp + pq;  // p's offset to g
                 bad |= v < -127 || v > 127;
                 pot[p] = (int8_t)v;
-                up[p] = (uint16_t)g;
+                up[p] = (Idx)g;
                 acc += v;
                 p = g;
                 pp = pot[g];
                 if (pp == kHzRoot) return g;
-                q = up[g];
+                q = (int)up[g];
             }
         };
         for (int k0 = 0; k0 < ne; k0 += 32) {
@@ -246,13 +253,13 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
                     int a1, a2;
                     const int r1 = find(p1, a1), r2 = find(p2, a2);
                     if (r1 == r2) continue;
-                    const int s1 = up[r1] + 1, s2 = up[r2] + 1;
+                    const int s1 = (int)up[r1] + 1, s2 = (int)up[r2] + 1;
                     // child root c joins parent root r with 2 pi offset v; the group has `size` pixels
                     auto link = [&](int c, int r, int v, int size) {
                         bad |= v < -127 || v > 127;
-                        up[c] = (uint16_t)r;
+                        up[c] = (Idx)r;
                         pot[c] = (int8_t)v;
-                        up[r] = (uint16_t)(size - 1);
+                        up[r] = (Idx)(size - 1);
                     };
                     if (s2 == 1) link(r2, r1, a1 - jump, s1 + 1);              // pixel 2 alone
                     else if (s1 == 1) link(r1, r2, a2 + jump, s2 + 1);         // pixel 1 alone
@@ -263,13 +270,14 @@ k_hz_gather(const uint32_t* __restrict__ pays, size_t stride, const float* __res
             __syncwarp();
         }
         if (lane == 0 && bad) atomicOr(err, 8);
+        if (!SHARED) __threadfence_block();
     }
     __syncthreads();
     const float* ph = phase + (size_t)a * n;
     float* out = unwrapped + (size_t)a * n;
     for (int p = threadIdx.x; p < n; p += kHzThreads) {
         int acc = 0;
-        for (int q = p; pot[q] != kHzRoot; q = up[q]) acc += pot[q];
+        for (int q = p; pot[q] != kHzRoot; q = (int)up[q]) acc += pot[q];
         out[p] = __fadd_rn(ph[p], __fmul_rn(kHzTwoPi, __int2float_rn(acc)));
     }
 }
@@ -289,8 +297,10 @@ int launch_herraez(tdm_ctx* c, int a0, int m) {
     float* base[2] = {reinterpret_cast<float*>(b.qc), reinterpret_cast<float*>(b.tq)};
     for (int k = 0; k < 2; ++k) buf[k] = SortBuf{base[k], reinterpret_cast<uint32_t*>(base[k] + ne)};
     const size_t smem = hz_gather_smem(F);
-    if (smem > kMaxSmemPerCta || !b.hz_rand) return TDM_EUNSUPPORTED;
-    if (cudaFuncSetAttribute(k_hz_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    const bool shared = F <= 256 && smem <= kMaxSmemPerCta;  // uint16 parents
+    if (!b.hz_rand) return TDM_EUNSUPPORTED;
+    if (shared && cudaFuncSetAttribute(k_hz_gather<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem) != cudaSuccess)
         return TDM_ECUDA;
     {
         Launch l(c, K_HERRAEZ);
@@ -311,9 +321,15 @@ int launch_herraez(tdm_ctx* c, int a0, int m) {
         k_hz_sort_level<<<dim3((ne + kHzThreads - 1) / kHzThreads, m), kHzThreads, 0, c->stream>>>(
             buf[cur], buf[cur ^ 1], stride, b.gx, F, SortLevel{ne, d});
     }
-    {
+    if (shared) {
         Launch l(c, K_HERRAEZ);
-        k_hz_gather<<<m, kHzThreads, smem, c->stream>>>(buf[cur].pay, stride, b.phase, F, b.unwrapped, b.err);
+        k_hz_gather<uint16_t, true><<<m, kHzThreads, smem, c->stream>>>(buf[cur].pay, stride, b.phase, F,
+                                                                         b.unwrapped, b.err, nullptr, 0);
+    } else {  // the forest in the other sort buffer, free now: 5 bytes a pixel within 16 F^2 an angle
+        Launch l(c, K_HERRAEZ);
+        k_hz_gather<uint32_t, false><<<m, kHzThreads, 0, c->stream>>>(
+            buf[cur].pay, stride, b.phase, F, b.unwrapped, b.err, reinterpret_cast<unsigned char*>(base[cur ^ 1]),
+            stride * sizeof(float));
     }
     return cudaGetLastError() == cudaSuccess ? TDM_OK : TDM_ECUDA;
 }

@@ -184,10 +184,6 @@ int check_geom(const tdm_geom* g, std::string& why) {
         why = "crop window (CIRCLE_CX/CY +- NXMAX) outside the hologram spectrum";
         return TDM_EINVAL;
     }
-    if (g->c_aber && g->deroul && !g->volkov && F > 256) {
-        why = "VOLKOV 0 (Herraez unwrapping) needs 2*NXMAX <= 256 (its pixel groups live in one CTA's shared memory)";
-        return TDM_EUNSUPPORTED;
-    }
     if (!(g->na > 0) || !(g->n0 > 0) || !(g->lambda0 > 0) || !(g->f_obj > 0) || !(g->rf > 0) || !(g->f_tube > 0) ||
         !(g->tpcam > 0)) {
         why = "optical parameters must be positive";
