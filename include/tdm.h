@@ -57,7 +57,9 @@ typedef struct {
     int born;           /* BORN: 1 Born, 0 Rytov */
     int c_aber;         /* C_ABER: aberration correction (and unwrapping) on/off */
     int deroul;         /* DEROUL: phase unwrapping on/off (only with C_ABER) */
-    int volkov;         /* VOLKOV: 1 Volkov; 0 Herraez */
+    int volkov;         /* VOLKOV: 1 Volkov; 0 Herraez (tdm_create then draws the C library's
+                           rand() sequence as the reference would for max_angles angles:
+                           max_angles * (2*NXMAX)^2 draws, about 60 ms for 600 x 256^2) */
     double na;          /* NA */
     double n0;          /* N0 */
     double lambda0;     /* LAMBDA (m) */
