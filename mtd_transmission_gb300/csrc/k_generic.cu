@@ -35,6 +35,26 @@ constexpr float kInvTwoPiG = 0.15915494309189535f;
 constexpr int kRows = 8;  // warps (rows) per CTA of a row pass
 constexpr int kCols = 8;  // columns (warps) per CTA of a column pass
 
+// Element-wise copy of COUNT items by NT threads, thread tid taking items
+// tid, tid + NT, ...: the thread issues all of its loads before its first
+// store, so they are in flight together rather than one at a time behind
+// each store (the loop bounds are compile-time, the loops unrolled).
+template <int COUNT, int NT, class Load, class Store>
+__device__ __forceinline__ void staged_copy(int tid, Load&& load, Store&& store) {
+    constexpr int IT = (COUNT + NT - 1) / NT;
+    decltype(load(0)) v[IT];
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        if (i < COUNT) v[k] = load(i);
+    }
+#pragma unroll
+    for (int k = 0; k < IT; ++k) {
+        const int i = tid + k * NT;
+        if (i < COUNT) store(i, v[k]);
+    }
+}
+
 template <class K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
     if (bytes <= 48 * 1024) return cudaSuccess;
@@ -105,10 +125,9 @@ gk_field_rows(const float2* __restrict__ spectra, const float4* __restrict__ arg
     float2* A = sm + w * 2 * F;
     float2* B = A + F;
     const float2* src = spec + (size_t)wrap_f(r + p.y, F) * F;
-    for (int n = lane; n < F; n += 32) {
-        const float2 v = src[wrap_f(n + p.x, F)];
-        A[n] = normalize ? c_mul(v, nrm) : v;
-    }
+    staged_copy<F, 32>(
+        lane, [&](int n) { return src[wrap_f(n + p.x, F)]; },
+        [&](int n, float2 v) { A[n] = normalize ? c_mul(v, nrm) : v; });
     __syncwarp();
     gfft<F, +1, 4 * F>(A, B, wq, lane);
     float2* dst = I1 + ((size_t)a * F + r) * F;
@@ -123,10 +142,15 @@ gk_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict_
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, x0 = blockIdx.x * kCols;
-    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
-        const int t = i % kCols, r = i / kCols;
-        if (x0 + t < F) sm[t * 2 * F + r] = I1[((size_t)a * F + r) * F + x0 + t];
-    }
+    staged_copy<kCols * F, kCols * 32>(
+        threadIdx.x,
+        [&](int i) {
+            const int t = i % kCols, r = i / kCols;
+            return x0 + t < F ? I1[((size_t)a * F + r) * F + x0 + t] : make_float2(0.f, 0.f);
+        },
+        [&](int i, float2 v) {
+            if (x0 + i % kCols < F) sm[(i % kCols) * 2 * F + i / kCols] = v;
+        });
     __syncthreads();
     if (x0 + w < F) gfft<F, +1, 4 * F>(sm + w * 2 * F, sm + w * 2 * F + F, wq, lane);
     __syncthreads();
@@ -168,10 +192,13 @@ gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, 
     const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
     if (live) {
         const float2* zr = zph + (ab ? rb : ra);
-        for (int m = lane; m < F; m += 32) {
-            const int x = gmirror_pos(m, F);
-            A[m] = zk ? zr[x] : make_float2(phase[ra + x], phase[rb + x]);
-        }
+        staged_copy<F, 32>(
+            lane,
+            [&](int m) {
+                const int x = gmirror_pos(m, F);
+                return zk ? zr[x] : make_float2(phase[ra + x], phase[rb + x]);
+            },
+            [&](int m, float2 v) { A[m] = v; });
         __syncwarp();
         gmirror_derivative<F>(A, B, wq, lane);
     }
@@ -180,11 +207,13 @@ gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, 
         const float2* zr = zph + (ab ? rb : ra);
         const float2* q = sm + (2 * kPairs + pair) * 2 * F;
         float* out = gxh + (ab ? rb : ra);
-        for (int x = lane; x < F; x += 32) {
-            const float2 z = zr[x], g = A[x], qv = q[x];
-            const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
-            out[x] = (ax - (ab ? qv.y : qv.x)) * kInvTwoPiG;
-        }
+        staged_copy<F, 32>(
+            lane, [&](int x) { return zr[x]; },
+            [&](int x, float2 z) {
+                const float2 g = A[x], qv = q[x];
+                const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
+                out[x] = (ax - (ab ? qv.y : qv.x)) * kInvTwoPiG;
+            });
     }
 }
 
@@ -197,7 +226,7 @@ gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, 
 //     FFT(Q)[2F-k] = -2 (-1)^k w (Im C[F-k] - Re C[k]),  FFT(Q)[F] = 2 i Im C[0],
 //     C[k] = (w V[k] + conj(w) V[F-k]) / 2.
 template <int F>
-__global__ void __launch_bounds__((kCols + kCols / 2) * 32)
+__global__ void __launch_bounds__((kCols + kCols / 2) * 32, 3)
 gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
                const float2* __restrict__ wq, float2* __restrict__ qc) {
     constexpr int L = 2 * F, Q4 = 4 * F;
@@ -205,27 +234,41 @@ gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, x0 = blockIdx.x * kCols;
     auto arr = [&](int t) { return sm + t * 2 * F; };  // warp t's pair of F-point arrays
-    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
-        const int c = i % kCols, y = i / kCols;
-        if (x0 + c >= F) continue;
-        const size_t o = ((size_t)a * F + y) * F + x0 + c;
-        const int e = gslot(y, F);
-        arr(c)[e] = zph[o];
-        reinterpret_cast<float*>(&arr(kCols + (c >> 1))[e])[c & 1] = phase[o];
-    }
+    constexpr int NT = (kCols + kCols / 2) * 32;
+    staged_copy<kCols * F, NT>(
+        threadIdx.x,
+        [&](int i) {
+            const size_t o = ((size_t)a * F + i / kCols) * F + x0 + i % kCols;
+            if (x0 + i % kCols >= F) return make_float3(0.f, 0.f, 0.f);
+            const float2 z = zph[o];
+            return make_float3(z.x, z.y, phase[o]);
+        },
+        [&](int i, float3 v) {
+            const int c = i % kCols, e = gslot(i / kCols, F);
+            if (x0 + c >= F) return;
+            arr(c)[e] = make_float2(v.x, v.y);
+            reinterpret_cast<float*>(&arr(kCols + (c >> 1))[e])[c & 1] = v.z;
+        });
     __syncthreads();
     const bool live = x0 + (w < kCols ? w : 2 * (w - kCols)) < F;  // warp-uniform
     if (live) gmirror_derivative<F>(arr(w), arr(w) + F, wq, lane);
     __syncthreads();
-    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
-        const int c = i % kCols, y = i / kCols;
-        if (x0 + c >= F) continue;
-        const size_t o = ((size_t)a * F + y) * F + x0 + c;
-        const float2 z = zph[o], g = arr(c)[y], q = arr(kCols + (c >> 1))[y];
-        const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
-        const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPiG;
-        arr(c)[F + gslot(y, F)] = make_float2(gxh[o], (y & 1) ? -gy : gy);
-    }
+    staged_copy<kCols * F, NT>(
+        threadIdx.x,
+        [&](int i) {
+            const size_t o = ((size_t)a * F + i / kCols) * F + x0 + i % kCols;
+            if (x0 + i % kCols >= F) return make_float3(1.f, 0.f, 0.f);
+            const float2 z = zph[o];
+            return make_float3(z.x, z.y, gxh[o]);
+        },
+        [&](int i, float3 v) {
+            const int c = i % kCols, y = i / kCols;
+            if (x0 + c >= F) return;
+            const float2 g = arr(c)[y], q = arr(kCols + (c >> 1))[y];
+            const float ay = (g.y * v.x - g.x * v.y) / (v.x * v.x + v.y * v.y);
+            const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPiG;
+            arr(c)[F + gslot(y, F)] = make_float2(v.z, (y & 1) ? -gy : gy);
+        });
     __syncthreads();
     if (w < kCols && x0 + w < F) {
         float2* V = arr(w) + F;
@@ -282,14 +325,12 @@ gk_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ w
     float2* A = sm + w * 2 * L;
     float2* B = A + L;
     const int rp = r ? L - r : 0;
-    for (int X = lane; X < L; X += 32) {
-        if (X >= F) {
-            A[X] = qc[((size_t)a * L + r) * F + (X - F)];
-        } else {
-            const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
-            A[X] = make_float2(-u.x, u.y);
-        }
-    }
+    staged_copy<L, 32>(
+        lane,
+        [&](int X) {
+            return X >= F ? qc[((size_t)a * L + r) * F + (X - F)] : qc[((size_t)a * L + rp) * F + (F - 1 - X)];
+        },
+        [&](int X, float2 u) { A[X] = X >= F ? u : make_float2(-u.x, u.y); });
     __syncwarp();
     gfft<L, -1, Q4>(A, B, wq, lane);
     const float nrm = 1.0f / ((float)L * (float)L), ky = gkappa(r, L);
@@ -320,28 +361,34 @@ gk_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ ph
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, c0 = blockIdx.x * kCols;
-    for (int i = threadIdx.x; i < kCols * L; i += blockDim.x) {
-        const int t = i % kCols, ky = i / kCols;
-        if (c0 + t >= F) continue;
-        float2 v;
-        if (ky <= L / 2) {
-            v = tq[((size_t)a * L + ky) * F + c0 + t];
-        } else {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
-            const float2 u = tq[((size_t)a * L + (L - ky)) * F + c0 + t];
-            const float2 wv = groot<Q4, L, -1>(wq, ky);
-            v = make_float2(wv.x * u.x + wv.y * u.y, wv.x * u.y - wv.y * u.x);
-        }
-        sm[t * 2 * L + ky] = v;
-    }
+    staged_copy<kCols * L, kCols * 32>(
+        threadIdx.x,
+        [&](int i) {
+            const int t = i % kCols, ky = i / kCols;
+            return c0 + t < F ? tq[((size_t)a * L + (ky <= L / 2 ? ky : L - ky)) * F + c0 + t] : make_float2(0.f, 0.f);
+        },
+        [&](int i, float2 u) {
+            const int t = i % kCols, ky = i / kCols;
+            if (c0 + t >= F) return;
+            if (ky > L / 2) {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
+                const float2 wv = groot<Q4, L, -1>(wq, ky);
+                u = make_float2(wv.x * u.x + wv.y * u.y, wv.x * u.y - wv.y * u.x);
+            }
+            sm[t * 2 * L + ky] = u;
+        });
     __syncthreads();
     if (c0 + w < F) gfft<L, +1, Q4>(sm + w * 2 * L, sm + w * 2 * L + L, wq, lane);
     __syncthreads();
-    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
-        const int t = i % kCols, y = i / kCols;
-        if (c0 + t >= F) continue;
-        const size_t o = ((size_t)a * F + y) * F + c0 + t;
-        unwrapped[o] = phase[o] + kTwoPiG * sm[t * 2 * L + F + y].x;
-    }
+    staged_copy<kCols * F, kCols * 32>(
+        threadIdx.x,
+        [&](int i) {
+            const size_t o = ((size_t)a * F + i / kCols) * F + c0 + i % kCols;
+            return c0 + i % kCols < F ? phase[o] : 0.f;
+        },
+        [&](int i, float ph) {
+            const int t = i % kCols, y = i / kCols;
+            if (c0 + t < F) unwrapped[((size_t)a * F + y) * F + c0 + t] = ph + kTwoPiG * sm[t * 2 * L + F + y].x;
+        });
 }
 
 // ---------------------------------------------------------------- cap passes
@@ -395,10 +442,15 @@ gk_cap_cols(const float2* __restrict__ r1, const int2* __restrict__ posspec, con
     const int a = blockIdx.y, kx0 = blockIdx.x * kCols;
     const int2 ps = posspec[a];
     if (threadIdx.x == 0) s_fz = cap_fzm0(p, ps);
-    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
-        const int t = i % kCols, ky = i / kCols;
-        if (kx0 + t < F) sm[t * 2 * F + ky] = r1[((size_t)a * F + ky) * F + kx0 + t];
-    }
+    staged_copy<kCols * F, kCols * 32>(
+        threadIdx.x,
+        [&](int i) {
+            const int t = i % kCols, ky = i / kCols;
+            return kx0 + t < F ? r1[((size_t)a * F + ky) * F + kx0 + t] : make_float2(0.f, 0.f);
+        },
+        [&](int i, float2 v) {
+            if (kx0 + i % kCols < F) sm[(i % kCols) * 2 * F + i / kCols] = v;
+        });
     __syncthreads();
     if (kx0 + w < F) gfft<F, -1, 4 * F>(sm + w * 2 * F, sm + w * 2 * F + F, wq, lane);
     __syncthreads();
