@@ -225,6 +225,7 @@ gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, 
 //     FFT(Q)[k] = 2 (-1)^k conj(w) (Re C[k] + Im C[F-k]),
 //     FFT(Q)[2F-k] = -2 (-1)^k w (Im C[F-k] - Re C[k]),  FFT(Q)[F] = 2 i Im C[0],
 //     C[k] = (w V[k] + conj(w) V[F-k]) / 2.
+// Three CTAs per SM (48 KB of shared memory each): registers capped at 56.
 template <int F>
 __global__ void __launch_bounds__((kCols + kCols / 2) * 32, 3)
 gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,

@@ -2,9 +2,11 @@
 the CPU (no GPU), with the index arithmetic of fft_generic.cuh and
 k_generic.cu:
 
-- gfft: the radix plan (4 first, then 2, 3, 5, 7) and the Stockham passes
-  (read b + k N/R, twiddle W_(S R)^((b mod S) k), R-point DFT, write
-  (b / S) S R + (b mod S) + m S) against numpy.fft, both signs;
+- gfft: the radix plan (10 while it divides, then 4, 2, 3, 5, 7), the
+  Stockham passes (read b + k N/R, twiddle W_(S R)^((b mod S) k) formed as
+  W^(k/2) W^(k - k/2) from W^1, R-point DFT, write
+  (b / S) S R + (b mod S) + m S) and the radix-10 DFT's 2 x 5 register
+  decomposition against numpy.fft, both signs;
 - gmirror_derivative: the 2F-point even mirror's spectral derivative at
   X = F + x from F-point transforms, the partner bin F - k read at index
   (k ? F - k : 0);
@@ -18,10 +20,39 @@ import pytest
 
 
 def gfft_radix(m):
-    for r in (4, 2, 3, 5, 7):
+    for r in (10, 4, 2, 3, 5, 7):
         if m % r == 0:
             return r
     return m
+
+
+def dft(v, sign):
+    R = len(v)
+    return np.array([np.sum(v * np.exp(sign * 2j * np.pi * np.arange(R) * m / R)) for m in range(R)])
+
+
+def dft_composite(x, R1, R2, sign):
+    """Emulates dft_composite<R1, R2>: k = R2 k1 + k2, m = m1 + R1 m2."""
+    R = R1 * R2
+    y = np.empty(R, complex)  # y[m1 R2 + k2]
+    for k2 in range(R2):
+        v = dft(np.array([x[R2 * k1 + k2] for k1 in range(R1)]), sign)
+        for m1 in range(R1):
+            y[m1 * R2 + k2] = v[m1] * np.exp(sign * 2j * np.pi * ((k2 * m1) % R) / R)
+    out = np.empty(R, complex)
+    for m1 in range(R1):
+        u = dft(y[m1 * R2:(m1 + 1) * R2], sign)
+        for m2 in range(R2):
+            out[m1 + R1 * m2] = u[m2]
+    return out
+
+
+def twiddle_powers(w1, R):
+    """W^k for k < R from W^1 as gfft_pass forms them."""
+    t = [1.0 + 0j, w1]
+    for k in range(2, R):
+        t.append(t[k >> 1] * t[k - (k >> 1)])
+    return np.array(t[:R])
 
 
 def gfft(x, sign):
@@ -36,14 +67,32 @@ def gfft(x, sign):
         for b in range(NB):
             p = b % S
             v = np.array([a[b + k * NB] for k in range(R)])
-            v = v * np.exp(sign * 2j * np.pi * p * np.arange(R) / (S * R))
-            y = np.array([np.sum(v * np.exp(sign * 2j * np.pi * np.arange(R) * m / R)) for m in range(R)])
+            v = v * twiddle_powers(np.exp(sign * 2j * np.pi * p / (S * R)), R)
+            y = dft_composite(v, 2, 5, sign) if R == 10 else dft(v, sign)
             base = (b // S) * S * R + p
             for m in range(R):
                 out[base + m * S] = y[m]
         a = out
         S *= R
     return a
+
+
+def test_radix_plan():
+    def passes(n):
+        out = []
+        while n > 1:
+            r = gfft_radix(n)
+            out.append(r)
+            n //= r
+        return out
+    assert passes(250) == [10, 5, 5] and passes(500) == [10, 10, 5]
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_radix10_register_decomposition(sign):
+    rng = np.random.default_rng(10)
+    x = rng.standard_normal(10) + 1j * rng.standard_normal(10)
+    assert np.abs(dft_composite(x, 2, 5, sign) - dft(x, sign)).max() <= 1e-12
 
 
 @pytest.mark.parametrize("N", [250, 500, 200, 300, 112, 6])
