@@ -45,17 +45,20 @@ SCHEDULE = (16, 4)  # angles per chunk, chunks in flight (tdm_set_schedule)
 # each kernel (what it must read and write at least once, wherever it lives).
 def algorithmic_bytes(name, acq, hits_per_angle, band):
     H, F, D = acq.ccd_roix, 2 * acq.nxmax, acq.dim_final
-    L = 2 * F
     per_angle = {
         "extract_rows": H * H * 2 + H * F * 8,
         "extract_cols": H * F * 8 + F * F * 8,
         "argmax": F * F * 8,
         "field_rows": F * F * 8 * 2,
         "field_cols": F * F * 8 + F * F * 4 * 2,
-        "volkov_rows": F * F * 4 + L * L * 4,
-        "volkov_cols": F * F * 4 + L * L * 4 + L * L * 8,
-        "volkov_integ_rows": L * L * 8 + L * F * 8,
-        "volkov_integ_cols": L * F * 8 + F * F * 4 * 2,
+        # phase and phasor in, gx out
+        "volkov_rows": F * F * 4 + F * F * 8 + F * F * 4,
+        # phase, phasor and gx in; the columns' DCT-II of gx and DST-II of gy out
+        "volkov_cols": F * F * 4 + F * F * 8 + F * F * 4 + F * F * 8,
+        # those in, one real row of the Poisson solve's DCT-III along x out
+        "volkov_integ_rows": F * F * 8 + F * F * 4,
+        # that and the wrapped phase in, the unwrapped phase out
+        "volkov_integ_cols": F * F * 4 * 3,
         "aber_fit": 2 * F * F * 4,
         "form": 3 * F * F * 4 + F * F * 8,
         "cap_rows": 2 * F * F * 8,

@@ -10,11 +10,14 @@
 //             1D spectral derivative of each row (kappa depends on kx only), so
 //             gradient_fft4 becomes a row pass and a column pass, each computed
 //             from F-point transforms (the mirror's spectrum is a DCT of the row,
-//             its derivative a DST: mirror_derivative); the two real fields of
-//             integ_grad4 share one complex 2D FFT (x + i y) and are separated by
-//             Hermitian symmetry.  Literal kappa (the mirror's Nyquist bin is
-//             zero, so its -1/2 factor does not enter the derivatives), literal
-//             Re() projections, zero-frequency term 0.
+//             its derivative a DST: mirror_derivative).  integ_grad4's Poisson
+//             solve on the mirror is a DCT-II / DST-II of the quadrant's gx and
+//             gy, a division by |kappa|^2 and an inverse DCT (DCT-III) back to
+//             the quadrant, all from F-point transforms (k_volkov_integ_rows).
+//             Literal kappa: the mirror's Nyquist bin of the derivatives is
+//             zero, and the Nyquist row and column of the Poisson solve cancel
+//             in the real part kept on the quadrant, so the -1/2 factor does
+//             not enter; literal Re() projections, zero-frequency term 0.
 //  fit/form   aberCorr2 / ampliCorr2 (Correction_aberration.cpp:166-217) and the
 //             Born/Rytov formation (main.cpp:289-316).  The least-squares
 //             projection onto degree-4 polynomials is computed in a basis that is
@@ -37,10 +40,6 @@ cudaError_t allow_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-__device__ __forceinline__ float kappa(int k, int L) {  // init_kvect_shift, FFT_fonctions.cpp:7-17
-    return (float)(k < L / 2 ? k : k - L) / (float)L;
-}
-__device__ __forceinline__ int mirror(int X, int F) { return X >= F ? X - F : F - 1 - X; }
 
 // ---------------------------------------------------------------- argmax
 // coordSpec (fonctions.cpp:88-101) in two steps: partial winners over slices
@@ -203,20 +202,20 @@ __device__ __forceinline__ void mirror_derivative(float2 (&x)[WarpFFT<F>::E], fl
     for (int n1 = 0; n1 < E; ++n1) x[n1] = (j + n1 * T < F / 2) ? y[n1] : make_float2(-y[n1].x, -y[n1].y);
 }
 
-// 2F-point FFT of a column with Q[2F-1-Y] = conj(Q[Y]) from one F-point
-// transform.  With u[y] = Q[F + y], a = Re u, b = Im u,
-//     FFT(Q)[k] = 2 (-1)^k e^{i pi k/2F} R[k],
-//     R[k] = sum_y a[y] cos(pi k (y + 1/2)/F) + b[y] sin(pi k (y + 1/2)/F),
-// real.  The cosine sum is a DCT-II of a and the sine sum a DCT-II of
-// b' = (-1)^y b read backwards, so both come from C = DCT-II(a + i b') (the
-// first half of mirror_derivative): with w = e^{-i pi k/2F},
-//     C[k] = (w V[k] + conj(w) V[F-k]) / 2,  C[F-k] = i (w V[k] - conj(w) V[F-k]) / 2,
-//     R[k] = Re C[k] + Im C[F-k],  R[2F-k] = Im C[F-k] - Re C[k],  R[F] = Im C[0].
-// x holds a + i b' permuted by mirror_pos (x[n1] = element j + T n1) on
-// entry; out(k, value) receives every bin k in [0, 2F) once.
+// The DCT-II along a column of gx and the DST-II of gy, for k in [0, F),
+// from one F-point transform (Makhoul's algorithm, two real sequences in one
+// complex transform):
+//     DCT-II(a)[k] = sum_y a[y] cos(pi k (2y + 1)/2F),
+//     DST-II(b)[k] = sum_y b[y] sin(pi k (2y + 1)/2F) = DCT-II((-1)^y b)[F - k].
+// With V the transform of a + i (-1)^y b permuted by mirror_pos and
+// w = e^{-i pi k/2F},
+//     DCT-II(a)[k] = Re(w V[k] + conj(w) V[F-k]) / 2,
+//     DST-II(b)[k] = Re(w V[k] - conj(w) V[F-k]) / 2.
+// x holds a + i (-1)^y b permuted (x[n1] = element j + T n1) on entry;
+// out(k, (DCT-II(a)[k], DST-II(b)[k])) receives every bin k in [0, F) once.
 template <int F, class Out>
-__device__ __forceinline__ void symmetric_fft(float2 (&x)[WarpFFT<F>::E], float2* s, int j,
-                                              const float2* __restrict__ tw, Out&& out) {
+__device__ __forceinline__ void column_dct_dst(float2 (&x)[WarpFFT<F>::E], float2* s, int j,
+                                               const float2* __restrict__ tw, Out&& out) {
     using W = WarpFFT<F>;
     constexpr int E = W::E, T = W::T, L = 2 * F;
     fft_warp_regs<F, -1>(x, s, j, tw);
@@ -232,20 +231,9 @@ __device__ __forceinline__ void symmetric_fft(float2 (&x)[WarpFFT<F>::E], float2
             const float2 pv = x[(E / T - 1 - q) * T + (T - 1 - k2)];
             float2 vm = make_float2(__shfl_sync(0xffffffffu, pv.x, src), __shfl_sync(0xffffffffu, pv.y, src));
             if (j == 0) vm = x[q == 0 ? (T - k2) % T : (E / T - q) * T + (T - 1 - k2)];
-            const int k = j + q * T + E * k2;
             const float2 w = twc<4 * T, k2, -1>(wl[q]);  // e^{-i pi k/2F}
             const float2 a = c_mul(w, x[q * T + k2]), b = c_mul(c_conj(w), vm);
-            const float ck = 0.5f * (a.x + b.x);          // Re C[k]
-            const float cf = 0.5f * (a.x - b.x);          // Im C[F-k] = Re((w V[k] - conj(w) V[F-k]) / 2)
-            const float sg = (k & 1) ? -2.0f : 2.0f;      // 2 (-1)^k
-            if (k == 0) {
-                out(0, make_float2(2.0f * ck, 0.0f));
-                out(F, make_float2(0.0f, 2.0f * 0.5f * (a.y + b.y)));  // 2 i Im C[0]
-            } else {
-                const float r1 = sg * (ck + cf), r2 = -sg * (cf - ck);
-                out(k, make_float2(r1 * w.x, -r1 * w.y));         // 2 (-1)^k conj(w) R[k]
-                out(L - k, make_float2(r2 * w.x, r2 * w.y));      // -2 (-1)^k w R[2F-k]
-            }
+            out(j + q * T + E * k2, make_float2(0.5f * (a.x + b.x), 0.5f * (a.x - b.x)));
         });
     });
 }
@@ -264,9 +252,8 @@ struct RCfg {
 
 // Pass 2 in CTAs of NC = 8 mirror columns: 12 F-point derivative transforms
 // (8 of Z, one per column, then 4 of the columns' packed phases), then NC
-// F-point transforms giving the 2F-point FFT of Q along each column
-// (symmetric_fft).  Bins [0, F) of a column's FFT are staged in its Q array,
-// bins [F, 2F) in the derivative array of the same index.
+// F-point transforms giving each column's DCT-II of gx and DST-II of gy
+// (column_dct_dst), staged in its Q array.
 template <int L>
 struct VCfg {
     using WF = WarpFFT<L / 2>;
@@ -303,7 +290,7 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
     const bool zk = tr < 2 * P;                       // Z transform of one row, else packed phases of a pair
     const int pair = zk ? tr >> 1 : tr - 2 * P, ab = tr & 1;
     const int a = blockIdx.y;
-    const int ya = blockIdx.x * 2 * P + 2 * pair, yb = ya + 1;
+    const int ya = blockIdx.x * 2 * P + 2 * pair;
     float2* s = sm + tr * W::STRIDE;
     const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
     const float2* zr = zph + (ab ? rb : ra);
@@ -339,23 +326,22 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
 }
 
 // Pass 2: columns X = F + x of the mirror (columns X and L-1-X are the same
-// image column): gy like gx, then Q = gx + i gy and its FFT along y.  The
-// columns X < F follow from Q[.][X] = -conj(Q[.][L-1-X]) and are rebuilt by
-// pass 3.  Along a column the y derivative of the even mirror is odd and gx is
-// even, so Q[L-1-Y] = conj(Q[Y]): the derivatives come from F-point transforms
-// on the half Y = F + y (mirror_derivative), and so does the FFT of Q
-// (symmetric_fft).  The loads and the gy epilogue run CTA-wide with the NC
-// columns fastest (contiguous in global memory); the phasor and gx are read
-// from L2 in the epilogue.
+// image column): gy like gx, then the first half of the Poisson solve's
+// transforms: along y, gx (even about the mirror's axis) is a DCT-II and gy
+// (odd) a DST-II of the quadrant's column, c[ky][x] = (DCT-II_y gx,
+// DST-II_y gy) for ky in [0, F) (column_dct_dst).  The derivatives come from
+// F-point transforms on the half Y = F + y (mirror_derivative).  The loads and
+// the gy epilogue run CTA-wide with the NC columns fastest (contiguous in
+// global memory); the phasor and gx are read from L2 in the epilogue.
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
 k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
-              const float2* __restrict__ tw, float2* __restrict__ qc) {
+              const float2* __restrict__ tw, float2* __restrict__ cdct) {
     using C = VCfg<L>;
     using WF = typename C::WF;
     constexpr int F = L / 2, NC = C::NC, NT = C::NT, FS = C::FS, T = WF::T, E = WF::E;
     extern __shared__ float2 sm[];
-    float2* sq = sm + C::BF * FS;  // NC arrays: Q of each column (permuted), then its FFT bins [0, F)
+    float2* sq = sm + C::BF * FS;  // NC arrays: gx + i (-1)^y gy of each column (permuted), then c[.][x]
     const int a = blockIdx.y, x0 = blockIdx.x * NC;
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     auto src = [&](int y, int c) { return ((size_t)a * F + y) * F + x0 + c; };
@@ -382,7 +368,7 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
     }
     __syncthreads();
     // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi and Q = gx + i gy at Y = F + y;
-    // the Q array takes gx + i (-1)^y gy, permuted (symmetric_fft's input)
+    // the Q array takes gx + i (-1)^y gy, permuted (column_dct_dst's input)
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * F; i += NT) {
         const int c = i % NC, y = i / NC;
@@ -398,137 +384,177 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
     __syncthreads();
     if (tr < NC) {  // warp-uniform
         float2* s = sq + tr * FS;
-        float2* hi = sm + tr * FS;  // the derivative array of the same index, free now
         float2 x[E];
 #pragma unroll
         for (int n1 = 0; n1 < E; ++n1) x[n1] = s[WF::pad(j + n1 * T)];
-        symmetric_fft<F>(x, s, j, tw, [&](int k, float2 v) {
-            if (k < F) s[k] = v;
-            else hi[k - F] = v;
-        });
+        column_dct_dst<F>(x, s, j, tw, [&](int k, float2 v) { s[k] = v; });
     }
     __syncthreads();
 #pragma unroll 4
-    for (int i = threadIdx.x; i < NC * L; i += NT) {
+    for (int i = threadIdx.x; i < NC * F; i += NT) {
         const int c = i % NC, ky = i / NC;
-        qc[((size_t)a * L + ky) * F + x0 + c] = ky < F ? sq[c * FS + ky] : sm[c * FS + ky - F];
+        cdct[((size_t)a * F + ky) * F + x0 + c] = sq[c * FS + ky];
     }
 }
 
-// Pass 3: rows ky in [0, L/2] of FFT2(Q); integ_grad4's tampon; inverse FFT
-// along x; only the quadrant-4 columns are kept.  The mirror symmetries of Q
-// give conj(Q^(-k)) = -exp(2 pi i (kx+ky)/L) conj(Q^(k)) (the Hermitian
-// partner needed to separate gx and gy), and the tampon rows obey
-// tam(kx, -ky) = exp(-2 pi i ky/L) tam(kx, ky), so pass 4 rebuilds the rows
-// ky > L/2.  The row's left half comes from the stored right half of row -ky.
-template <int L>
-struct TamMul {
-    int r;
-    float nrm, ky;
-    // w = exp(-2 pi i (kx + ky)/L)
-    __device__ __forceinline__ float2 operator()(int kx, float2 w, float2 Q) const {
-        // Qm = conj(Q^(-k)) = -exp(+2 pi i (kx+ky)/L) conj(Q)
-        const float2 Qm = make_float2(-(w.x * Q.x - w.y * Q.y), -(-w.y * Q.x - w.x * Q.y));
-        const float2 Gx = make_float2(0.5f * (Q.x + Qm.x) * nrm, 0.5f * (Q.y + Qm.y) * nrm);
-        const float2 Gy = make_float2(0.5f * (Q.y - Qm.y) * nrm, -0.5f * (Q.x - Qm.x) * nrm);
-        const float kxv = kappa(kx, L);
-        const float k2 = kxv * kxv + ky * ky;
-        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
-        const float rden = 1.0f / (kTwoPi * k2);
-        return (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y * rden, -num.x * rden);
-    }
-};
-
-template <int L>
+// Pass 3: rows ky of the Poisson solve: integ_grad4 on the mirror
+// (src/deroulement_volkov4.cpp:162-191) followed by cut_quad4 (:247-276),
+// reduced to the quadrant.  With kappa = k/2F (init_kvect_shift, FFT_fonctions.cpp:7-17, on
+// the half k < F that the folding keeps), A = DST-II_x DCT-II_y gx and
+// B = DCT-II_x DST-II_y gy (k in [0, F)^2),
+//     P = -4/L^2 (kappa_x A + kappa_y B) / (kappa_x^2 + kappa_y^2),  P(0, 0) = 0,
+//     2 pi IntM = DCT-III_y DCT-III_x P,  DCT-III(P)[n] = sum_k w_k P[k] cos(pi k (2n+1)/2F),
+// w_0 = 1, w_k = 2: the 2F x 2F transforms of the reference, with the
+// symmetric halves of the spectrum folded together (the Nyquist terms cancel).
+// Along x, A and B come from one F-point transform of (-1)^x Re c + i Im c
+// permuted by mirror_pos: with V that transform, w = e^{-i pi k/2F},
+// qu = w (V[k] + conj V[F-k]) / 2 and qv = w (V[k] - conj V[F-k]) / 2i,
+//     A[k] = -Im qu,  B[k] = Re qv.
+// The DCT-III of two real rows is one inverse transform: with
+// X = P_r1 + i P_r2 and X[F] = 0, the unnormalised inverse transform of
+// conj(w) (X[k] - i X[F-k]) is U_r1 + i U_r2 permuted by mirror_pos.
+template <int F>
 struct ICfg {
-    using W = WarpFFT<L>;
-    static constexpr int B = 8 * W::G;   // rows or columns per CTA
-    static constexpr int NT = B * W::T;
-    static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
+    using W = WarpFFT<F>;
+    static constexpr int NW = 4;                   // warps per CTA
+    static constexpr int R = 2 * NW * W::G;        // rows (pass 3) or columns (pass 4) per CTA, two per transform
+    static constexpr int NT = NW * 32;
+    static constexpr size_t SMEM = (size_t)NW * W::G * W::STRIDE * sizeof(float2);
 };
 
-template <int L>
-__global__ void __launch_bounds__(ICfg<L>::NT)
-k_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ tw, float2* __restrict__ tq) {
-    using C = ICfg<L>;
-    using W = typename C::W;
-    constexpr int F = L / 2, T = W::T, E = W::E;
-    extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / T, j = threadIdx.x % T;
-    const int a = blockIdx.y, r = blockIdx.x * C::B + tr;
-    const bool active = r <= L / 2;  // rows past L/2 only keep their warp company
-    const int rp = (L - r) & (L - 1);
-    float2 x[E];
-#pragma unroll
-    for (int n1 = 0; n1 < E; ++n1) {
-        const int X = j + n1 * T;
-        float2 v = make_float2(0.f, 0.f);
-        if (active) {
-            if (X >= F) {
-                v = qc[((size_t)a * L + r) * F + (X - F)];
-            } else {
-                const float2 u = qc[((size_t)a * L + rp) * F + (F - 1 - X)];
-                v = make_float2(-u.x, u.y);
-            }
-        }
-        x[n1] = v;
-    }
-    // forward FFT along x, tampon, inverse FFT: fft_warp_filter with the
-    // twiddle exp(-2 pi i (kx + r)/L) of bin kx = j + q T + E k2 formed as the
-    // lane's factor for (j + q T + r) times the compile-time root exp(-2 pi i k2/T)
-    float2 wl[E / T];
-#pragma unroll
-    for (int q = 0; q < E / T; ++q) wl[q] = __ldg(&tw[((j + q * T + r) & (L - 1)) * (kTwN / L)]);
-    const TamMul<L> tam{r, 1.0f / ((float)L * (float)L), kappa(r, L)};
-    float2* s = sm + tr * W::STRIDE;
-    fft_warp_regs<L, -1>(x, s, j, tw);
+// P[k] of the lane's bins of one row from its transform x (bin (j + qT) + E k2
+// in register qT + k2), src the holder of bin F - k.
+template <int F>
+__device__ __forceinline__ void poisson_row(const float2 (&x)[WarpFFT<F>::E], const float2 (&wl)[WarpFFT<F>::E / WarpFFT<F>::T],
+                                            int j, int src, float kyv, float (&p)[WarpFFT<F>::E]) {
+    using W = WarpFFT<F>;
+    constexpr int E = W::E, T = W::T, L = 2 * F;
+    constexpr float s = -4.0f / ((float)L * (float)L);
     static_for<0, E / T>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
         static_for<0, T>([&](auto kc) {
             constexpr int k2 = decltype(kc)::value;
-            x[q * T + k2] = tam(j + q * T + E * k2, twc<T, k2, -1>(wl[q]), x[q * T + k2]);
+            const float2 pv = x[(E / T - 1 - q) * T + (T - 1 - k2)];
+            float2 vm = make_float2(__shfl_sync(0xffffffffu, pv.x, src), __shfl_sync(0xffffffffu, pv.y, src));
+            if (j == 0) vm = x[q == 0 ? (T - k2) % T : (E / T - q) * T + (T - 1 - k2)];
+            const int k = j + q * T + E * k2;
+            const float2 w = twc<4 * T, k2, -1>(wl[q]);  // e^{-i pi k/2F}
+            const float2 v = x[q * T + k2];
+            const float2 e = c_mul(w, make_float2(v.x + vm.x, v.y - vm.y));  // 2 qu
+            const float2 d = c_mul(w, make_float2(v.x - vm.x, v.y + vm.y));  // 2i qv
+            const float kx = (float)k / (float)L;
+            const float den = kx * kx + kyv * kyv;
+            // A = -Im qu = -e.y / 2, B = Re qv = d.y / 2
+            p[q * T + k2] = den > 0.0f ? (0.5f * s) * (kyv * d.y - kx * e.y) / den : 0.0f;
         });
     });
-    fft_warp_regs_rev<L, +1>(x, s, j, tw);
-    if (active) {
-        float2* dst = tq + ((size_t)a * L + r) * F - F;
+}
+
+// The DCT-III input of the lanes' bins: y = conj(w) (X[k] - i X[F-k]), X[F] = 0.
+template <int F>
+__device__ __forceinline__ void dct3_input(const float2 (&xv)[WarpFFT<F>::E], const float2 (&wl)[WarpFFT<F>::E / WarpFFT<F>::T],
+                                           int j, int src, float2 (&y)[WarpFFT<F>::E]) {
+    using W = WarpFFT<F>;
+    constexpr int E = W::E, T = W::T;
+    static_for<0, E / T>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        static_for<0, T>([&](auto kc) {
+            constexpr int k2 = decltype(kc)::value;
+            const float2 pv = xv[(E / T - 1 - q) * T + (T - 1 - k2)];
+            float2 xm = make_float2(__shfl_sync(0xffffffffu, pv.x, src), __shfl_sync(0xffffffffu, pv.y, src));
+            if (j == 0) xm = q == 0 && k2 == 0 ? make_float2(0.0f, 0.0f) : xv[q == 0 ? (T - k2) % T : (E / T - q) * T + (T - 1 - k2)];
+            const float2 w = twc<4 * T, k2, -1>(wl[q]);  // e^{-i pi k/2F}
+            const float2 xk = xv[q * T + k2];
+            y[q * T + k2] = c_mul(c_conj(w), make_float2(xk.x + xm.y, xk.y - xm.x));
+        });
+    });
+}
+
+template <int F>
+__global__ void __launch_bounds__(ICfg<F>::NT)
+k_volkov_integ_rows(const float2* __restrict__ cdct, const float2* __restrict__ tw, float* __restrict__ urows) {
+    using C = ICfg<F>;
+    using W = typename C::W;
+    constexpr int T = W::T, E = W::E, L = 2 * F;
+    extern __shared__ float2 sm[];
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    const int a = blockIdx.y, r1 = blockIdx.x * C::R + 2 * tr;  // rows r1 and r1 + 1
+    float2* s = sm + tr * W::STRIDE;
+    const int src = ((threadIdx.x & 31) & ~(T - 1)) + ((T - j) & (T - 1));  // holder of bin F - k
+    float2 wl[E / T];  // e^{-i pi (j + qT)/2F}
 #pragma unroll
-        for (int n1 = E / 2; n1 < E; ++n1) dst[j + n1 * T] = x[n1];
+    for (int q = 0; q < E / T; ++q) wl[q] = __ldg(&tw[(j + q * T) * (kTwN / (2 * L))]);
+    float p1[E], p2[E];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float2* row = cdct + ((size_t)a * F + r1 + h) * F;
+        float2 x[E];
+#pragma unroll
+        for (int n1 = 0; n1 < E; ++n1) {  // element m = j + T n1 is column mirror_pos(m): even for m < F/2
+            const int m = j + n1 * T;
+            const float2 v = row[mirror_pos(m, F)];
+            x[n1] = make_float2(m < F / 2 ? v.x : -v.x, v.y);
+        }
+        fft_warp_regs<F, -1>(x, s, j, tw);
+        poisson_row<F>(x, wl, j, src, (float)(r1 + h) / (float)L, h ? p2 : p1);
+    }
+    float2 xv[E], y[E];
+#pragma unroll
+    for (int n = 0; n < E; ++n) xv[n] = make_float2(p1[n], p2[n]);
+    dct3_input<F>(xv, wl, j, src, y);
+    fft_warp_regs_rev<F, +1>(y, s, j, tw);
+    float* u1 = urows + ((size_t)a * F + r1) * F;
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int xx = mirror_pos(j + n1 * T, F);
+        u1[xx] = y[n1].x;
+        u1[F + xx] = y[n1].y;
     }
 }
 
-// Pass 4: columns of quadrant 4: inverse FFT along y, real part, phi + 2 pi IntM.
-template <int L>
-__global__ void __launch_bounds__(ICfg<L>::NT)
-k_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ phase, const float2* __restrict__ tw,
+// Pass 4: columns of U, two per transform: the DCT-III along y (dct3_input
+// and one inverse transform) gives 2 pi IntM, and phi + 2 pi IntM is stored
+// through the transforms' arrays, rows contiguous.
+template <int F>
+__global__ void __launch_bounds__(ICfg<F>::NT)
+k_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ phase, const float2* __restrict__ tw,
                     float* __restrict__ unwrapped) {
-    using C = ICfg<L>;
+    using C = ICfg<F>;
     using W = typename C::W;
-    constexpr int F = L / 2, B = C::B, NT = C::NT;
+    constexpr int T = W::T, E = W::E, L = 2 * F, R = C::R, NT = C::NT;
     extern __shared__ float2 sm[];
-    const int tr = threadIdx.x / W::T, j = threadIdx.x % W::T;
-    const int a = blockIdx.y, c0 = blockIdx.x * B;
+    const int tr = threadIdx.x / T, j = threadIdx.x % T;
+    const int a = blockIdx.y, c0 = blockIdx.x * R;
+    float* smf = reinterpret_cast<float*>(sm);
+    // column c0 + t of U into float slot (t & 1) of transform t / 2's array, at row ky
 #pragma unroll  // every staging load in flight before the first store
-    for (int r = 0; r < B * L / NT; ++r) {
-        const int i = threadIdx.x + r * NT, t = i % B, ky = i / B;
-        float2 v;
-        if (ky <= L / 2) {
-            v = tq[((size_t)a * L + ky) * F + c0 + t];
-        } else {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
-            const float2 u = tq[((size_t)a * L + (L - ky)) * F + c0 + t];
-            const float2 w = __ldg(&tw[ky * (kTwN / L)]);  // exp(-2 pi i ky/L)
-            v = make_float2(w.x * u.x + w.y * u.y, w.x * u.y - w.y * u.x);
-        }
-        sm[t * W::STRIDE + W::pad(ky)] = v;
+    for (int r = 0; r < R * F / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % R, ky = i / R;
+        smf[2 * ((t >> 1) * W::STRIDE + ky) + (t & 1)] = urows[((size_t)a * F + ky) * F + c0 + t];
     }
     __syncthreads();
-    fft_warp<L, +1>(sm + tr * W::STRIDE, j, tw);
+    float2* s = sm + tr * W::STRIDE;
+    const int src = ((threadIdx.x & 31) & ~(T - 1)) + ((T - j) & (T - 1));
+    float2 wl[E / T];
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) wl[q] = __ldg(&tw[(j + q * T) * (kTwN / (2 * L))]);
+    float2 xv[E], y[E];
+#pragma unroll
+    for (int q = 0; q < E / T; ++q) {
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) xv[q * T + k2] = s[j + q * T + E * k2];
+    }
+    dct3_input<F>(xv, wl, j, src, y);
+    fft_warp_regs_rev<F, +1>(y, s, j, tw);
+    __syncwarp();  // the transform's exchange is done with s
+#pragma unroll
+    for (int n1 = 0; n1 < E; ++n1) s[mirror_pos(j + n1 * T, F)] = y[n1];
     __syncthreads();
 #pragma unroll 8
-    for (int r = 0; r < B * F / NT; ++r) {
-        const int i = threadIdx.x + r * NT, t = i % B, y = i / B;
-        const size_t o = ((size_t)a * F + y) * F + c0 + t;
-        unwrapped[o] = phase[o] + kTwoPi * sm[t * W::STRIDE + W::pad(F + y)].x;
+    for (int r = 0; r < R * F / NT; ++r) {
+        const int i = threadIdx.x + r * NT, t = i % R, yy = i / R;
+        const size_t o = ((size_t)a * F + yy) * F + c0 + t;
+        unwrapped[o] = phase[o] + smf[2 * ((t >> 1) * W::STRIDE + yy) + (t & 1)];
     }
 }
 
@@ -625,7 +651,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     constexpr int L = 2 * F;
     using FC = FieldCfg<F>;
     using VC = VCfg<L>;
-    using IC = ICfg<L>;
+    using IC = ICfg<F>;
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
@@ -634,7 +660,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     const size_t sm_vcols = VC::SMEM_COLS;
     if (allow_smem(k_field_rows<F>, FC::SMEM) || allow_smem(k_field_cols<F>, FC::SMEM) ||
         allow_smem(k_volkov_rows<L>, sm_vrows) || allow_smem(k_volkov_cols<L>, sm_vcols) ||
-        allow_smem(k_volkov_integ_rows<L>, IC::SMEM) || allow_smem(k_volkov_integ_cols<L>, IC::SMEM))
+        allow_smem(k_volkov_integ_rows<F>, IC::SMEM) || allow_smem(k_volkov_integ_cols<F>, IC::SMEM))
         return TDM_ECUDA;
     for (int g0 = a0; g0 < a0 + n; g0 += c->chunk) {
         const int m = (a0 + n - g0) < c->chunk ? (a0 + n - g0) : c->chunk;
@@ -671,15 +697,15 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
                 k_volkov_cols<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vcols, c->stream>>>(b.phase, b.zph, b.gx,
                                                                                                      b.tw, b.qc);
             }
+            float* urows = reinterpret_cast<float*>(b.tq);
             {
                 Launch l(c, K_VOLKOV_INTEG_ROWS);
-                k_volkov_integ_rows<L><<<dim3((L / 2 + IC::B) / IC::B, m), IC::NT, IC::SMEM, c->stream>>>(
-                    b.qc, b.tw, b.tq);
+                k_volkov_integ_rows<F><<<dim3(F / IC::R, m), IC::NT, IC::SMEM, c->stream>>>(b.qc, b.tw, urows);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
-                k_volkov_integ_cols<L><<<dim3(F / IC::B, m), IC::NT, IC::SMEM, c->stream>>>(b.tq, b.phase, b.tw,
-                                                                                                  b.unwrapped);
+                k_volkov_integ_cols<F><<<dim3(F / IC::R, m), IC::NT, IC::SMEM, c->stream>>>(urows, b.phase, b.tw,
+                                                                                              b.unwrapped);
             }
             unw = b.unwrapped;
         }

@@ -15,9 +15,12 @@
 //  gk_volkov_rows / gk_volkov_cols deroul_volkov4_total_sym_paire (src/deroulement_volkov4.cpp:14-92):
 //                                  the mirror's derivatives from F-point transforms
 //                                  (a DCT-II of the row, its derivative a DST), and
-//                                  the 2F-point FFT of Q = gx + i gy along each column
-//                                  from one F-point transform (Q is conjugate-symmetric)
-//  gk_volkov_integ_rows / _cols    integ_grad4 (:162-191) and cut_quad4 (:247-276)
+//                                  the DCT-II of gx and DST-II of gy along each column
+//                                  from one F-point transform
+//  gk_volkov_integ_rows / _cols    integ_grad4 (:162-191) and cut_quad4 (:247-276) as
+//                                  k_fields.cu's Poisson passes compute them: along x
+//                                  the second half of the forward transforms, the
+//                                  division by |kappa|^2 and a DCT-III; along y a DCT-III
 //  gk_cap_rows(_form) / gk_cap_cols per-field spectrum (Reconstruction/main.cpp:203-217)
 //                                  and the cap records of retroPropag_Born
 //                                  (Reconstruction/src/fonctions.cpp:875-935)
@@ -64,10 +67,6 @@ cudaError_t allow_smem(K kernel, size_t bytes) {
 __host__ __device__ constexpr int gmirror_pos(int m, int F) { return m < F / 2 ? 2 * m : 2 * (F - 1 - m) + 1; }
 // element m of the permuted sequence that holds row (or column) y: gmirror_pos(m) = y
 __host__ __device__ constexpr int gslot(int y, int F) { return (y & 1) ? F - 1 - (y >> 1) : (y >> 1); }
-
-__device__ __forceinline__ float gkappa(int k, int L) {  // init_kvect_shift, FFT_fonctions.cpp:7-17
-    return (float)(k < L / 2 ? k : k - L) / (float)L;
-}
 
 // exp(s 2 pi i k / M) from the 4F-entry table (M divides 4F).
 template <int Q, int M, int S>
@@ -218,18 +217,18 @@ gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, 
 }
 
 // Pass 2: columns X = F + x of the mirror, kCols per CTA: the y derivatives
-// (kCols Z columns, kCols/2 packed phase pairs), gy and Q = gx + i gy, then
-// the 2F-point FFT of Q along each column from one F-point transform of
-// gx + i (-1)^y gy permuted by gmirror_pos (the algebra of k_fields.cu's
-// symmetric_fft): with V that transform and w = e^{-i pi k/2F},
-//     FFT(Q)[k] = 2 (-1)^k conj(w) (Re C[k] + Im C[F-k]),
-//     FFT(Q)[2F-k] = -2 (-1)^k w (Im C[F-k] - Re C[k]),  FFT(Q)[F] = 2 i Im C[0],
-//     C[k] = (w V[k] + conj(w) V[F-k]) / 2.
+// (kCols Z columns, kCols/2 packed phase pairs), gy, then the column's
+// DCT-II of gx and DST-II of gy from one F-point transform of
+// gx + i (-1)^y gy permuted by gmirror_pos (k_fields.cu's column_dct_dst):
+// with V that transform and w = e^{-i pi k/2F},
+//     DCT-II(gx)[k] = Re(w V[k] + conj(w) V[F-k]) / 2,
+//     DST-II(gy)[k] = Re(w V[k] - conj(w) V[F-k]) / 2,
+// stored as cdct[ky][x] for ky in [0, F).
 // Three CTAs per SM (48 KB of shared memory each): registers capped at 56.
 template <int F>
 __global__ void __launch_bounds__((kCols + kCols / 2) * 32, 3)
 gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
-               const float2* __restrict__ wq, float2* __restrict__ qc) {
+               const float2* __restrict__ wq, float2* __restrict__ cdct) {
     constexpr int L = 2 * F, Q4 = 4 * F;
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -275,120 +274,117 @@ gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, 
         float2* V = arr(w) + F;
         float2* S = arr(w);
         gfft<F, -1, Q4>(V, S, wq, lane);
-        // bins of this column: [0, F) into S, [F, 2F) into the phase pair's arrays
-        // (free now), after every lane has read V
-        float2 lo[(F + 31) / 32], hi[(F + 31) / 32];
-#pragma unroll
-        for (int u = 0; u < (F + 31) / 32; ++u) {
-            const int k = lane + 32 * u;
-            if (k >= F) break;
+        for (int k = lane; k < F; k += 32) {  // S is free: gfft left the result in V
             const float2 wk = groot<Q4, 2 * L, -1>(wq, k);  // e^{-i pi k/2F}
             const float2 va = c_mul(wk, V[k]), vb = c_mul(c_conj(wk), V[k ? F - k : 0]);
-            const float ck = 0.5f * (va.x + vb.x), cf = 0.5f * (va.x - vb.x);
-            const float sg = (k & 1) ? -2.0f : 2.0f;
-            if (k == 0) {
-                lo[u] = make_float2(2.0f * ck, 0.0f);
-                hi[u] = make_float2(0.0f, va.y + vb.y);  // bin F
-            } else {
-                const float r1 = sg * (ck + cf), r2 = -sg * (cf - ck);
-                lo[u] = make_float2(r1 * wk.x, -r1 * wk.y);  // bin k
-                hi[u] = make_float2(r2 * wk.x, r2 * wk.y);   // bin 2F - k
-            }
-        }
-        __syncwarp();
-        float2* H = arr(kCols + (w >> 1)) + (w & 1) * F;
-#pragma unroll
-        for (int u = 0; u < (F + 31) / 32; ++u) {
-            const int k = lane + 32 * u;
-            if (k >= F) break;
-            S[k] = lo[u];
-            H[k == 0 ? 0 : F - k] = hi[u];  // bin F + j at H[j]
+            S[k] = make_float2(0.5f * (va.x + vb.x), 0.5f * (va.x - vb.x));
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kCols * L; i += blockDim.x) {
+    for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
         const int c = i % kCols, ky = i / kCols;
-        if (x0 + c >= F) continue;
-        qc[((size_t)a * L + ky) * F + x0 + c] = ky < F ? arr(c)[ky] : arr(kCols + (c >> 1))[(c & 1) * F + ky - F];
+        if (x0 + c < F) cdct[((size_t)a * F + ky) * F + x0 + c] = arr(c)[ky];
     }
 }
 
-// Pass 3: rows ky in [0, L/2] of FFT2(Q); integ_grad4's tampon; inverse FFT
-// along x; the quadrant-4 columns are kept (k_volkov_integ_rows' algebra).
+// Pass 3: row pairs of the Poisson solve (k_fields.cu's k_volkov_integ_rows):
+// per row, one F-point transform of (-1)^x Re c + i Im c permuted by
+// gmirror_pos gives A = DST-II_x and B = DCT-II_x of the row, and
+// P = -4/L^2 (kappa_x A + kappa_y B) / (kappa_x^2 + kappa_y^2); the two rows'
+// P = P_r1 + i P_r2 then take one inverse transform for their DCT-III along x.
+// Three F-point arrays per warp: the transform, its scratch and P.
 template <int F>
 __global__ void __launch_bounds__(kRows * 32)
-gk_volkov_integ_rows(const float2* __restrict__ qc, const float2* __restrict__ wq, float2* __restrict__ tq) {
+gk_volkov_integ_rows(const float2* __restrict__ cdct, const float2* __restrict__ wq, float* __restrict__ urows) {
     constexpr int L = 2 * F, Q4 = 4 * F;
+    constexpr float sc = -4.0f / ((float)L * (float)L);
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int a = blockIdx.y, r = blockIdx.x * kRows + w;
-    if (r > L / 2) return;  // warp-uniform; no CTA barrier below
-    float2* A = sm + w * 2 * L;
-    float2* B = A + L;
-    const int rp = r ? L - r : 0;
-    staged_copy<L, 32>(
-        lane,
-        [&](int X) {
-            return X >= F ? qc[((size_t)a * L + r) * F + (X - F)] : qc[((size_t)a * L + rp) * F + (F - 1 - X)];
-        },
-        [&](int X, float2 u) { A[X] = X >= F ? u : make_float2(-u.x, u.y); });
-    __syncwarp();
-    gfft<L, -1, Q4>(A, B, wq, lane);
-    const float nrm = 1.0f / ((float)L * (float)L), ky = gkappa(r, L);
-    for (int kx = lane; kx < L; kx += 32) {
-        const float2 wv = groot<Q4, L, -1>(wq, kx + r);  // exp(-2 pi i (kx + ky)/L)
-        const float2 Qv = A[kx];
-        const float2 Qm = make_float2(-(wv.x * Qv.x - wv.y * Qv.y), -(-wv.y * Qv.x - wv.x * Qv.y));
-        const float2 Gx = make_float2(0.5f * (Qv.x + Qm.x) * nrm, 0.5f * (Qv.y + Qm.y) * nrm);
-        const float2 Gy = make_float2(0.5f * (Qv.y - Qm.y) * nrm, -0.5f * (Qv.x - Qm.x) * nrm);
-        const float kxv = gkappa(kx, L);
-        const float k2 = kxv * kxv + ky * ky;
-        const float2 num = make_float2(kxv * Gx.x + ky * Gy.x, kxv * Gx.y + ky * Gy.y);
-        const float rden = 1.0f / (kTwoPiG * k2);
-        A[kx] = (r == 0 && kx == 0) ? make_float2(0.0f, 0.0f) : make_float2(num.y * rden, -num.x * rden);
+    const int a = blockIdx.y, r1 = 2 * (blockIdx.x * kRows + w);
+    if (r1 >= F) return;  // warp-uniform; no CTA barrier below
+    float2* A = sm + w * 3 * F;
+    float2* B = A + F;
+    float2* P = B + F;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float2* row = cdct + ((size_t)a * F + r1 + h) * F;
+        staged_copy<F, 32>(
+            lane, [&](int m) { return row[gmirror_pos(m, F)]; },
+            [&](int m, float2 v) { A[m] = make_float2(m < F / 2 ? v.x : -v.x, v.y); });  // (-1)^x, x = gmirror_pos(m)
+        __syncwarp();
+        gfft<F, -1, Q4>(A, B, wq, lane);
+        const float kyv = (float)(r1 + h) / (float)L;
+        for (int k = lane; k < F; k += 32) {
+            const float2 v = A[k], vm = A[k ? F - k : 0];
+            const float2 wk = groot<Q4, 2 * L, -1>(wq, k);  // e^{-i pi k/2F}
+            const float2 e = c_mul(wk, make_float2(v.x + vm.x, v.y - vm.y));  // 2 qu
+            const float2 d = c_mul(wk, make_float2(v.x - vm.x, v.y + vm.y));  // 2i qv
+            const float kx = (float)k / (float)L, den = kx * kx + kyv * kyv;
+            const float pk = den > 0.0f ? (0.5f * sc) * (kyv * d.y - kx * e.y) / den : 0.0f;
+            reinterpret_cast<float*>(&P[k])[h] = pk;
+        }
+        __syncwarp();  // every lane has read A before the next row overwrites it
+    }
+    for (int k = lane; k < F; k += 32) {  // DCT-III input conj(w) (X[k] - i X[F-k]), X[F] = 0
+        const float2 x = P[k], xm = k ? P[F - k] : make_float2(0.0f, 0.0f);
+        A[k] = c_mul(c_conj(groot<Q4, 2 * L, -1>(wq, k)), make_float2(x.x + xm.y, x.y - xm.x));
     }
     __syncwarp();
-    gfft<L, +1, Q4>(A, B, wq, lane);
-    float2* dst = tq + ((size_t)a * L + r) * F - F;
-    for (int X = F + lane; X < L; X += 32) dst[X] = A[X];
+    gfft<F, +1, Q4>(A, B, wq, lane);
+    float* u1 = urows + ((size_t)a * F + r1) * F;
+    for (int m = lane; m < F; m += 32) {
+        const int x = gmirror_pos(m, F);
+        u1[x] = A[m].x;
+        u1[F + x] = A[m].y;
+    }
 }
 
-// Pass 4: columns of quadrant 4: inverse FFT along y, real part, phi + 2 pi IntM.
+// Pass 4: column pairs: the DCT-III along y gives 2 pi IntM, and
+// phi + 2 pi IntM is stored with the columns fastest.  Three F-point arrays
+// per warp: the transform, its scratch and the column pair.
 template <int F>
 __global__ void __launch_bounds__(kCols * 32)
-gk_volkov_integ_cols(const float2* __restrict__ tq, const float* __restrict__ phase, const float2* __restrict__ wq,
+gk_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ phase, const float2* __restrict__ wq,
                      float* __restrict__ unwrapped) {
-    constexpr int L = 2 * F, Q4 = 4 * F;
+    constexpr int L = 2 * F, Q4 = 4 * F, NC = 2 * kCols;
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int a = blockIdx.y, c0 = blockIdx.x * kCols;
-    staged_copy<kCols * L, kCols * 32>(
+    const int a = blockIdx.y, c0 = blockIdx.x * NC;
+    auto pair = [&](int t) { return sm + t * 3 * F + 2 * F; };  // warp t's column pair
+    staged_copy<NC * F, kCols * 32>(
         threadIdx.x,
         [&](int i) {
-            const int t = i % kCols, ky = i / kCols;
-            return c0 + t < F ? tq[((size_t)a * L + (ky <= L / 2 ? ky : L - ky)) * F + c0 + t] : make_float2(0.f, 0.f);
+            const int t = i % NC, ky = i / NC;
+            return c0 + t < F ? urows[((size_t)a * F + ky) * F + c0 + t] : 0.f;
         },
-        [&](int i, float2 u) {
-            const int t = i % kCols, ky = i / kCols;
-            if (c0 + t >= F) return;
-            if (ky > L / 2) {  // tam(kx, ky) = exp(2 pi i ky/L) tam(kx, L - ky)
-                const float2 wv = groot<Q4, L, -1>(wq, ky);
-                u = make_float2(wv.x * u.x + wv.y * u.y, wv.x * u.y - wv.y * u.x);
-            }
-            sm[t * 2 * L + ky] = u;
+        [&](int i, float u) {
+            const int t = i % NC, ky = i / NC;
+            reinterpret_cast<float*>(&pair(t >> 1)[ky])[t & 1] = u;
         });
     __syncthreads();
-    if (c0 + w < F) gfft<L, +1, Q4>(sm + w * 2 * L, sm + w * 2 * L + L, wq, lane);
+    if (c0 + 2 * w < F) {  // warp-uniform; F is even, so both columns are in range
+        float2* A = sm + w * 3 * F;
+        float2* B = A + F;
+        float2* X = pair(w);
+        for (int k = lane; k < F; k += 32) {
+            const float2 x = X[k], xm = k ? X[F - k] : make_float2(0.0f, 0.0f);
+            A[k] = c_mul(c_conj(groot<Q4, 2 * L, -1>(wq, k)), make_float2(x.x + xm.y, x.y - xm.x));
+        }
+        __syncwarp();
+        gfft<F, +1, Q4>(A, B, wq, lane);
+        for (int m = lane; m < F; m += 32) X[gmirror_pos(m, F)] = A[m];
+    }
     __syncthreads();
-    staged_copy<kCols * F, kCols * 32>(
+    staged_copy<NC * F, kCols * 32>(
         threadIdx.x,
         [&](int i) {
-            const size_t o = ((size_t)a * F + i / kCols) * F + c0 + i % kCols;
-            return c0 + i % kCols < F ? phase[o] : 0.f;
+            const size_t o = ((size_t)a * F + i / NC) * F + c0 + i % NC;
+            return c0 + i % NC < F ? phase[o] : 0.f;
         },
         [&](int i, float ph) {
-            const int t = i % kCols, y = i / kCols;
-            if (c0 + t < F) unwrapped[((size_t)a * F + y) * F + c0 + t] = ph + kTwoPiG * sm[t * 2 * L + F + y].x;
+            const int t = i % NC, y = i / NC;
+            if (c0 + t < F)
+                unwrapped[((size_t)a * F + y) * F + c0 + t] = ph + reinterpret_cast<const float*>(&pair(t >> 1)[y])[t & 1];
         });
 }
 
@@ -479,13 +475,12 @@ constexpr size_t warp_arrays(int n, int warps) { return (size_t)warps * 2 * n * 
 template <int F>
 int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapped, float* dbg_amp, int argparts,
                  bool form) {
-    constexpr int L = 2 * F;
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
     const size_t sm_rows = warp_arrays(F, kRows), sm_cols = warp_arrays(F, kCols);
     const size_t sm_vrows = warp_arrays(F, 3 * kPairs), sm_vcols = warp_arrays(F, kCols + kCols / 2);
-    const size_t sm_irows = warp_arrays(L, kRows), sm_icols = warp_arrays(L, kCols);
+    const size_t sm_irows = (size_t)kRows * 3 * F * sizeof(float2), sm_icols = (size_t)kCols * 3 * F * sizeof(float2);
     if (allow_smem(gk_field_rows<F>, sm_rows) || allow_smem(gk_field_cols<F>, sm_cols) ||
         allow_smem(gk_volkov_rows<F>, sm_vrows) || allow_smem(gk_volkov_cols<F>, sm_vcols) ||
         allow_smem(gk_volkov_integ_rows<F>, sm_irows) || allow_smem(gk_volkov_integ_cols<F>, sm_icols))
@@ -521,15 +516,16 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
                 gk_volkov_cols<F><<<dim3(cols, m), (kCols + kCols / 2) * 32, sm_vcols, c->stream>>>(
                     b.phase, b.zph, b.gx, b.wq, b.qc);
             }
+            float* urows = reinterpret_cast<float*>(b.tq);
             {
                 Launch l(c, K_VOLKOV_INTEG_ROWS);
-                gk_volkov_integ_rows<F><<<dim3((L / 2 + kRows) / kRows, m), kRows * 32, sm_irows, c->stream>>>(
-                    b.qc, b.wq, b.tq);
+                gk_volkov_integ_rows<F><<<dim3((F / 2 + kRows - 1) / kRows, m), kRows * 32, sm_irows, c->stream>>>(
+                    b.qc, b.wq, urows);
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
-                gk_volkov_integ_cols<F><<<dim3(cols, m), kCols * 32, sm_icols, c->stream>>>(b.tq, b.phase, b.wq,
-                                                                                          b.unwrapped);
+                gk_volkov_integ_cols<F><<<dim3((F + 2 * kCols - 1) / (2 * kCols), m), kCols * 32, sm_icols,
+                                          c->stream>>>(urows, b.phase, b.wq, b.unwrapped);
             }
             unw = b.unwrapped;
         }
