@@ -10,7 +10,13 @@
 //             1D spectral derivative of each row (kappa depends on kx only), so
 //             gradient_fft4 becomes a row pass and a column pass, each computed
 //             from F-point transforms (the mirror's spectrum is a DCT of the row,
-//             its derivative a DST: mirror_derivative).  integ_grad4's Poisson
+//             its derivative a DST: mirror_derivative).  The wrapped phase's own
+//             gradient, which the reference subtracts from the phasor's before the
+//             Poisson solve and whose solve it adds back, returns the phase less
+//             its mean (the solve inverts the spectral gradient exactly, the mean
+//             being the zero-frequency term it sets to 0), so the passes solve
+//             for the phasor's gradient alone and add the mean of the wrapped
+//             phase.  integ_grad4's Poisson
 //             solve on the mirror is a DCT-II / DST-II of the quadrant's gx and
 //             gy, a division by |kappa|^2 and an inverse DCT (DCT-III) back to
 //             the quadrant, all from F-point transforms (k_volkov_integ_rows).
@@ -27,6 +33,7 @@
 #include "fft_warp.cuh"
 #include "form.cuh"
 #include "argmax.cuh"
+#include "phase_mean.cuh"
 
 namespace tdm {
 namespace {
@@ -112,10 +119,14 @@ k_field_rows(const float2* __restrict__ spectra, const float4* __restrict__ argp
 }
 
 // mode 1: phase/amplitude (C_ABER); mode 0: the field itself is the result.
+// mode 1 also leaves the CTA's sum of the wrapped phase in
+// psum[a * kPhaseParts + blockIdx.x] (FP32 per thread and warp, FP64 across
+// the warps in a fixed order).
 template <int F>
 __global__ void __launch_bounds__(FieldCfg<F>::NT)
 k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ tw, float* __restrict__ phase,
-             float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields) {
+             float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields,
+             double* __restrict__ psum) {
     using C = FieldCfg<F>;
     using W = typename C::W;
     constexpr int B = C::B, NT = C::NT;
@@ -130,6 +141,7 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
     __syncthreads();
     fft_warp<F, +1>(sm + tr * W::STRIDE, j, tw);
     __syncthreads();
+    float acc = 0.0f;
 #pragma unroll 8
     for (int r0 = 0; r0 < B * F / NT; ++r0) {
         const int i = threadIdx.x + r0 * NT, t = i % B, y = i / B;
@@ -138,7 +150,9 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
         const size_t o = ((size_t)a * F + yo) * F + xo;
         if (mode) {
             const float m = hypotf(u.x, u.y);
-            phase[o] = atan2f(u.y, u.x);
+            const float ph = atan2f(u.y, u.x);
+            phase[o] = ph;
+            acc += ph;
             amp[o] = m;
             // exp(i phase) without the round trip through the angle; atan2(0, 0) = 0
             zph[o] = m > 0.0f ? make_float2(u.x / m, u.y / m) : make_float2(1.0f, 0.0f);
@@ -146,6 +160,7 @@ k_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__
             fields[o] = u;
         }
     }
+    if (mode) phase_sum_cta<NT>(acc, psum + (size_t)a * kPhaseParts + blockIdx.x);
 }
 
 // ---------------------------------------------------------------- Volkov unwrap
@@ -238,95 +253,74 @@ __device__ __forceinline__ void column_dct_dst(float2 (&x)[WarpFFT<F>::E], float
     });
 }
 
-// Pass 1 in CTAs of 4 image row pairs: 8 row transforms of Z, then 4 of the
-// pairs' packed phases, F-point each (mirror_derivative).
+// Pass 1 in CTAs of 8 image rows: one F-point derivative transform of Z per
+// row (mirror_derivative).
 template <int F>
 struct RCfg {
     using W = WarpFFT<F>;
-    static constexpr int P = 4;                 // row pairs per CTA
-    static constexpr int B = 3 * P;             // transforms per CTA
+    static constexpr int B = 8;                 // rows (transforms) per CTA
     static constexpr int NT = B * W::T;
-    static_assert((2 * P) % W::G == 0, "a warp holds one kind of transform");
+    static_assert(B % W::G == 0, "whole warps");
     static constexpr size_t SMEM = (size_t)B * W::STRIDE * sizeof(float2);
 };
 
-// Pass 2 in CTAs of NC = 8 mirror columns: 12 F-point derivative transforms
-// (8 of Z, one per column, then 4 of the columns' packed phases), then NC
-// F-point transforms giving each column's DCT-II of gx and DST-II of gy
-// (column_dct_dst), staged in its Q array.
+// Pass 2 in CTAs of NC = 8 mirror columns: NC F-point derivative transforms
+// of Z, then NC F-point transforms giving each column's DCT-II of gx and
+// DST-II of gy (column_dct_dst), staged in its Q array.
 template <int L>
 struct VCfg {
     using WF = WarpFFT<L / 2>;
-    static constexpr int P = 4;                  // column pairs per CTA
-    static constexpr int NC = 2 * P;             // columns per CTA
-    static constexpr int BF = 3 * P;             // derivative transforms per CTA
-    static_assert(NC % WF::G == 0, "a warp holds one kind of derivative transform");
+    static constexpr int NC = 8;                 // columns per CTA
+    static constexpr int BF = NC;                // derivative transforms per CTA
+    static_assert(NC % WF::G == 0, "whole warps");
     static constexpr int NT = BF * WF::T;
     // array stride 2 mod 16 float2 and at least F: a warp's 8 columns x 4 rows
     // of the staging loops land in distinct banks
     static constexpr int FS = WF::LEN + ((2 - WF::LEN % 16) + 16) % 16;
     static constexpr size_t SMEM_COLS = (size_t)(BF + NC) * FS * sizeof(float2);
     // CTAs per SM the registers are bounded for (up to L = 512; larger mirrors
-    // need their registers).  Alone the pass runs faster at 2 CTAs; with four
-    // chunks in flight the smaller footprint leaves room for the other streams' CTAs.
-    static constexpr int COLS_CTAS = L <= 512 ? 3 : 1;
+    // need their registers)
+    static constexpr int COLS_CTAS = L <= 512 ? 4 : 1;
 };
 
 // Pass 1: rows of the mirror.  Mirror rows Y and L-1-Y are the same image
-// row, and only the right half of gx = (Re(-i dZ/dx / Z) - Re(dphi/dx)) / 2pi
-// is kept: gx[Y][X] = sign(X) gxh[m(Y)][m(X)].  Each image row's x derivative
-// on that half comes from F-point transforms (mirror_derivative): one of Z
-// per row, one of the packed phases phi_a + i phi_b per pair.
+// row, and only the right half of the phasor's gradient
+// gx = Re(-i dZ/dx / Z) / 2pi is kept: gx[Y][X] = sign(X) gxh[m(Y)][m(X)].
+// Each image row's x derivative on that half comes from F-point transforms
+// (mirror_derivative).
 template <int L>
 __global__ void __launch_bounds__(RCfg<L / 2>::NT)
-k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ tw,
-              float* __restrict__ gxh) {
+k_volkov_rows(const float2* __restrict__ zph, const float2* __restrict__ tw, float* __restrict__ gxh) {
     constexpr int F = L / 2;
     using C = RCfg<F>;
     using W = typename C::W;
-    constexpr int T = W::T, E = W::E, P = C::P;
+    constexpr int T = W::T, E = W::E;
     extern __shared__ float2 sm[];
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
-    const bool zk = tr < 2 * P;                       // Z transform of one row, else packed phases of a pair
-    const int pair = zk ? tr >> 1 : tr - 2 * P, ab = tr & 1;
-    const int a = blockIdx.y;
-    const int ya = blockIdx.x * 2 * P + 2 * pair;
+    const int a = blockIdx.y, y = blockIdx.x * C::B + tr;
     float2* s = sm + tr * W::STRIDE;
-    const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
-    const float2* zr = zph + (ab ? rb : ra);
+    const size_t row = ((size_t)a * F + y) * F;
+    const float2* zr = zph + row;
     float2 x[E];
-    if (zk) {
 #pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) x[n1] = zr[mirror_pos(j + n1 * T, F)];
-    } else {
-#pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) {
-            const int p = mirror_pos(j + n1 * T, F);
-            x[n1] = make_float2(phase[ra + p], phase[rb + p]);
-        }
-    }
+    for (int n1 = 0; n1 < E; ++n1) x[n1] = zr[mirror_pos(j + n1 * T, F)];
     mirror_derivative<F>(x, s, j, tw);
     __syncwarp();  // the transform's exchanges are done with s
 #pragma unroll
     for (int n1 = 0; n1 < E; ++n1) s[W::pad(mirror_pos(j + n1 * T, F))] = x[n1];
-    __syncthreads();
-    if (zk) {
-        const float2* sp = sm + (2 * P + pair) * W::STRIDE;
-        float* out = gxh + (ab ? rb : ra);
+    __syncwarp();
+    float* out = gxh + row;
 #pragma unroll
-        for (int n1 = 0; n1 < E; ++n1) {
-            const int xx = j + n1 * T;
-            const float2 z = zr[xx];
-            const float2 g = s[W::pad(xx)];
-            const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
-            const float2 q = sp[W::pad(xx)];
-            out[xx] = (ax - (ab ? q.y : q.x)) * kInvTwoPi;
-        }
+    for (int n1 = 0; n1 < E; ++n1) {
+        const int xx = j + n1 * T;
+        const float2 z = zr[xx];
+        const float2 g = s[W::pad(xx)];
+        out[xx] = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y) * kInvTwoPi;  // Re(-i g / Z) / 2pi
     }
 }
 
 // Pass 2: columns X = F + x of the mirror (columns X and L-1-X are the same
-// image column): gy like gx, then the first half of the Poisson solve's
+// image column): gy = Re(-i dZ/dy / Z) / 2pi like gx, then the first half of the Poisson solve's
 // transforms: along y, gx (even about the mirror's axis) is a DCT-II and gy
 // (odd) a DST-II of the quadrant's column, c[ky][x] = (DCT-II_y gx,
 // DST-II_y gy) for ky in [0, F) (column_dct_dst).  The derivatives come from
@@ -335,8 +329,8 @@ k_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, c
 // global memory); the phasor and gx are read from L2 in the epilogue.
 template <int L>
 __global__ void __launch_bounds__(VCfg<L>::NT, VCfg<L>::COLS_CTAS)
-k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
-              const float2* __restrict__ tw, float2* __restrict__ cdct) {
+k_volkov_cols(const float2* __restrict__ zph, const float* __restrict__ gxh, const float2* __restrict__ tw,
+              float2* __restrict__ cdct) {
     using C = VCfg<L>;
     using WF = typename C::WF;
     constexpr int F = L / 2, NC = C::NC, NT = C::NT, FS = C::FS, T = WF::T, E = WF::E;
@@ -351,12 +345,10 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
     for (int i = threadIdx.x; i < NC * F; i += NT) {
         const int c = i % NC, y = i / NC;
         const size_t o = src(y, c);
-        const int e = WF::pad(slot(y));
-        sm[c * FS + e] = zph[o];
-        reinterpret_cast<float*>(&sm[(NC + (c >> 1)) * FS + e])[c & 1] = phase[o];
+        sm[c * FS + WF::pad(slot(y))] = zph[o];
     }
     __syncthreads();
-    {  // y derivatives of Z (transforms 0 .. NC-1) and of the packed phases
+    {  // y derivatives of Z
         float2* s = sm + tr * FS;
         float2 x[E];
 #pragma unroll
@@ -367,8 +359,8 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
         for (int n1 = 0; n1 < E; ++n1) s[WF::pad(mirror_pos(j + n1 * T, F))] = x[n1];
     }
     __syncthreads();
-    // gy = (Re(-i dZ/dy / Z) - Re(dphi/dy)) / 2pi and Q = gx + i gy at Y = F + y;
-    // the Q array takes gx + i (-1)^y gy, permuted (column_dct_dst's input)
+    // gy = Re(-i dZ/dy / Z) / 2pi at Y = F + y; the Q array takes
+    // gx + i (-1)^y gy, permuted (column_dct_dst's input)
 #pragma unroll 4
     for (int i = threadIdx.x; i < NC * F; i += NT) {
         const int c = i % NC, y = i / NC;
@@ -376,13 +368,11 @@ k_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, c
         const float2 z = zph[o];
         const float gx = gxh[o];
         const float2 g = sm[c * FS + WF::pad(y)];
-        const float2 q = sm[(NC + (c >> 1)) * FS + WF::pad(y)];
-        const float ay = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);
-        const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPi;
+        const float gy = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y) * kInvTwoPi;
         sq[c * FS + WF::pad(slot(y))] = make_float2(gx, (y & 1) ? -gy : gy);
     }
     __syncthreads();
-    if (tr < NC) {  // warp-uniform
+    {
         float2* s = sq + tr * FS;
         float2 x[E];
 #pragma unroll
@@ -513,12 +503,13 @@ k_volkov_integ_rows(const float2* __restrict__ cdct, const float2* __restrict__ 
 }
 
 // Pass 4: columns of U, two per transform: the DCT-III along y (dct3_input
-// and one inverse transform) gives 2 pi IntM, and phi + 2 pi IntM is stored
-// through the transforms' arrays, rows contiguous.
+// and one inverse transform) gives the unwrapped phase less its mean, and the
+// wrapped phase's mean (from the field column pass's nps sums) is added as
+// the rows are stored, contiguous, through the transforms' arrays.
 template <int F>
 __global__ void __launch_bounds__(ICfg<F>::NT)
-k_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ phase, const float2* __restrict__ tw,
-                    float* __restrict__ unwrapped) {
+k_volkov_integ_cols(const float* __restrict__ urows, const double* __restrict__ psum, int nps,
+                    const float2* __restrict__ tw, float* __restrict__ unwrapped) {
     using C = ICfg<F>;
     using W = typename C::W;
     constexpr int T = W::T, E = W::E, L = 2 * F, R = C::R, NT = C::NT;
@@ -526,6 +517,8 @@ k_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ p
     const int tr = threadIdx.x / T, j = threadIdx.x % T;
     const int a = blockIdx.y, c0 = blockIdx.x * R;
     float* smf = reinterpret_cast<float*>(sm);
+    __shared__ float s_mean;
+    if (threadIdx.x == 0) s_mean = phase_mean(psum + (size_t)a * kPhaseParts, nps, F);  // ordered by the barrier below
     // column c0 + t of U into float slot (t & 1) of transform t / 2's array, at row ky
 #pragma unroll  // every staging load in flight before the first store
     for (int r = 0; r < R * F / NT; ++r) {
@@ -550,11 +543,11 @@ k_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ p
 #pragma unroll
     for (int n1 = 0; n1 < E; ++n1) s[mirror_pos(j + n1 * T, F)] = y[n1];
     __syncthreads();
+    const float mean = s_mean;
 #pragma unroll 8
     for (int r = 0; r < R * F / NT; ++r) {
         const int i = threadIdx.x + r * NT, t = i % R, yy = i / R;
-        const size_t o = ((size_t)a * F + yy) * F + c0 + t;
-        unwrapped[o] = phase[o] + smf[2 * ((t >> 1) * W::STRIDE + yy) + (t & 1)];
+        unwrapped[((size_t)a * F + yy) * F + c0 + t] = mean + smf[2 * ((t >> 1) * W::STRIDE + yy) + (t & 1)];
     }
 }
 
@@ -655,6 +648,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
     const Params& p = c->p;
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
+    static_assert(F / FC::B <= kPhaseParts, "phase sums per angle");
     using RC = RCfg<F>;
     const size_t sm_vrows = RC::SMEM;
     const size_t sm_vcols = VC::SMEM_COLS;
@@ -679,7 +673,7 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         {
             Launch l(c, K_FIELD_COLS);
             k_field_cols<F><<<dim3(F / FC::B, m), FC::NT, FC::SMEM, c->stream>>>(
-                b.I1, p.c_aber, b.tw, b.phase, b.amp, b.zph, b.fields + (size_t)g0 * FF);
+                b.I1, p.c_aber, b.tw, b.phase, b.amp, b.zph, b.fields + (size_t)g0 * FF, b.phase_sum);
         }
         if (!p.c_aber) continue;
         const float* unw = b.phase;
@@ -689,13 +683,11 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
         } else if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                k_volkov_rows<L><<<dim3(F / (2 * RC::P), m), RC::NT, sm_vrows, c->stream>>>(b.phase, b.zph, b.tw,
-                                                                                                     b.gx);
+                k_volkov_rows<L><<<dim3(F / RC::B, m), RC::NT, sm_vrows, c->stream>>>(b.zph, b.tw, b.gx);
             }
             {
                 Launch l(c, K_VOLKOV_COLS);
-                k_volkov_cols<L><<<dim3(F / (2 * VC::P), m), VC::NT, sm_vcols, c->stream>>>(b.phase, b.zph, b.gx,
-                                                                                                     b.tw, b.qc);
+                k_volkov_cols<L><<<dim3(F / VC::NC, m), VC::NT, sm_vcols, c->stream>>>(b.zph, b.gx, b.tw, b.qc);
             }
             float* urows = reinterpret_cast<float*>(b.tq);
             {
@@ -704,8 +696,8 @@ int fields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrappe
             }
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
-                k_volkov_integ_cols<F><<<dim3(F / IC::R, m), IC::NT, IC::SMEM, c->stream>>>(urows, b.phase, b.tw,
-                                                                                              b.unwrapped);
+                k_volkov_integ_cols<F><<<dim3(F / IC::R, m), IC::NT, IC::SMEM, c->stream>>>(
+                    urows, b.phase_sum, F / FC::B, b.tw, b.unwrapped);
             }
             unw = b.unwrapped;
         }

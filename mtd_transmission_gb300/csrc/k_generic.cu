@@ -29,6 +29,7 @@
 #include "cap_geometry.cuh"
 #include "form.cuh"
 #include "argmax.cuh"
+#include "phase_mean.cuh"
 
 namespace tdm {
 namespace {
@@ -133,11 +134,13 @@ gk_field_rows(const float2* __restrict__ spectra, const float4* __restrict__ arg
     for (int k = lane; k < F; k += 32) dst[k] = A[k];
 }
 
-// mode 1: phase/amplitude/phasor (C_ABER); mode 0: the field itself.
+// mode 1: phase/amplitude/phasor (C_ABER) and the CTA's sum of the wrapped
+// phase in psum[a * kPhaseParts + blockIdx.x]; mode 0: the field itself.
 template <int F>
 __global__ void __launch_bounds__(kCols * 32)
 gk_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict__ wq, float* __restrict__ phase,
-              float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields) {
+              float* __restrict__ amp, float2* __restrict__ zph, float2* __restrict__ fields,
+              double* __restrict__ psum) {
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, x0 = blockIdx.x * kCols;
@@ -153,6 +156,7 @@ gk_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict_
     __syncthreads();
     if (x0 + w < F) gfft<F, +1, 4 * F>(sm + w * 2 * F, sm + w * 2 * F + F, wq, lane);
     __syncthreads();
+    float acc = 0.0f;
     for (int i = threadIdx.x; i < kCols * F; i += blockDim.x) {
         const int t = i % kCols, y = i / kCols;
         if (x0 + t >= F) continue;
@@ -161,96 +165,77 @@ gk_field_cols(const float2* __restrict__ I1, int mode, const float2* __restrict_
         const size_t o = ((size_t)a * F + yo) * F + xo;
         if (mode) {
             const float m = hypotf(u.x, u.y);
-            phase[o] = atan2f(u.y, u.x);
+            const float ph = atan2f(u.y, u.x);
+            phase[o] = ph;
+            acc += ph;
             amp[o] = m;
             zph[o] = m > 0.0f ? make_float2(u.x / m, u.y / m) : make_float2(1.0f, 0.0f);
         } else {
             fields[o] = u;
         }
     }
+    if (mode) phase_sum_cta<kCols * 32>(acc, psum + (size_t)a * kPhaseParts + blockIdx.x);
 }
 
 // ---------------------------------------------------------------- Volkov unwrap
-// Pass 1: rows.  Per image row pair, three transforms (the phasor Z of each
-// row, and the two rows' phases packed as a + i b); the x derivative on the
-// mirror's right half gives gx = (Re(-i dZ/dx / Z) - dphi/dx) / 2pi.
-constexpr int kPairs = 2;  // row pairs per CTA: 3 kPairs warps
+// Pass 1: rows, one warp per image row: the x derivative of the phasor Z on
+// the mirror's right half gives gx = Re(-i dZ/dx / Z) / 2pi (the wrapped
+// phase's own gradient is not formed: k_fields.cu's Volkov notes).
+constexpr int kVRows = 8;  // rows (warps) per CTA
 template <int F>
-__global__ void __launch_bounds__(3 * kPairs * 32)
-gk_volkov_rows(const float* __restrict__ phase, const float2* __restrict__ zph, const float2* __restrict__ wq,
-               float* __restrict__ gxh) {
+__global__ void __launch_bounds__(kVRows * 32)
+gk_volkov_rows(const float2* __restrict__ zph, const float2* __restrict__ wq, float* __restrict__ gxh) {
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int a = blockIdx.y;
-    const bool zk = w < 2 * kPairs;
-    const int pair = zk ? w >> 1 : w - 2 * kPairs, ab = w & 1;
-    const int ya = 2 * (blockIdx.x * kPairs + pair);
-    const bool live = ya < F;  // warp-uniform
+    const int a = blockIdx.y, y = blockIdx.x * kVRows + w;
+    if (y >= F) return;  // warp-uniform; no CTA barrier below
     float2* A = sm + w * 2 * F;
     float2* B = A + F;
-    const size_t ra = ((size_t)a * F + ya) * F, rb = ra + F;
-    if (live) {
-        const float2* zr = zph + (ab ? rb : ra);
-        staged_copy<F, 32>(
-            lane,
-            [&](int m) {
-                const int x = gmirror_pos(m, F);
-                return zk ? zr[x] : make_float2(phase[ra + x], phase[rb + x]);
-            },
-            [&](int m, float2 v) { A[m] = v; });
-        __syncwarp();
-        gmirror_derivative<F>(A, B, wq, lane);
-    }
-    __syncthreads();
-    if (live && zk) {
-        const float2* zr = zph + (ab ? rb : ra);
-        const float2* q = sm + (2 * kPairs + pair) * 2 * F;
-        float* out = gxh + (ab ? rb : ra);
-        staged_copy<F, 32>(
-            lane, [&](int x) { return zr[x]; },
-            [&](int x, float2 z) {
-                const float2 g = A[x], qv = q[x];
-                const float ax = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y);  // Re(-i g / Z)
-                out[x] = (ax - (ab ? qv.y : qv.x)) * kInvTwoPiG;
-            });
-    }
+    const size_t row = ((size_t)a * F + y) * F;
+    const float2* zr = zph + row;
+    staged_copy<F, 32>(
+        lane, [&](int m) { return zr[gmirror_pos(m, F)]; }, [&](int m, float2 v) { A[m] = v; });
+    __syncwarp();
+    gmirror_derivative<F>(A, B, wq, lane);
+    float* out = gxh + row;
+    staged_copy<F, 32>(
+        lane, [&](int x) { return zr[x]; },
+        [&](int x, float2 z) {
+            const float2 g = A[x];
+            out[x] = (g.y * z.x - g.x * z.y) / (z.x * z.x + z.y * z.y) * kInvTwoPiG;  // Re(-i g / Z) / 2pi
+        });
 }
 
 // Pass 2: columns X = F + x of the mirror, kCols per CTA: the y derivatives
-// (kCols Z columns, kCols/2 packed phase pairs), gy, then the column's
+// of the kCols Z columns, gy = Re(-i dZ/dy / Z) / 2pi, then the column's
 // DCT-II of gx and DST-II of gy from one F-point transform of
 // gx + i (-1)^y gy permuted by gmirror_pos (k_fields.cu's column_dct_dst):
 // with V that transform and w = e^{-i pi k/2F},
 //     DCT-II(gx)[k] = Re(w V[k] + conj(w) V[F-k]) / 2,
 //     DST-II(gy)[k] = Re(w V[k] - conj(w) V[F-k]) / 2,
 // stored as cdct[ky][x] for ky in [0, F).
-// Three CTAs per SM (48 KB of shared memory each): registers capped at 56.
 template <int F>
-__global__ void __launch_bounds__((kCols + kCols / 2) * 32, 3)
-gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, const float* __restrict__ gxh,
-               const float2* __restrict__ wq, float2* __restrict__ cdct) {
+__global__ void __launch_bounds__(kCols * 32)
+gk_volkov_cols(const float2* __restrict__ zph, const float* __restrict__ gxh, const float2* __restrict__ wq,
+               float2* __restrict__ cdct) {
     constexpr int L = 2 * F, Q4 = 4 * F;
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, x0 = blockIdx.x * kCols;
     auto arr = [&](int t) { return sm + t * 2 * F; };  // warp t's pair of F-point arrays
-    constexpr int NT = (kCols + kCols / 2) * 32;
+    constexpr int NT = kCols * 32;
     staged_copy<kCols * F, NT>(
         threadIdx.x,
         [&](int i) {
             const size_t o = ((size_t)a * F + i / kCols) * F + x0 + i % kCols;
-            if (x0 + i % kCols >= F) return make_float3(0.f, 0.f, 0.f);
-            const float2 z = zph[o];
-            return make_float3(z.x, z.y, phase[o]);
+            return x0 + i % kCols < F ? zph[o] : make_float2(0.f, 0.f);
         },
-        [&](int i, float3 v) {
-            const int c = i % kCols, e = gslot(i / kCols, F);
-            if (x0 + c >= F) return;
-            arr(c)[e] = make_float2(v.x, v.y);
-            reinterpret_cast<float*>(&arr(kCols + (c >> 1))[e])[c & 1] = v.z;
+        [&](int i, float2 v) {
+            const int c = i % kCols;
+            if (x0 + c < F) arr(c)[gslot(i / kCols, F)] = v;
         });
     __syncthreads();
-    const bool live = x0 + (w < kCols ? w : 2 * (w - kCols)) < F;  // warp-uniform
+    const bool live = x0 + w < F;  // warp-uniform
     if (live) gmirror_derivative<F>(arr(w), arr(w) + F, wq, lane);
     __syncthreads();
     staged_copy<kCols * F, NT>(
@@ -264,9 +249,8 @@ gk_volkov_cols(const float* __restrict__ phase, const float2* __restrict__ zph, 
         [&](int i, float3 v) {
             const int c = i % kCols, y = i / kCols;
             if (x0 + c >= F) return;
-            const float2 g = arr(c)[y], q = arr(kCols + (c >> 1))[y];
-            const float ay = (g.y * v.x - g.x * v.y) / (v.x * v.x + v.y * v.y);
-            const float gy = (ay - ((c & 1) ? q.y : q.x)) * kInvTwoPiG;
+            const float2 g = arr(c)[y];
+            const float gy = (g.y * v.x - g.x * v.y) / (v.x * v.x + v.y * v.y) * kInvTwoPiG;
             arr(c)[F + gslot(y, F)] = make_float2(v.z, (y & 1) ? -gy : gy);
         });
     __syncthreads();
@@ -339,18 +323,21 @@ gk_volkov_integ_rows(const float2* __restrict__ cdct, const float2* __restrict__
     }
 }
 
-// Pass 4: column pairs: the DCT-III along y gives 2 pi IntM, and
-// phi + 2 pi IntM is stored with the columns fastest.  Three F-point arrays
-// per warp: the transform, its scratch and the column pair.
+// Pass 4: column pairs: the DCT-III along y gives the unwrapped phase less
+// its mean, and the wrapped phase's mean (from the field column pass's nps
+// sums) is added as it is stored with the columns fastest.  Three F-point
+// arrays per warp: the transform, its scratch and the column pair.
 template <int F>
 __global__ void __launch_bounds__(kCols * 32)
-gk_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ phase, const float2* __restrict__ wq,
-                     float* __restrict__ unwrapped) {
+gk_volkov_integ_cols(const float* __restrict__ urows, const double* __restrict__ psum, int nps,
+                     const float2* __restrict__ wq, float* __restrict__ unwrapped) {
     constexpr int L = 2 * F, Q4 = 4 * F, NC = 2 * kCols;
     extern __shared__ float2 sm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = blockIdx.y, c0 = blockIdx.x * NC;
     auto pair = [&](int t) { return sm + t * 3 * F + 2 * F; };  // warp t's column pair
+    __shared__ float s_mean;
+    if (threadIdx.x == 0) s_mean = phase_mean(psum + (size_t)a * kPhaseParts, nps, F);  // ordered by the barriers below
     staged_copy<NC * F, kCols * 32>(
         threadIdx.x,
         [&](int i) {
@@ -375,17 +362,12 @@ gk_volkov_integ_cols(const float* __restrict__ urows, const float* __restrict__ 
         for (int m = lane; m < F; m += 32) X[gmirror_pos(m, F)] = A[m];
     }
     __syncthreads();
-    staged_copy<NC * F, kCols * 32>(
-        threadIdx.x,
-        [&](int i) {
-            const size_t o = ((size_t)a * F + i / NC) * F + c0 + i % NC;
-            return c0 + i % NC < F ? phase[o] : 0.f;
-        },
-        [&](int i, float ph) {
-            const int t = i % NC, y = i / NC;
-            if (c0 + t < F)
-                unwrapped[((size_t)a * F + y) * F + c0 + t] = ph + reinterpret_cast<const float*>(&pair(t >> 1)[y])[t & 1];
-        });
+    const float mean = s_mean;
+    for (int i = threadIdx.x; i < NC * F; i += kCols * 32) {
+        const int t = i % NC, y = i / NC;
+        if (c0 + t < F)
+            unwrapped[((size_t)a * F + y) * F + c0 + t] = mean + reinterpret_cast<const float*>(&pair(t >> 1)[y])[t & 1];
+    }
 }
 
 // ---------------------------------------------------------------- cap passes
@@ -479,7 +461,8 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
     Buffers& b = c->b;
     const size_t FF = (size_t)F * F;
     const size_t sm_rows = warp_arrays(F, kRows), sm_cols = warp_arrays(F, kCols);
-    const size_t sm_vrows = warp_arrays(F, 3 * kPairs), sm_vcols = warp_arrays(F, kCols + kCols / 2);
+    const size_t sm_vrows = warp_arrays(F, kVRows), sm_vcols = warp_arrays(F, kCols);
+    static_assert((F + kCols - 1) / kCols <= kPhaseParts, "phase sums per angle");
     const size_t sm_irows = (size_t)kRows * 3 * F * sizeof(float2), sm_icols = (size_t)kCols * 3 * F * sizeof(float2);
     if (allow_smem(gk_field_rows<F>, sm_rows) || allow_smem(gk_field_cols<F>, sm_cols) ||
         allow_smem(gk_volkov_rows<F>, sm_vrows) || allow_smem(gk_volkov_cols<F>, sm_vcols) ||
@@ -497,8 +480,8 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
         }
         {
             Launch l(c, K_FIELD_COLS);
-            gk_field_cols<F><<<dim3(cols, m), kCols * 32, sm_cols, c->stream>>>(b.I1, p.c_aber, b.wq, b.phase, b.amp,
-                                                                                b.zph, b.fields + (size_t)g0 * FF);
+            gk_field_cols<F><<<dim3(cols, m), kCols * 32, sm_cols, c->stream>>>(
+                b.I1, p.c_aber, b.wq, b.phase, b.amp, b.zph, b.fields + (size_t)g0 * FF, b.phase_sum);
         }
         if (!p.c_aber) continue;
         const float* unw = b.phase;
@@ -508,13 +491,12 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
         } else if (p.deroul) {
             {
                 Launch l(c, K_VOLKOV_ROWS);
-                gk_volkov_rows<F><<<dim3((F / 2 + kPairs - 1) / kPairs, m), 3 * kPairs * 32, sm_vrows, c->stream>>>(
-                    b.phase, b.zph, b.wq, b.gx);
+                gk_volkov_rows<F><<<dim3((F + kVRows - 1) / kVRows, m), kVRows * 32, sm_vrows, c->stream>>>(
+                    b.zph, b.wq, b.gx);
             }
             {
                 Launch l(c, K_VOLKOV_COLS);
-                gk_volkov_cols<F><<<dim3(cols, m), (kCols + kCols / 2) * 32, sm_vcols, c->stream>>>(
-                    b.phase, b.zph, b.gx, b.wq, b.qc);
+                gk_volkov_cols<F><<<dim3(cols, m), kCols * 32, sm_vcols, c->stream>>>(b.zph, b.gx, b.wq, b.qc);
             }
             float* urows = reinterpret_cast<float*>(b.tq);
             {
@@ -525,7 +507,7 @@ int gfields_impl(tdm_ctx* c, int a0, int n, float* dbg_phase, float* dbg_unwrapp
             {
                 Launch l(c, K_VOLKOV_INTEG_COLS);
                 gk_volkov_integ_cols<F><<<dim3((F + 2 * kCols - 1) / (2 * kCols), m), kCols * 32, sm_icols,
-                                          c->stream>>>(urows, b.phase, b.wq, b.unwrapped);
+                                          c->stream>>>(urows, b.phase_sum, (int)cols, b.wq, b.unwrapped);
             }
             unw = b.unwrapped;
         }

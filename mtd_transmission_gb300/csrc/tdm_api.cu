@@ -79,7 +79,7 @@ int dev_alloc(tdm_ctx* c, T** p, size_t count) {
 void free_all(tdm_ctx* c) {
     Buffers& b = c->b;
     void* ptrs[] = {b.tw, b.win_h, b.tuk_f, b.s_tab, b.s_tabf, b.wq, b.holo_stage, b.inter, b.spectra, b.posspec,
-                    b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.unwrapped, b.beta,
+                    b.specval, b.argpart, b.I1, b.phase, b.amp, b.zph, b.gx, b.qc, b.tq, b.phase_sum, b.unwrapped, b.beta,
                     b.fit_part, b.fit_done, b.fields, b.r1, b.rec_buf[0].val, b.rec_buf[0].z, b.rec_buf[1].val,
                     b.rec_buf[1].z, b.posspec_vol[0], b.posspec_vol[1], b.vol, b.out_re, b.out_im, b.out_otf,
                     b.out_cnt, b.samp_idx, b.samp_q, b.rinv, b.err, b.xv[0], b.xv[1], b.xv[2], b.xv[3],
@@ -362,6 +362,7 @@ int tdm_create(const tdm_geom* geom, int max_angles, tdm_ctx** out) {
     TRY(dev_alloc(c, &b.gx, CH * FF));
     TRY(dev_alloc(c, &b.qc, CH * L * F));
     TRY(dev_alloc(c, &b.tq, CH * L * F));
+    TRY(dev_alloc(c, &b.phase_sum, CH * kPhaseParts));
     TRY(dev_alloc(c, &b.unwrapped, CH * FF));
     TRY(dev_alloc(c, &b.beta, CH * 2 * kNC));
     TRY(dev_alloc(c, &b.fit_part, CH * 2 * 8 * kNC));
@@ -768,7 +769,7 @@ struct ChunkScratch {
     float4* argpart;
     float2 *I1, *zph, *qc, *tq, *r1;
     float *phase, *amp, *gx, *unwrapped, *fit_part;
-    double* beta;
+    double *beta, *phase_sum;
     unsigned* fit_done;
 };
 
@@ -778,14 +779,14 @@ static ChunkScratch scratch_at(const tdm_ctx* c, int s) {
     return ChunkScratch{b.inter + S * c->p.F * c->p.H, b.argpart + S * kArgPartsMax, b.I1 + S * FF, b.zph + S * FF,
                         b.qc + S * LF, b.tq + S * LF, b.r1 + S * FF, b.phase + S * FF, b.amp + S * FF,
                         b.gx + S * FF, b.unwrapped + S * FF, b.fit_part + S * 2 * 8 * kNC, b.beta + S * 2 * kNC,
-                        b.fit_done + S * 2};
+                        b.phase_sum + S * kPhaseParts, b.fit_done + S * 2};
 }
 
 static void use_scratch(tdm_ctx* c, const ChunkScratch& k) {
     Buffers& b = c->b;
     b.inter = k.inter, b.argpart = k.argpart, b.I1 = k.I1, b.zph = k.zph, b.qc = k.qc, b.tq = k.tq, b.r1 = k.r1;
     b.phase = k.phase, b.amp = k.amp, b.gx = k.gx, b.unwrapped = k.unwrapped, b.fit_part = k.fit_part;
-    b.beta = k.beta, b.fit_done = k.fit_done;
+    b.beta = k.beta, b.phase_sum = k.phase_sum, b.fit_done = k.fit_done;
 }
 
 // Per-angle stages of the pipeline, streamed by hologram chunk: for each

@@ -43,6 +43,10 @@ struct Params {
 };
 
 // Device buffers (all owned by the context).
+// Per-CTA sums of an angle's wrapped phase kept for the Volkov unwrap's mean
+// term (one per CTA of the field column pass).
+constexpr int kPhaseParts = 64;
+
 struct Buffers {
     float2* tw = nullptr;          // kTwTotal twiddles (twiddle_table)
     float2* win_h = nullptr;       // H, hologram window with sign (hologram_window)
@@ -62,8 +66,11 @@ struct Buffers {
     float* amp = nullptr;          // chunk x F*F
     float2* zph = nullptr;         // chunk x F*F unit phasor exp(i phase) (Volkov input)
     float* gx = nullptr;           // chunk x F*F (right half of the mirror's gx, per image row)
-    float2* qc = nullptr;          // chunk x L*F (FFT along y of Q, columns X >= F)
-    float2* tq = nullptr;          // chunk x L*F
+    float2* qc = nullptr;          // chunk x L*F: Volkov, F*F per angle: per column the DCT-II of gx and DST-II of gy;
+                                   // Herraez, sort scratch
+    float2* tq = nullptr;          // chunk x L*F: Volkov, F*F floats per angle: the Poisson solve's rows;
+                                   // Herraez, sort scratch
+    double* phase_sum = nullptr;   // chunk x kPhaseParts: the field column pass's per-CTA sums of the wrapped phase
     float* unwrapped = nullptr;    // chunk x F*F
     int* hz_rand = nullptr;        // VOLKOV 0: max_angles x (4F - 4) border rand() draws (crand_border_table)
     double* beta = nullptr;        // chunk x 2 x kNC
