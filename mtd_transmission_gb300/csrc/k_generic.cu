@@ -214,8 +214,9 @@ gk_volkov_rows(const float2* __restrict__ zph, const float2* __restrict__ wq, fl
 //     DCT-II(gx)[k] = Re(w V[k] + conj(w) V[F-k]) / 2,
 //     DST-II(gy)[k] = Re(w V[k] - conj(w) V[F-k]) / 2,
 // stored as cdct[ky][x] for ky in [0, F).
+// Four CTAs per SM: registers capped at 64 (uncapped, 80 and three CTAs ran slower).
 template <int F>
-__global__ void __launch_bounds__(kCols * 32)
+__global__ void __launch_bounds__(kCols * 32, 4)
 gk_volkov_cols(const float2* __restrict__ zph, const float* __restrict__ gxh, const float2* __restrict__ wq,
                float2* __restrict__ cdct) {
     constexpr int L = 2 * F, Q4 = 4 * F;

@@ -14,7 +14,8 @@ inverses (k_fields.cu: column_dct_dst in k_volkov_cols, k_volkov_integ_rows
 and k_volkov_integ_cols; k_generic.cu the same on the mixed-radix engine).
 The emulation below follows their pairing of bins k and F - k, their
 permutation of the samples and their packing of two real sequences per
-complex transform.
+complex transform.  The last test checks the identity that lets the kernels
+drop the wrapped phase's own gradient and add its mean instead.
 """
 from __future__ import annotations
 
@@ -125,3 +126,45 @@ def test_nyquist_terms_cancel():
         tam[0, 0] = 0.0
         out.append(np.real(np.fft.ifft2(tam))[F:, F:])
     assert np.abs(out[0] - out[1]).max() <= 1e-12 * np.abs(out[0]).max()
+
+
+def test_phase_gradient_term_is_the_phase_less_its_mean():
+    """deroul_volkov4_total_sym_paire forms gx = (Re(-i dZ/dx / Z) - dphi/dx) / 2pi
+    (and gy alike) on the even mirror, solves, and adds phi back.  The
+    solve inverts the spectral gradient exactly except at zero frequency,
+    which it sets to 0, so the phi terms contribute -(phi - mean phi): the
+    kernels solve for the phasor's gradient alone and add mean(phi)."""
+    F = 16
+    L = 2 * F
+    rng = np.random.default_rng(5)
+    true = np.cumsum(np.cumsum(rng.standard_normal((F, F)) * 0.8, 0), 1)
+    phi = np.angle(np.exp(1j * true))
+
+    def even(q):
+        return mirror(q, 1, 1)
+
+    k = np.arange(L)
+    kap = np.where(k < L // 2, k, k - L) / L
+
+    def dx(m):  # gradient_fft4 along x
+        return np.fft.ifft(np.fft.fft(m, axis=1) * 2j * np.pi * kap[None, :], axis=1)
+
+    def dy(m):
+        return np.fft.ifft(np.fft.fft(m, axis=0) * 2j * np.pi * kap[:, None], axis=0)
+
+    def solve(gx, gy):
+        kx, ky = kap[None, :], kap[:, None]
+        k2 = kx ** 2 + ky ** 2
+        k2[0, 0] = 1.0
+        t = -1j * (kx * np.fft.fft2(gx) + ky * np.fft.fft2(gy)) / (2 * np.pi * k2)
+        t[0, 0] = 0.0
+        return np.real(np.fft.ifft2(t))
+
+    Z = even(np.cos(phi)) + 1j * even(np.sin(phi))
+    pm = even(phi)
+    gxz, gyz = np.real(-1j * dx(Z) / Z) / (2 * np.pi), np.real(-1j * dy(Z) / Z) / (2 * np.pi)
+    gxp, gyp = np.real(dx(pm)) / (2 * np.pi), np.real(dy(pm)) / (2 * np.pi)
+    reference = pm + 2 * np.pi * solve(gxz - gxp, gyz - gyp)
+    kernels = pm.mean() + 2 * np.pi * solve(gxz, gyz)
+    assert np.abs(reference - kernels).max() <= 1e-12 * np.abs(reference).max()
+    assert abs(pm.mean() - phi.mean()) <= 1e-15 * F * F  # the mirror's mean is the quadrant's
