@@ -43,8 +43,7 @@ constexpr float kInvTwoPi = 0.15915494309189535f;
 
 template <class K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return max_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 

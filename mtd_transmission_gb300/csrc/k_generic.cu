@@ -61,8 +61,7 @@ __device__ __forceinline__ void staged_copy(int tid, Load&& load, Store&& store)
 
 template <class K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return max_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 __host__ __device__ constexpr int gmirror_pos(int m, int F) { return m < F / 2 ? 2 * m : 2 * (F - 1 - m) + 1; }

@@ -299,8 +299,7 @@ int launch_herraez(tdm_ctx* c, int a0, int m) {
     const size_t smem = hz_gather_smem(F);
     const bool shared = F <= 256 && smem <= kMaxSmemPerCta;  // uint16 parents
     if (!b.hz_rand) return TDM_EUNSUPPORTED;
-    if (shared && cudaFuncSetAttribute(k_hz_gather<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem) != cudaSuccess)
+    if (shared && max_dynamic_smem(reinterpret_cast<const void*>(k_hz_gather<uint16_t, true>), smem) != cudaSuccess)
         return TDM_ECUDA;
     {
         Launch l(c, K_HERRAEZ);

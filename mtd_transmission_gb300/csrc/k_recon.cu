@@ -31,8 +31,7 @@ namespace {
 
 template <class K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return max_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 template <int F>

@@ -4,6 +4,9 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "bulk_copy.cuh"
@@ -26,6 +29,19 @@ cudaEvent_t prof_event(tdm_ctx* c) {
     }
     cudaEvent_t e = nullptr;
     cudaEventCreate(&e);
+    return e;
+}
+
+cudaError_t max_dynamic_smem(const void* fn, size_t bytes) {
+    int dev = 0;
+    if (cudaError_t e = cudaGetDevice(&dev)) return e;
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> done;  // largest size set per kernel and device
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& have = done[{fn, dev}];
+    if (have >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) have = bytes;
     return e;
 }
 }  // namespace tdm
@@ -58,6 +74,7 @@ int cuda_fail(tdm_ctx* c, cudaError_t e, const char* what) {
     } while (0)
 
 bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
 
 bool is_device_ptr(const void* p) {
     if (!p) return false;

@@ -188,6 +188,12 @@ struct Launch {
         c->launches++;
     }
 };
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) of kernel fn on the current
+// device, made once per kernel, device and size (the launchers run per chunk,
+// and the attribute call costs host time on each).  It is set for any size:
+// a kernel's static shared memory counts against the default 48 KB too.
+cudaError_t max_dynamic_smem(const void* fn, size_t bytes);
+
 // Extraction of holograms [0, n) from device memory into spectra[a0, a0 + n).
 // With argmax = true (n at most one chunk), the column pass also leaves the
 // specular search's partial winners of each angle in b.argpart; the return
