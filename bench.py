@@ -51,14 +51,14 @@ def algorithmic_bytes(name, acq, hits_per_angle, band):
         "argmax": F * F * 8,
         "field_rows": F * F * 8 * 2,
         "field_cols": F * F * 8 + F * F * 4 * 2,
-        # phase and phasor in, gx out
-        "volkov_rows": F * F * 4 + F * F * 8 + F * F * 4,
-        # phase, phasor and gx in; the columns' DCT-II of gx and DST-II of gy out
-        "volkov_cols": F * F * 4 + F * F * 8 + F * F * 4 + F * F * 8,
+        # phasor in, gx out
+        "volkov_rows": F * F * 8 + F * F * 4,
+        # phasor and gx in; the columns' DCT-II of gx and DST-II of gy out
+        "volkov_cols": F * F * 8 + F * F * 4 + F * F * 8,
         # those in, one real row of the Poisson solve's DCT-III along x out
         "volkov_integ_rows": F * F * 8 + F * F * 4,
-        # that and the wrapped phase in, the unwrapped phase out
-        "volkov_integ_cols": F * F * 4 * 3,
+        # that in, the unwrapped phase out
+        "volkov_integ_cols": F * F * 4 * 2,
         "aber_fit": 2 * F * F * 4,
         "form": 3 * F * F * 4 + F * F * 8,
         "cap_rows": 2 * F * F * 8,

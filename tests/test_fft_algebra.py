@@ -7,8 +7,8 @@ transforms, restated in numpy on the CPU (no GPU).
 - The holder of bin N - k (used to pair bins k and -k by a lane shuffle).
 - mirror_derivative: the spectral derivative of the 2F-point even mirror of a
   row from two F-point transforms of the row permuted by mirror_pos.
-- symmetric_fft: the 2F-point FFT of a column with Q[2F-1-Y] = conj(Q[Y])
-  from one F-point transform.
+- column_dct_dst: a column's DCT-II of gx and DST-II of gy from one F-point
+  transform of gx + i (-1)^y gy permuted by mirror_pos.
 """
 from __future__ import annotations
 
@@ -104,29 +104,20 @@ def test_mirror_derivative(F):
     assert np.abs(got - ref[F:]).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("F", [64, 128, 256, 512])
-def test_symmetric_fft(F):
+@pytest.mark.parametrize("F", [64, 128, 250, 256, 512])
+def test_column_dct_dst(F):
     rng = np.random.default_rng(F + 2)
-    L = 2 * F
-    u = rng.standard_normal(F) + 1j * rng.standard_normal(F)   # Q[F + y]
-    Q = np.empty(L, complex)
-    Q[F:] = u
-    Q[:F] = np.conj(u[::-1])                                      # Q[2F-1-Y] = conj(Q[Y])
-    ref = np.fft.fft(Q)
+    a, b = rng.standard_normal(F), rng.standard_normal(F)
     y = np.arange(F)
-    v_in = u.real + 1j * ((-1.0) ** y) * u.imag                   # a + i (-1)^y b, placed at slot(y)
+    k = np.arange(F)[:, None]
+    dct = (a[None, :] * np.cos(np.pi * k * (2 * y + 1) / (2 * F))).sum(1)
+    dst = (b[None, :] * np.sin(np.pi * k * (2 * y + 1) / (2 * F))).sum(1)
     m = np.arange(F)
-    V = np.fft.fft(v_in[mirror_pos(m, F)])
-    out = np.empty(L, complex)
-    for k in range(F):
-        w = np.exp(-1j * np.pi * k / L)
-        A, B = w * V[k], np.conj(w) * V[(F - k) % F]
-        ck, cf = 0.5 * (A.real + B.real), 0.5 * (A.real - B.real)
-        sg = -2.0 if k & 1 else 2.0
-        if k == 0:
-            out[0] = 2 * ck
-            out[F] = 1j * (A.imag + B.imag)
-        else:
-            out[k] = sg * (ck + cf) * np.conj(w)
-            out[L - k] = -sg * (cf - ck) * w
-    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+    V = np.fft.fft((a + 1j * ((-1.0) ** y) * b)[mirror_pos(m, F)])
+    kk = np.arange(F)
+    w = np.exp(-1j * np.pi * kk / (2 * F))
+    A, B = w * V, np.conj(w) * V[(F - kk) % F]
+    ck, cf = 0.5 * (A.real + B.real), 0.5 * (A.real - B.real)
+    scale = np.abs(a).sum() + np.abs(b).sum()
+    assert np.abs(ck - dct).max() <= 1e-12 * scale
+    assert np.abs(cf - dst).max() <= 1e-12 * scale
