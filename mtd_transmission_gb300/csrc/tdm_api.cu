@@ -617,6 +617,18 @@ static int stage_slots(const tdm_ctx* c) {
 static uint8_t* stage_slot(tdm_ctx* c, int s) {
     return c->b.holo_stage + (size_t)s * c->holo_chunk * c->p.H * c->p.H * 2;
 }
+// Chunks per hologram upload in the pipeline: up to 4 consecutive staging
+// slots take one copy (a divisor of the ring's slot count, and at most a
+// quarter of the ring, so later groups' uploads overlap the earlier ones'
+// extraction).  Uploads of about 33 MB (one 16-hologram chunk of 1024^2) ran
+// the host link at 260 GB/s with the volumes' downloads in flight, against
+// 340 GB/s for uploads of 126 MB or more; groups of 8 chunks did worse in
+// the pipeline than groups of 4.
+static int upload_group(int nslot) {
+    for (int g = std::min(4, nslot / 4); g > 1; --g)
+        if (nslot % g == 0) return g;
+    return 1;
+}
 
 static int stage_extract(tdm_ctx* c, const void* holos, int bits, int n) {
     const Params& p = c->p;
@@ -821,7 +833,7 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
     const bool dev = is_device_ptr(holos);
     const int nchunks = (n + c->holo_chunk - 1) / c->holo_chunk;
     const int nl = std::max(1, std::min(std::min(c->lanes, kMaxLanes), std::min(c->chunk_cap / c->chunk, nchunks)));
-    const int nslot = stage_slots(c);
+    const int nslot = stage_slots(c), grp = upload_group(nslot);
     struct Restore {
         tdm_ctx* c;
         cudaStream_t main;
@@ -843,14 +855,18 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
         c->stream = lane ? c->lane_stream[lane - 1] : restore.main;
         use_scratch(c, lane_scratch[lane]);
         const void* src = static_cast<const char*>(holos) + h0 * per;
-        const int buf = k % nslot;
+        const int buf = k % nslot, buf0 = buf - buf % grp;  // the chunk's slot and its group's first
         if (!dev) {
-            uint8_t* dst = stage_slot(c, buf);
-            TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf], 0));  // no-op before its first record
-            TDM_CU(cudaMemcpyAsync(dst, src, m * per, cudaMemcpyHostToDevice, c->copy_stream));
-            TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
-            TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf], 0));
-            src = dst;
+            if (buf == buf0) {  // one upload for the group's chunks, into its consecutive slots
+                const int gm = std::min(grp, nchunks - k);
+                for (int q = 0; q < gm; ++q)
+                    TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf + q], 0));  // no-op before a first record
+                const size_t bytes = (size_t)std::min(gm * c->holo_chunk, n - h0) * per;
+                TDM_CU(cudaMemcpyAsync(stage_slot(c, buf), src, bytes, cudaMemcpyHostToDevice, c->copy_stream));
+                TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
+            }
+            TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf0], 0));
+            src = stage_slot(c, buf0) + (size_t)(buf - buf0) * c->holo_chunk * per;  // packed as on the host
         }
         // the extraction leaves the specular search's partial winners for the
         // field stage; with C_ABER the cap row pass forms the fields

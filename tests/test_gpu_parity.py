@@ -315,29 +315,33 @@ def test_autotune_keeps_results():
 def test_schedules_keep_results():
     """Every schedule (angles per chunk x chunks in flight, each chunk on its
     own stream and scratch slots) gives the same volume bit for bit, from
-    device holograms and from host holograms (the upload ring wraps around);
+    device holograms and from host holograms (uploaded several chunks per
+    copy into the staging ring, the last group partial), 16-bit and 8-bit;
     schedules beyond the buffers' capacity are refused."""
     import torch
     from mtd_transmission_gb300.api import TdmError
     acq, _, d = small_case("plain_512_born", M=40)
     D = acq.dim_final
-    h_holos = torch.from_numpy(np.ascontiguousarray(d["holos"])).pin_memory()
-    holos = h_holos.cuda()
+    stacks = []
+    for h in (np.ascontiguousarray(d["holos"]), np.ascontiguousarray((d["holos"] >> 4).astype(np.uint8))):
+        h_holos = torch.from_numpy(h).pin_memory()
+        stacks.append((h_holos.cuda(), h_holos))
     with Context(Geometry.from_acquisition(acq), 40) as ctx:
         ctx.set_mask(np.ascontiguousarray(d["mask"]))
-        ctx.set_schedule(16, 1)
-        re0 = torch.zeros((D, D, D), device="cuda")
-        im0 = torch.zeros_like(re0)
-        ctx.pipeline(holos, indice=re0, absorption=im0)
-        ctx.synchronize()
-        for chunk, lanes in ((4, 4), (8, 3), (8, 4), (16, 2), (32, 1), (5, 2)):
-            ctx.set_schedule(chunk, lanes)
-            for src in (holos, h_holos):
-                re = torch.zeros_like(re0)
-                im = torch.zeros_like(re0)
-                ctx.pipeline(src, indice=re, absorption=im)
-                ctx.synchronize()
-                assert torch.equal(re, re0) and torch.equal(im, im0), (chunk, lanes, src.is_cuda)
+        for holos, h_holos in stacks:
+            ctx.set_schedule(16, 1)
+            re0 = torch.zeros((D, D, D), device="cuda")
+            im0 = torch.zeros_like(re0)
+            ctx.pipeline(holos, indice=re0, absorption=im0)
+            ctx.synchronize()
+            for chunk, lanes in ((4, 4), (8, 3), (8, 4), (16, 2), (32, 1), (5, 2), (3, 2)):
+                ctx.set_schedule(chunk, lanes)
+                for src in (holos, h_holos):
+                    re = torch.zeros_like(re0)
+                    im = torch.zeros_like(re0)
+                    ctx.pipeline(src, indice=re, absorption=im)
+                    ctx.synchronize()
+                    assert torch.equal(re, re0) and torch.equal(im, im0), (chunk, lanes, src.is_cuda, src.dtype)
         for chunk, lanes in ((64, 3), (8, 9), (0, 1), (129, 1)):
             with pytest.raises(TdmError):
                 ctx.set_schedule(chunk, lanes)
