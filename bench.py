@@ -232,11 +232,12 @@ def max_over_ranks(values, world: int, device):
     return t.tolist()
 
 
-def host_link_probe(h_in, d_in, pairs_out, reps: int = 3, chunk: int = 32 << 20):
+def host_link_probe(h_in, d_in, pairs_out, reps: int = 3, chunk: int = 128 << 20):
     """Copy throughput of the host link with the step's own pinned buffers:
     h_in -> d_in alone, the (device, host) pairs_out device -> host alone, and
-    both at once on two streams; 32 MB copies, as the pipeline's uploads are,
-    best of reps.  GB/s (1e9 bytes/s)."""
+    both at once on two streams; 128 MB copies, about the size of the
+    pipeline's grouped uploads (four 16-hologram chunks), best of reps.
+    GB/s (1e9 bytes/s)."""
     import torch
     src = h_in.view(-1).view(torch.uint8)
     dst = d_in.view(-1).view(torch.uint8)
