@@ -620,10 +620,10 @@ static uint8_t* stage_slot(tdm_ctx* c, int s) {
 // Chunks per hologram upload in the pipeline: up to 4 consecutive staging
 // slots take one copy (a divisor of the ring's slot count, and at most a
 // quarter of the ring, so later groups' uploads overlap the earlier ones'
-// extraction).  Uploads of about 33 MB (one 16-hologram chunk of 1024^2) ran
-// the host link at 260 GB/s with the volumes' downloads in flight, against
-// 340 GB/s for uploads of 126 MB or more; groups of 8 chunks did worse in
-// the pipeline than groups of 4.
+// extraction).  With the volumes' downloads in flight, uploads of one
+// 16-hologram chunk of 1024^2 (33 MB) kept the host link well below the rate
+// it reaches in both directions at once with uploads of 126 MB or more;
+// groups of 8 chunks did no better in the pipeline than groups of 4.
 static int upload_group(int nslot) {
     for (int g = std::min(4, nslot / 4); g > 1; --g)
         if (nslot % g == 0) return g;
