@@ -857,16 +857,22 @@ static int stage_angles(tdm_ctx* c, const void* holos, int bits, int n) {
         const void* src = static_cast<const char*>(holos) + h0 * per;
         const int buf = k % nslot, buf0 = buf - buf % grp;  // the chunk's slot and its group's first
         if (!dev) {
-            if (buf == buf0) {  // one upload for the group's chunks, into its consecutive slots
-                const int gm = std::min(grp, nchunks - k);
-                for (int q = 0; q < gm; ++q)
+            // the upload that carries chunk k starts at chunk ks: a group's chunks
+            // go up in one copy, except that the call's first chunk goes alone
+            // (its extraction starts after one chunk, not a group)
+            const int ks = k < grp ? std::min(k, 1) : k - k % grp;
+            const size_t chunk_bytes = (size_t)c->holo_chunk * per;
+            uint8_t* dst = stage_slot(c, buf0) + (size_t)(buf - buf0) * chunk_bytes;  // packed as on the host
+            if (k == ks) {
+                const int cnt = std::min(k == 0 && grp > 1 ? 1 : grp - (k % grp), nchunks - k);
+                for (int q = 0; q < cnt; ++q)
                     TDM_CU(cudaStreamWaitEvent(c->copy_stream, c->ev_free[buf + q], 0));  // no-op before a first record
-                const size_t bytes = (size_t)std::min(gm * c->holo_chunk, n - h0) * per;
-                TDM_CU(cudaMemcpyAsync(stage_slot(c, buf), src, bytes, cudaMemcpyHostToDevice, c->copy_stream));
+                const size_t bytes = (size_t)std::min(cnt * c->holo_chunk, n - h0) * per;
+                TDM_CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->copy_stream));
                 TDM_CU(cudaEventRecord(c->ev_copy[buf], c->copy_stream));
             }
-            TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[buf0], 0));
-            src = stage_slot(c, buf0) + (size_t)(buf - buf0) * c->holo_chunk * per;  // packed as on the host
+            TDM_CU(cudaStreamWaitEvent(c->stream, c->ev_copy[ks % nslot], 0));
+            src = dst;
         }
         // the extraction leaves the specular search's partial winners for the
         // field stage; with C_ABER the cap row pass forms the fields
