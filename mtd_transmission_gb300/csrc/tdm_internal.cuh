@@ -191,7 +191,10 @@ struct Launch {
 // cudaFuncSetAttribute(MaxDynamicSharedMemorySize) of kernel fn on the current
 // device, made once per kernel, device and size (the launchers run per chunk,
 // and the attribute call costs host time on each).  It is set for any size:
-// a kernel's static shared memory counts against the default 48 KB too.
+// a kernel's static shared memory counts against the default 48 KB too.  The
+// attribute belongs to the function, shared by every context on the device,
+// so it is only ever raised: a context of another geometry asking for less
+// must not lower it under a launch (or a captured graph) that needs more.
 cudaError_t max_dynamic_smem(const void* fn, size_t bytes);
 
 // Extraction of holograms [0, n) from device memory into spectra[a0, a0 + n).
